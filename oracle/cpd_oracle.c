@@ -1,0 +1,771 @@
+/*
+ * cpd_oracle.c -- TEST INFRASTRUCTURE ONLY (see cpd_oracle.h).
+ *
+ * Double-precision restatement of the reference's 2-D compound-prism
+ * spectrometer model and CPU fitness estimator. Build with -ffp-contract=off:
+ * every fused multiply-add below is an explicit fma() at a site where the Rust
+ * source calls `mul_add` (scalar mul_add, or the std SimdVector mul_add which is
+ * `Simd::mul_add`, fused, src/spectrometer/vector.rs:497-503). Dot products are
+ * the un-fused `hadamard_product(..).reduce_sum()` of vector.rs:281-283.
+ * Citations are paths inside the reference project.
+ */
+#include "cpd_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct { double x, y; } v2;
+
+static v2 v2_make(double x, double y) { v2 r = {x, y}; return r; }
+static v2 v2_add(v2 a, v2 b) { return v2_make(a.x + b.x, a.y + b.y); }
+static v2 v2_sub(v2 a, v2 b) { return v2_make(a.x - b.x, a.y - b.y); }
+static v2 v2_scale(v2 a, double s) { return v2_make(a.x * s, a.y * s); }
+static v2 v2_div(v2 a, double s) { return v2_make(a.x / s, a.y / s); }
+static v2 v2_neg(v2 a) { return v2_make(-a.x, -a.y); }
+/* Vector::dot = hadamard_product + reduce_sum (vector.rs:281-283, 489-495). */
+static double v2_dot(v2 a, v2 b) { return a.x * b.x + a.y * b.y; }
+/* SimdVector::mul_add: self * b + c fused per lane (vector.rs:497-503). */
+static v2 v2_fma(v2 a, double b, v2 c) { return v2_make(fma(a.x, b, c.x), fma(a.y, b, c.y)); }
+/* angled_xy / rot_180_xy / rot_90_xy / rot_90_ccw_xy (vector.rs:336-378). */
+static v2 v2_angled(double th) { return v2_make(cos(th), sin(th)); }
+static v2 v2_rot180(v2 a) { return v2_make(-a.x, -a.y); }
+static v2 v2_rot90(v2 a) { return v2_make(-a.y, a.x); }
+static v2 v2_rot90ccw(v2 a) { return v2_make(a.y, -a.x); }
+static double sqr(double x) { return x * x; }
+/* num_traits Float::fract = self - self.trunc(). */
+static double fractd(double x) { return x - trunc(x); }
+/* Float::is_sign_positive: true for +0 and positive values. */
+static int sign_positive(double x) { return !signbit(x); }
+
+/* ---------------------------------------------------------------- numerics */
+
+/* Shaw's rational inverse normal CDF, src/spectrometer/erf.rs:27-73.
+ * `polynomial` (erf.rs:8-16) is a Horner reduce with mul_add from the first
+ * (highest-degree) coefficient. */
+static const double SHAW_P[8] = {
+    4.3304513840364031401e-8, 0.000036313870818023761224, 0.0034424140686962222423,
+    0.085838533424158257377, 0.73176759583280610539, 2.3884158540184385711,
+    3.0333178251950406994, 1.2533141359896652729};
+static const double SHAW_Q[8] = {
+    1.3141263119543315917e-6, 0.00030617264753008793976, 0.014494272424798068406,
+    0.2168237095066675527, 1.2356513216582148689, 2.9373357991677046357,
+    2.9202373175993672857, 1.0};
+
+static double horner(const double *c, int n, double z)
+{
+    double s = c[0];
+    for (int i = 1; i < n; i++) s = fma(s, z, c[i]);
+    return s;
+}
+
+double orc_norminv(double x)
+{
+    double u = x > 0.5 ? 1.0 - x : x;
+    double v = -log(2.0 * u);
+    double p = horner(SHAW_P, 8, v);
+    double q = horner(SHAW_Q, 8, v);
+    return copysign(v * p / q, x - 0.5);
+}
+
+/* Glass::calc_n, src/spectrometer/glasscat.rs:17-22. */
+double orc_calc_n(const double coeffs[6], double w) { return horner(coeffs, 6, w); }
+
+/* Qrng 1-D: alpha = 1/phi (qrng.rs:156-158); next() = state.iadd_mod_1(alpha)
+ * = fract(state + alpha) (qrng.rs:217-219, 248-254). */
+static const double ORC_ALPHA = 1.0 / 1.61803398874989484820458683436563;
+
+void orc_qrng_points(double seed, size_t n, double *out)
+{
+    double st = seed;
+    for (size_t i = 0; i < n; i++) {
+        st = fractd(st + ORC_ALPHA);
+        out[i] = st;
+    }
+}
+
+/* Welford, src/spectrometer/welford.rs:5-57. */
+typedef struct { double count, mean, m2; } welford;
+
+static void wf_next(welford *w, double x)
+{
+    w->count += 1.0;
+    double delta = x - w->mean;
+    w->mean += delta / w->count;
+    double delta2 = x - w->mean;
+    w->m2 += delta * delta2;
+}
+
+static void wf_skip(welford *w, double new_count)
+{
+    if (w->count < new_count) {
+        double zero_count = new_count - w->count;
+        double count = new_count;
+        w->mean = (w->count * w->mean) / count;
+        w->m2 += sqr(w->mean) * w->count * zero_count / count;
+        w->count = count;
+    }
+}
+
+static int wf_sem_le(const welford *w, double err2)
+{
+    return w->m2 < err2 * (w->count * (w->count - 1.0));
+}
+
+/* FloatExt::plog2p, src/spectrometer/utils.rs:196-202. */
+static double plog2p(double p) { return p > 0.0 ? p * log2(p) : 0.0; }
+
+/* FloatExt::euclid_div_rem, utils.rs:177-192. */
+static void euclid_div_rem(double a, double b, double *q, double *r)
+{
+    double qq = trunc(a / b);
+    double rr = a - qq * b;
+    if (rr < 0.0) {
+        *q = b > 0.0 ? qq - 1.0 : qq + 1.0;
+        *r = rr + fabs(b);
+    } else {
+        *q = qq;
+        *r = rr;
+    }
+}
+
+/* Rust `f64 as u32`: saturating, NaN -> 0 (utils.rs:55-74 `v as $to`). */
+static uint32_t sat_u32(double q)
+{
+    if (!(q == q)) return 0;
+    if (q <= 0.0) return 0;
+    if (q >= 4294967295.0) return 4294967295u;
+    return (uint32_t)q;
+}
+
+/* ---------------------------------------------------------------- geometry */
+
+typedef struct { v2 point, normal; } hyperplane;
+
+typedef struct {
+    int nglass, ar_coated;
+    double glass[ORC_MAX_GLASS][6];
+    double height;
+    hyperplane planes[ORC_MAX_GLASS]; /* surface 0 .. G-1 (entry face + inner faces) */
+    /* CurvedPlane exit face: SphericalLikeSurface + RadialBounds (geometry.rs:280-315) */
+    v2 center;
+    double radius;
+    v2 bound_center;
+    double bound_r2;
+} prism;
+
+typedef struct {
+    uint32_t bin_count;
+    double bin_size, slope, intercept, min_ci, length;
+    v2 normal, position, direction;
+} detector;
+
+typedef struct {
+    prism cp;
+    detector det;
+    double wmin, wmax, beam_width, beam_y_mean;
+} spectrometer;
+
+/* create_joined_trapezoids, src/spectrometer/geometry.rs:430-489, and
+ * CompoundPrism::new (src/spectrometer/ray.rs:137-183) with the 2-D surface
+ * types of the pyo3 CompoundPrism (src/pylib.rs:690-754). */
+static int build_prism(const orc_spec *s, prism *cp)
+{
+    int G = s->nglass;
+    if (G < 1 || G > ORC_MAX_GLASS) return ORC_INVALID;
+    memset(cp, 0, sizeof(*cp));
+    cp->nglass = G;
+    cp->ar_coated = s->ar_coated;
+    cp->height = s->height;
+    memcpy(cp->glass, s->glass, sizeof(cp->glass));
+    double h2 = s->height * 0.5;
+    /* first face */
+    v2 normal = v2_rot180(v2_angled(s->angles[0]));
+    cp->planes[0].point = v2_make(fabs(normal.y / normal.x) * h2, h2);
+    cp->planes[0].normal = normal;
+    int prev_sign = sign_positive(normal.y);
+    double d1 = cp->planes[0].point.x;
+    double mx = cp->planes[0].point.x;
+    /* array_prepend(first_sep_length, sep_lengths) (utils.rs:5-12): inner face i uses
+     * lengths[i], the last face uses lengths[G-1]. Angles: inner faces angles[1..G-1],
+     * last face angles[G]. */
+    hyperplane last = {{0, 0}, {0, 0}};
+    for (int k = 1; k <= G; k++) {
+        double angle = s->angles[k];
+        double sep_len = s->lengths[k - 1];
+        v2 n = v2_rot180(v2_angled(angle));
+        int sign = sign_positive(n.y);
+        double d2 = fabs(n.y / n.x) * h2;
+        double sep_dist = sep_len + (prev_sign != sign ? d1 + d2 : fabs(d1 - d2));
+        prev_sign = sign;
+        d1 = d2;
+        mx += sep_dist;
+        hyperplane hp = {v2_make(mx, h2), n};
+        if (k < G) cp->planes[k] = hp;
+        else last = hp;
+    }
+    /* CurvedPlane::from_hyperplane, geometry.rs:283-314. */
+    double k_curv = s->curvature;
+    double chord = fabs(s->height / last.normal.x); /* sec_xy (vector.rs:392-397) */
+    double radius = chord * 0.5 / fabs(k_curv);
+    double apothem = sqrt(sqr(radius) - sqr(chord) * 0.25);
+    double sagitta = radius - apothem;
+    cp->center = v2_fma(last.normal, copysign(apothem, k_curv), last.point);
+    cp->radius = radius;
+    cp->bound_center = v2_fma(last.normal, -copysign(sagitta, k_curv), last.point);
+    cp->bound_r2 = sqr(sagitta) + sqr(chord) * 0.25;
+    return ORC_OK;
+}
+
+/* LinearDetectorArray::new, src/spectrometer/spectrometer.rs:183-219, with
+ * min_ci = cos(max_incident_angle) (src/pylib.rs:886). */
+static void build_detector(const orc_spec *s, detector *d)
+{
+    d->bin_count = s->bin_count;
+    d->bin_size = s->bin_size;
+    d->slope = s->linear_slope;
+    d->intercept = s->linear_intercept;
+    d->min_ci = cos(s->max_incident_angle);
+    d->length = s->det_length;
+    d->normal = v2_rot180(v2_angled(s->det_angle));
+    d->direction = s->det_flipped ? v2_rot90(d->normal) : v2_rot90ccw(d->normal);
+    d->position = v2_make(s->det_position[0], s->det_position[1]);
+}
+
+static int build_spectrometer(const orc_spec *s, spectrometer *sp)
+{
+    int e = build_prism(s, &sp->cp);
+    if (e) return e;
+    if (s->bin_count == 0) return ORC_INVALID;
+    build_detector(s, &sp->det);
+    sp->wmin = s->wmin;
+    sp->wmax = s->wmax;
+    sp->beam_width = s->beam_width;
+    sp->beam_y_mean = s->beam_y_mean;
+    return ORC_OK;
+}
+
+/* ---------------------------------------------------------------- ray trace */
+
+typedef struct { v2 origin, dir; double ts, tp; } ray;
+
+/* Ray::new_from_start (ray.rs:277-279). */
+static ray ray_start(double y)
+{
+    ray r = {{0.0, y}, {1.0, 0.0}, 1.0, 1.0};
+    return r;
+}
+
+/* HyperPlane::intersection with PrismBounds 2-D (geometry.rs:124-145, 62-67). */
+static int plane_intersect(const hyperplane *p, double height, const ray *r, double *dist)
+{
+    double ci = v2_dot(r->dir, p->normal);
+    if (ci == 0.0) return 0;
+    double d = v2_dot(v2_sub(p->point, r->origin), p->normal) / ci;
+    if (d >= 0.0) {
+        v2 h = v2_fma(r->dir, d, r->origin);
+        if (0.0 <= h.y && h.y <= height) {
+            *dist = d;
+            return 1;
+        }
+    }
+    return 0;
+}
+
+/* SphericalLikeSurface::intersection + RadialBounds (geometry.rs:161-216, 85-91). */
+static int curved_intersect(const prism *cp, const ray *r, double *dist, v2 *normal)
+{
+    v2 delta = v2_sub(r->origin, cp->center);
+    double ud = v2_dot(r->dir, delta);
+    double disc = sqr(ud) - v2_dot(delta, delta) + sqr(cp->radius);
+    if (!(disc > 0.0)) return 0; /* tangent and none are misses */
+    double sd = sqrt(disc);
+    double d1 = -ud - sd, d2 = -ud + sd;
+    v2 p1 = v2_fma(r->dir, d1, r->origin);
+    v2 p2 = v2_fma(r->dir, d2, r->origin);
+    double dd;
+    v2 p;
+    if (sign_positive(d1) && v2_dot(v2_sub(p1, cp->bound_center), v2_sub(p1, cp->bound_center)) <= cp->bound_r2) {
+        dd = d1;
+        p = p1;
+    } else if (sign_positive(d2) &&
+               v2_dot(v2_sub(p2, cp->bound_center), v2_sub(p2, cp->bound_center)) <= cp->bound_r2) {
+        dd = d2;
+        p = p2;
+    } else {
+        return 0;
+    }
+    *dist = dd;
+    *normal = v2_div(v2_sub(cp->center, p), cp->radius);
+    return 1;
+}
+
+/* Ray::refract (ray.rs:309-367). */
+static int refract(ray *r, v2 normal, double n1, double n2, int ar_coated)
+{
+    double ci = -v2_dot(r->dir, normal);
+    double rr = n1 / n2;
+    double cr_sq = 1.0 - sqr(rr) * (1.0 - sqr(ci));
+    if (cr_sq < 0.0) return ORC_TOTAL_INTERNAL_REFLECTION;
+    double cr = sqrt(cr_sq);
+    v2 v = v2_add(v2_scale(r->dir, rr), v2_scale(normal, rr * ci - cr));
+    double ts, tp;
+    if (ar_coated && ci > 0.5) {
+        ts = r->ts * 0.99;
+        tp = r->tp * 0.99;
+    } else {
+        double rs = sqr((n1 * ci - n2 * cr) / (n1 * ci + n2 * cr));
+        double rp = sqr((n1 * cr - n2 * ci) / (n1 * cr + n2 * ci));
+        ts = r->ts * (1.0 - rs);
+        tp = r->tp * (1.0 - rp);
+    }
+    r->dir = v;
+    r->ts = ts;
+    r->tp = tp;
+    return ORC_OK;
+}
+
+/* surface_propagate (ray.rs:370-382): intersect, translate (ray.rs:281-294, a
+ * fused mul_add), refract. */
+static int plane_propagate(ray *r, const hyperplane *p, double height, double n1, double n2, int ar)
+{
+    double d;
+    if (!plane_intersect(p, height, r, &d)) return ORC_NO_SURFACE_INTERSECTION;
+    r->origin = v2_fma(r->dir, d, r->origin);
+    return refract(r, p->normal, n1, n2, ar);
+}
+
+static int curved_propagate(ray *r, const prism *cp, double n1, double n2, int ar)
+{
+    double d;
+    v2 normal;
+    if (!curved_intersect(cp, r, &d, &normal)) return ORC_NO_SURFACE_INTERSECTION;
+    r->origin = v2_fma(r->dir, d, r->origin);
+    return refract(r, normal, n1, n2, ar);
+}
+
+/* CompoundPrism::propagate (ray.rs:485-499): air -> glass0 -> ... -> glass(G-1) -> air. */
+static int prism_propagate(const prism *cp, ray *r, double w)
+{
+    double n1 = orc_calc_n(cp->glass[0], w);
+    int e = plane_propagate(r, &cp->planes[0], cp->height, 1.0, n1, cp->ar_coated);
+    if (e) return e;
+    for (int k = 1; k < cp->nglass; k++) {
+        double n2 = orc_calc_n(cp->glass[k], w);
+        e = plane_propagate(r, &cp->planes[k], cp->height, n1, n2, cp->ar_coated);
+        if (e) return e;
+        n1 = n2;
+    }
+    return curved_propagate(r, cp, n1, 1.0, cp->ar_coated);
+}
+
+/* Ray::intersect_detector_array (ray.rs:390-402) with
+ * LinearDetectorArray::{intersection, bin_index} (spectrometer.rs:265-303). */
+static int detector_hit(const detector *dt, const ray *r, v2 *pos_out, uint32_t *bin, double *t)
+{
+    double ci = -v2_dot(r->dir, dt->normal);
+    if (ci <= dt->min_ci) return ORC_ANGULAR_RESPONSE_TOO_WEAK;
+    double d = v2_dot(v2_sub(r->origin, dt->position), dt->normal) / ci;
+    v2 p = v2_fma(r->dir, d, r->origin);
+    if (pos_out) *pos_out = p;
+    double pos = v2_dot(v2_sub(p, dt->position), dt->direction);
+    if (pos < 0.0 || dt->length < pos) return ORC_NO_SURFACE_INTERSECTION;
+    double q, rem;
+    euclid_div_rem(pos - dt->intercept, dt->slope, &q, &rem);
+    uint32_t b = sat_u32(q);
+    if (b < dt->bin_count && rem < dt->bin_size) {
+        *bin = b;
+        *t = (r->ts + r->tp) * 0.5; /* average_transmittance (ray.rs:297-299) */
+        return ORC_OK;
+    }
+    return ORC_NO_SURFACE_INTERSECTION;
+}
+
+/* GaussianBeam 2-D inverse_cdf (spectrometer.rs:26-30). */
+static double beam_y(const spectrometer *sp, double u)
+{
+    return sp->beam_y_mean - sp->beam_width * orc_norminv(u);
+}
+
+/* UniformDistribution::inverse_cdf (distribution.rs:32-34). */
+static double sample_wavelength(const spectrometer *sp, double u)
+{
+    return sp->wmin + (sp->wmax - sp->wmin) * u;
+}
+
+/* Spectrometer::propagate (spectrometer.rs:421-427). */
+static int spec_propagate(const spectrometer *sp, double y, double w, uint32_t *bin, double *t)
+{
+    ray r = ray_start(y);
+    int e = prism_propagate(&sp->cp, &r, w);
+    if (e) return e;
+    return detector_hit(&sp->det, &r, NULL, bin, t);
+}
+
+/* size_and_deviation + mid_pt (spectrometer.rs:429-437, 305-308). */
+static void size_and_deviation(const spectrometer *sp, double *size, double *dev)
+{
+    v2 mid = v2_fma(sp->det.direction, sp->det.length * 0.5, sp->det.position);
+    double dx = mid.x;
+    double dy = mid.y - sp->beam_y_mean;
+    v2 dv = v2_make(dx, dy);
+    double sz = sqrt(v2_dot(dv, dv));
+    *size = sz;
+    *dev = fabs(dv.y / sz);
+}
+
+/* ------------------------------------------------------ detector positioning */
+
+/* fit_ray_difference_surface (geometry.rs:495-542). */
+static int fit_ray_difference_surface(const ray *lower, const ray *upper, double d_length,
+                                      double d_angle, v2 *vertex, int32_t *flipped)
+{
+    v2 spec_dir = v2_rot90(v2_angled(d_angle));
+    v2 spec = v2_scale(spec_dir, d_length);
+    double a = upper->dir.x, b = -lower->dir.x, c = upper->dir.y, d = -lower->dir.y;
+    double det = a * d - b * c;
+    if (det == 0.0) return 0;
+    double i10 = -c / det, i11 = a / det;
+    v2 temp = v2_add(v2_sub(spec, upper->origin), lower->origin);
+    double d2 = i10 * temp.x + i11 * temp.y;
+    if (d2 > 0.0) {
+        *vertex = v2_fma(lower->dir, d2, lower->origin);
+        *flipped = 0;
+        return 1;
+    }
+    temp = v2_add(v2_sub(v2_neg(spec), upper->origin), lower->origin);
+    d2 = i10 * temp.x + i11 * temp.y;
+    if (d2 < 0.0) return 0;
+    *vertex = v2_fma(lower->dir, d2, lower->origin);
+    *flipped = 1;
+    return 1;
+}
+
+int orc_position_detector(const orc_spec *s, double acceptance, double pos_out[2], int32_t *flipped_out)
+{
+    prism cp;
+    int e = build_prism(s, &cp);
+    if (e) return e;
+    spectrometer sp;
+    sp.wmin = s->wmin;
+    sp.wmax = s->wmax;
+    /* detector_array_positioning, spectrometer.rs:322-364 */
+    ray r0 = ray_start(s->beam_y_mean);
+    double unaccepted_halved = fmax(1.0 - acceptance, 0.0) * 0.5;
+    double wmin = sample_wavelength(&sp, unaccepted_halved);
+    double wmax = sample_wavelength(&sp, 1.0 - unaccepted_halved);
+    ray lower = r0, upper = r0;
+    e = prism_propagate(&cp, &lower, wmin);
+    if (e) return e;
+    e = prism_propagate(&cp, &upper, wmax);
+    if (e) return e;
+    if ((lower.ts + lower.tp) * 0.5 <= 1e-3 || (upper.ts + upper.tp) * 0.5 <= 1e-3)
+        return ORC_ANGULAR_RESPONSE_TOO_WEAK;
+    v2 vtx;
+    if (!fit_ray_difference_surface(&lower, &upper, s->det_length, s->det_angle, &vtx, flipped_out))
+        return ORC_NO_SURFACE_INTERSECTION;
+    pos_out[0] = vtx.x;
+    pos_out[1] = vtx.y;
+    return ORC_OK;
+}
+
+/* ---------------------------------------------------------------- API */
+
+int orc_propagate(const orc_spec *s, double wavelength, double ray_u, uint32_t *bin, double *t)
+{
+    spectrometer sp;
+    int e = build_spectrometer(s, &sp);
+    if (e) return e;
+    return spec_propagate(&sp, beam_y(&sp, ray_u), wavelength, bin, t);
+}
+
+int orc_design_dump(const orc_spec *s, double *out)
+{
+    spectrometer sp;
+    int e = build_spectrometer(s, &sp);
+    if (e) return e;
+    int G = sp.cp.nglass, k = 0;
+    for (int i = 0; i < G; i++) {
+        out[k++] = sp.cp.planes[i].point.x;
+        out[k++] = sp.cp.planes[i].point.y;
+        out[k++] = sp.cp.planes[i].normal.x;
+        out[k++] = sp.cp.planes[i].normal.y;
+    }
+    out[k++] = sp.cp.center.x;
+    out[k++] = sp.cp.center.y;
+    out[k++] = sp.cp.radius;
+    out[k++] = sp.cp.bound_center.x;
+    out[k++] = sp.cp.bound_center.y;
+    out[k++] = sp.cp.bound_r2;
+    out[k++] = sp.det.normal.x;
+    out[k++] = sp.det.normal.y;
+    out[k++] = sp.det.direction.x;
+    out[k++] = sp.det.direction.y;
+    out[k++] = sp.det.min_ci;
+    size_and_deviation(&sp, &out[k], &out[k + 1]);
+    return ORC_OK;
+}
+
+int orc_propagation_path(const orc_spec *s, double wavelength, double initial_y, double *rows)
+{
+    spectrometer sp;
+    int e = build_spectrometer(s, &sp);
+    if (e) return -e;
+    const prism *cp = &sp.cp;
+    ray r = ray_start(initial_y);
+    int n = 0;
+#define ORC_ROW(rr)                  \
+    do {                             \
+        rows[4 * n + 0] = (rr).origin.x; \
+        rows[4 * n + 1] = (rr).origin.y; \
+        rows[4 * n + 2] = (rr).dir.x;    \
+        rows[4 * n + 3] = (rr).dir.y;    \
+        n++;                         \
+    } while (0)
+    /* propagate_trace (ray.rs:501-541) yields the start ray and each refracted ray
+     * until the first error; propagation_path (spectrometer.rs:439-464) then tries
+     * the detector with the last ray it yielded, whether or not the prism trace
+     * reached the exit face. */
+    ORC_ROW(r);
+    double n1 = orc_calc_n(cp->glass[0], wavelength);
+    ray nr0 = r;
+    int ok = plane_propagate(&nr0, &cp->planes[0], cp->height, 1.0, n1, cp->ar_coated) == ORC_OK;
+    if (ok) {
+        r = nr0;
+        ORC_ROW(r);
+    }
+    for (int k = 1; ok && k < cp->nglass; k++) {
+        double n2 = orc_calc_n(cp->glass[k], wavelength);
+        ray nr = r;
+        ok = plane_propagate(&nr, &cp->planes[k], cp->height, n1, n2, cp->ar_coated) == ORC_OK;
+        if (ok) {
+            r = nr;
+            ORC_ROW(r);
+        }
+        n1 = n2;
+    }
+    if (ok) {
+        ray nr = r;
+        if (curved_propagate(&nr, cp, n1, 1.0, cp->ar_coated) == ORC_OK) {
+            r = nr;
+            ORC_ROW(r);
+        }
+    }
+    v2 p;
+    uint32_t b;
+    double t;
+    if (detector_hit(&sp.det, &r, &p, &b, &t) == ORC_OK) {
+        ray last = r;
+        last.origin = p;
+        ORC_ROW(last);
+    }
+#undef ORC_ROW
+    return n;
+}
+
+/* vector_quasi_monte_carlo_integration + p_dets_l_wavelength (fitness.rs:5-34, 48-69). */
+static void p_dets_adaptive(const spectrometer *sp, double w, size_t max_m, welford *stats)
+{
+    uint32_t nbin = sp->det.bin_count;
+    const double max_err = 5e-3;
+    const double max_err_sq = max_err * max_err;
+    for (uint32_t i = 0; i < nbin; i++) stats[i].count = stats[i].mean = stats[i].m2 = 0.0;
+    double count = 0.0;
+    double st = 0.5;
+    for (size_t it = 0; it < max_m; it++) {
+        st = fractd(st + ORC_ALPHA);
+        count += 1.0;
+        uint32_t bin;
+        double t;
+        if (spec_propagate(sp, beam_y(sp, st), w, &bin, &t) == ORC_OK) {
+            wf_skip(&stats[bin], count);
+            wf_next(&stats[bin], t);
+            if (wf_sem_le(&stats[bin], max_err_sq)) break;
+        }
+    }
+    for (uint32_t i = 0; i < nbin; i++) wf_skip(&stats[i], count);
+}
+
+int orc_p_dets_l_wavelength(const orc_spec *s, double wavelength, size_t max_m, double *out)
+{
+    spectrometer sp;
+    int e = build_spectrometer(s, &sp);
+    if (e) return e;
+    welford *stats = calloc(sp.det.bin_count, sizeof(welford));
+    if (!stats) return ORC_INVALID;
+    p_dets_adaptive(&sp, wavelength, max_m, stats);
+    for (uint32_t i = 0; i < sp.det.bin_count; i++) out[i] = stats[i].mean;
+    free(stats);
+    return ORC_OK;
+}
+
+/* mutual_information + fitness (fitness.rs:79-147). */
+int orc_fitness_adaptive(const orc_spec *s, size_t max_n, size_t max_m, double out[3])
+{
+    spectrometer sp;
+    int e = build_spectrometer(s, &sp);
+    if (e) return e;
+    uint32_t nbin = sp.det.bin_count;
+    welford *p_dets = calloc(nbin, sizeof(welford));
+    welford *row = calloc(nbin, sizeof(welford));
+    if (!p_dets || !row) {
+        free(p_dets);
+        free(row);
+        return ORC_INVALID;
+    }
+    welford h_det_l_w = {0, 0, 0};
+    const double max_err_sqr = 5e-3 * 5e-3;
+    double st = 0.5;
+    for (size_t it = 0; it < max_n; it++) {
+        st = fractd(st + ORC_ALPHA);
+        double w = sample_wavelength(&sp, st);
+        p_dets_adaptive(&sp, w, max_m, row);
+        double h = 0.0;
+        for (uint32_t i = 0; i < nbin; i++) {
+            wf_next(&p_dets[i], row[i].mean);
+            h += plog2p(row[i].mean);
+        }
+        wf_next(&h_det_l_w, h);
+        int all = 1;
+        for (uint32_t i = 0; i < nbin; i++)
+            if (!wf_sem_le(&p_dets[i], max_err_sqr)) {
+                all = 0;
+                break;
+            }
+        if (all) break;
+    }
+    double h_det = 0.0;
+    for (uint32_t i = 0; i < nbin; i++) h_det = h_det + plog2p(p_dets[i].mean);
+    double size, dev;
+    size_and_deviation(&sp, &size, &dev);
+    out[0] = size;
+    out[1] = h_det_l_w.mean - h_det;
+    out[2] = dev;
+    free(p_dets);
+    free(row);
+    return ORC_OK;
+}
+
+/* --------------------------------------------- fixed-N on explicit point sets */
+
+typedef struct {
+    const spectrometer *sp;
+    const double *lam_u, *ys;
+    size_t W, R;
+    double *p;          /* W*B */
+    uint64_t hits;
+    size_t k0, k1;
+} fixed_job;
+
+static void *fixed_worker(void *arg)
+{
+    fixed_job *j = (fixed_job *)arg;
+    uint32_t B = j->sp->det.bin_count;
+    uint64_t hits = 0;
+    for (size_t k = j->k0; k < j->k1; k++) {
+        double w = sample_wavelength(j->sp, j->lam_u[k]);
+        double *row = j->p + k * B;
+        for (uint32_t b = 0; b < B; b++) row[b] = 0.0;
+        for (size_t r = 0; r < j->R; r++) {
+            uint32_t bin;
+            double t;
+            if (spec_propagate(j->sp, j->ys[r], w, &bin, &t) == ORC_OK) {
+                row[bin] += t;
+                hits++;
+            }
+        }
+        for (uint32_t b = 0; b < B; b++) row[b] = row[b] / (double)j->R;
+    }
+    j->hits = hits;
+    return NULL;
+}
+
+int orc_fitness_points(const orc_spec *s, const double *lam_u, size_t W, const double *ray_u,
+                       size_t R, int nthreads, double *p_out, double stats[4], uint64_t *hits_out)
+{
+    spectrometer sp;
+    int e = build_spectrometer(s, &sp);
+    if (e) return e;
+    if (W == 0 || R == 0) return ORC_INVALID;
+    uint32_t B = sp.det.bin_count;
+    double *p = p_out ? p_out : malloc(sizeof(double) * W * B);
+    double *ys = malloc(sizeof(double) * R);
+    if (!p || !ys) {
+        if (!p_out) free(p);
+        free(ys);
+        return ORC_INVALID;
+    }
+    for (size_t r = 0; r < R; r++) ys[r] = beam_y(&sp, ray_u[r]);
+    if (nthreads < 1) nthreads = 1;
+    if ((size_t)nthreads > W) nthreads = (int)W;
+    fixed_job *jobs = calloc((size_t)nthreads, sizeof(fixed_job));
+    pthread_t *th = calloc((size_t)nthreads, sizeof(pthread_t));
+    for (int i = 0; i < nthreads; i++) {
+        jobs[i].sp = &sp;
+        jobs[i].lam_u = lam_u;
+        jobs[i].ys = ys;
+        jobs[i].W = W;
+        jobs[i].R = R;
+        jobs[i].p = p;
+        jobs[i].k0 = W * (size_t)i / (size_t)nthreads;
+        jobs[i].k1 = W * (size_t)(i + 1) / (size_t)nthreads;
+    }
+    for (int i = 1; i < nthreads; i++) pthread_create(&th[i], NULL, fixed_worker, &jobs[i]);
+    fixed_worker(&jobs[0]);
+    uint64_t hits = jobs[0].hits;
+    for (int i = 1; i < nthreads; i++) {
+        pthread_join(th[i], NULL);
+        hits += jobs[i].hits;
+    }
+    /* mutual information over the W rows, in row order (fitness.rs:95-122). */
+    if (stats) {
+        double h_cond = 0.0;
+        double *pbar = calloc(B, sizeof(double));
+        for (size_t k = 0; k < W; k++) {
+            double h = 0.0;
+            for (uint32_t b = 0; b < B; b++) {
+                h += plog2p(p[k * B + b]);
+                pbar[b] += p[k * B + b];
+            }
+            h_cond += h;
+        }
+        h_cond /= (double)W;
+        double h_det = 0.0;
+        for (uint32_t b = 0; b < B; b++) h_det += plog2p(pbar[b] / (double)W);
+        double size, dev;
+        size_and_deviation(&sp, &size, &dev);
+        stats[0] = h_cond - h_det;
+        stats[1] = h_cond;
+        stats[2] = h_det;
+        stats[3] = size;
+        free(pbar);
+    }
+    if (hits_out) *hits_out = hits;
+    free(jobs);
+    free(th);
+    free(ys);
+    if (!p_out) free(p);
+    return ORC_OK;
+}
+
+int orc_trace_pairs(const orc_spec *s, const double *lam_u, const double *ray_u, size_t n,
+                    uint32_t *bins, double *ts)
+{
+    spectrometer sp;
+    int e = build_spectrometer(s, &sp);
+    if (e) return e;
+    for (size_t i = 0; i < n; i++) {
+        double w = sample_wavelength(&sp, lam_u[i]);
+        uint32_t b;
+        double t;
+        if (spec_propagate(&sp, beam_y(&sp, ray_u[i]), w, &b, &t) == ORC_OK) {
+            bins[i] = b;
+            ts[i] = t;
+        } else {
+            bins[i] = sp.det.bin_count;
+            ts[i] = 0.0;
+        }
+    }
+    return ORC_OK;
+}

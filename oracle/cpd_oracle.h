@@ -1,0 +1,115 @@
+/*
+ * cpd_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C, double-precision restatement of the compound-prism spectrometer
+ * fitness path of jdtatz/compound-prism-designer (Rust crate `src/`). It is the
+ * parity checker for the CUDA implementation and the timed CPU baseline. Only
+ * tests, the smoke check and the benchmark's CPU-baseline / reference legs may
+ * load it; the product library never links or calls it.
+ *
+ * Every function cites the reference file:line it restates. Arithmetic is
+ * compiled with -ffp-contract=off, and fma() is called exactly where the Rust
+ * source calls `mul_add` (Rust never contracts a*b+c on its own), so the
+ * results are the reference's own f64 results up to the last-ulp differences of
+ * libm's log/sin/cos.
+ *
+ * Parity pin: the known-design golden values of src/fitness.rs:250-257
+ * (size 41.3, info 0.7407, deviation 0.377159) and the Shaw inverse-normal
+ * accuracy points of src/spectrometer/erf.rs:142-161 (tests/test_oracle_golden.py).
+ */
+#ifndef CPD_ORACLE_H
+#define CPD_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAX_GLASS 6
+
+/* Error codes: the four RayTraceError variants of src/spectrometer/ray.rs:10-16. */
+enum {
+    ORC_OK = 0,
+    ORC_NO_SURFACE_INTERSECTION = 1,
+    ORC_OUT_OF_BOUNDS = 2,
+    ORC_TOTAL_INTERNAL_REFLECTION = 3,
+    ORC_ANGULAR_RESPONSE_TOO_WEAK = 4,
+    ORC_INVALID = 10
+};
+
+/* Flat spectrometer description, field for field what the pyo3 constructors take
+ * (src/pylib.rs: CompoundPrism 690-754, DetectorArray 864-902,
+ * UniformWavelengthDistribution 298-309, GaussianBeam 347-356). */
+typedef struct orc_spec {
+    int32_t nglass;                       /* G, 1..6 */
+    int32_t ar_coated;
+    double glass[ORC_MAX_GLASS][6];       /* Horner coefficients, highest degree first */
+    double angles[ORC_MAX_GLASS + 1];     /* G+1 face angles (radians) */
+    double lengths[ORC_MAX_GLASS];        /* G separation lengths */
+    double curvature;                     /* signed normalized curvature of the exit face */
+    double height, width;
+    /* detector array */
+    uint32_t bin_count;
+    int32_t det_flipped;
+    double bin_size, linear_slope, linear_intercept, det_length, max_incident_angle, det_angle;
+    double det_position[2];
+    /* source */
+    double wmin, wmax;                    /* UniformDistribution bounds (micrometres) */
+    double beam_width, beam_y_mean;       /* GaussianBeam */
+} orc_spec;
+
+/* Shaw inverse normal CDF (src/spectrometer/erf.rs:62-73). */
+double orc_norminv(double x);
+/* Horner glass polynomial (src/spectrometer/glasscat.rs:300-305). */
+double orc_calc_n(const double coeffs[6], double w);
+/* The reference CPU point set: Qrng::new_from_scalar(seed).take(n), i.e. the
+ * incremental R1 sequence state = fract(state + 1/phi) (src/spectrometer/qrng.rs:526-563). */
+void orc_qrng_points(double seed, size_t n, double *out);
+
+/* detector_array_positioning (src/spectrometer/spectrometer.rs:322-364). Uses
+ * only the prism fields, the source fields and det_length/det_angle of `s`. */
+int orc_position_detector(const orc_spec *s, double acceptance, double pos_out[2],
+                          int32_t *flipped_out);
+
+/* One ray: Spectrometer::propagate (spectrometer.rs:421-427) for the ray
+ * GaussianBeam::inverse_cdf([ray_u]) at wavelength `wavelength` (micrometres).
+ * Returns ORC_OK and (bin, t) or a RayTraceError code. */
+int orc_propagate(const orc_spec *s, double wavelength, double ray_u, uint32_t *bin, double *t);
+
+/* Geometry dump for table-equality tests: 2*(G) plane values (point x,y; normal x,y per plane),
+ * then curved (center x,y, radius, bound center x,y, bound radius^2),
+ * then detector (normal x,y, direction x,y, min_ci), then (size, deviation).
+ * Writes 4*G + 6 + 5 + 2 doubles. */
+int orc_design_dump(const orc_spec *s, double *out);
+
+/* Spectrometer::propagation_path (spectrometer.rs:439-464): writes up to
+ * (G+3) rows of (origin x, origin y, dir x, dir y); returns the row count. */
+int orc_propagation_path(const orc_spec *s, double wavelength, double initial_y, double *rows);
+
+/* fitness() (src/fitness.rs:130-147) with the reference's adaptive SEM stops.
+ * out = {size, info, deviation}. */
+int orc_fitness_adaptive(const orc_spec *s, size_t max_n, size_t max_m, double out[3]);
+
+/* p_dets_l_wavelength (src/fitness.rs:48-69) for one wavelength: writes bin_count means. */
+int orc_p_dets_l_wavelength(const orc_spec *s, double wavelength, size_t max_m, double *out);
+
+/* Fixed-N estimator on explicit point sets: wavelength u-points lam_u[W]
+ * (lambda = wmin + (wmax-wmin)*u) and ray u-points ray_u[R]. p(d|lambda) = sum(t)/R over
+ * all R rays (misses count as zeros, as the Welford `skip` of fitness.rs:30-32 does).
+ * p_out (optional, W*B), stats (optional, 4): {info, h_cond_mean, h_det, size}.
+ * hits_out (optional): total count of rays that reached a bin.
+ * nthreads <= 0 uses one thread. */
+int orc_fitness_points(const orc_spec *s, const double *lam_u, size_t W, const double *ray_u,
+                       size_t R, int nthreads, double *p_out, double stats[4], uint64_t *hits_out);
+
+/* Per-ray twin of propagation_test_kernel (src/spectrometer/kernel.rs:195-224) in f64:
+ * lambda = wmin + (wmax-wmin)*lam_u[i]; bin_count marks a lost ray. */
+int orc_trace_pairs(const orc_spec *s, const double *lam_u, const double *ray_u, size_t n,
+                    uint32_t *bins, double *ts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

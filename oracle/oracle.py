@@ -1,0 +1,208 @@
+"""ctypes loader for the C oracle -- TEST INFRASTRUCTURE ONLY.
+
+The oracle is a double-precision restatement of the reference's CPU fitness
+path (src/fitness.rs and src/spectrometer/*.rs of jdtatz/compound-prism-designer).
+Only tests, the smoke check and the benchmark's CPU-baseline/reference legs
+import this module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
+
+MAX_GLASS = 6
+(OK, NO_SURFACE_INTERSECTION, OUT_OF_BOUNDS, TOTAL_INTERNAL_REFLECTION,
+ ANGULAR_RESPONSE_TOO_WEAK) = range(5)
+INVALID = 10
+
+
+class OrcSpec(C.Structure):
+    _fields_ = [
+        ("nglass", C.c_int32),
+        ("ar_coated", C.c_int32),
+        ("glass", (C.c_double * 6) * MAX_GLASS),
+        ("angles", C.c_double * (MAX_GLASS + 1)),
+        ("lengths", C.c_double * MAX_GLASS),
+        ("curvature", C.c_double),
+        ("height", C.c_double),
+        ("width", C.c_double),
+        ("bin_count", C.c_uint32),
+        ("det_flipped", C.c_int32),
+        ("bin_size", C.c_double),
+        ("linear_slope", C.c_double),
+        ("linear_intercept", C.c_double),
+        ("det_length", C.c_double),
+        ("max_incident_angle", C.c_double),
+        ("det_angle", C.c_double),
+        ("det_position", C.c_double * 2),
+        ("wmin", C.c_double),
+        ("wmax", C.c_double),
+        ("beam_width", C.c_double),
+        ("beam_y_mean", C.c_double),
+    ]
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.check_call(["bash", os.path.join(HERE, "build.sh")])
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        dp = C.POINTER(C.c_double)
+        up = C.POINTER(C.c_uint32)
+        sp = C.POINTER(OrcSpec)
+        L.orc_norminv.restype = C.c_double
+        L.orc_norminv.argtypes = [C.c_double]
+        L.orc_calc_n.restype = C.c_double
+        L.orc_calc_n.argtypes = [dp, C.c_double]
+        L.orc_qrng_points.argtypes = [C.c_double, C.c_size_t, dp]
+        L.orc_position_detector.argtypes = [sp, C.c_double, dp, C.POINTER(C.c_int32)]
+        L.orc_propagate.argtypes = [sp, C.c_double, C.c_double, up, dp]
+        L.orc_design_dump.argtypes = [sp, dp]
+        L.orc_propagation_path.argtypes = [sp, C.c_double, C.c_double, dp]
+        L.orc_fitness_adaptive.argtypes = [sp, C.c_size_t, C.c_size_t, dp]
+        L.orc_p_dets_l_wavelength.argtypes = [sp, C.c_double, C.c_size_t, dp]
+        L.orc_fitness_points.argtypes = [sp, dp, C.c_size_t, dp, C.c_size_t, C.c_int, dp, dp,
+                                         C.POINTER(C.c_uint64)]
+        L.orc_trace_pairs.argtypes = [sp, dp, dp, C.c_size_t, up, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def make_spec(d: dict) -> OrcSpec:
+    """Fill an OrcSpec from the flat parameter dict used across the tests."""
+    s = OrcSpec()
+    G = len(d["glasses"])
+    s.nglass = G
+    s.ar_coated = int(bool(d["ar_coated"]))
+    for g, coeffs in enumerate(d["glasses"]):
+        for i, c in enumerate(coeffs):
+            s.glass[g][i] = float(c)
+    for i, a in enumerate(d["angles"]):
+        s.angles[i] = float(a)
+    for i, l in enumerate(d["lengths"]):
+        s.lengths[i] = float(l)
+    s.curvature = float(d["curvature"])
+    s.height = float(d["height"])
+    s.width = float(d["width"])
+    s.bin_count = int(d["bin_count"])
+    s.det_flipped = int(bool(d.get("det_flipped", False)))
+    s.bin_size = float(d["bin_size"])
+    s.linear_slope = float(d["linear_slope"])
+    s.linear_intercept = float(d["linear_intercept"])
+    s.det_length = float(d["det_length"])
+    s.max_incident_angle = float(d["max_incident_angle"])
+    s.det_angle = float(d["det_angle"])
+    pos = d.get("det_position", (0.0, 0.0))
+    s.det_position[0] = float(pos[0])
+    s.det_position[1] = float(pos[1])
+    s.wmin, s.wmax = (float(x) for x in d["wavelength_bounds"])
+    s.beam_width = float(d["beam_width"])
+    s.beam_y_mean = float(d["beam_y_mean"])
+    return s
+
+
+def norminv(x: float) -> float:
+    return lib().orc_norminv(float(x))
+
+
+def qrng_points(seed: float, n: int) -> np.ndarray:
+    out = np.empty(n, dtype=np.float64)
+    lib().orc_qrng_points(float(seed), n, _dp(out))
+    return out
+
+
+def position_detector(d: dict, acceptance: float = 1.0):
+    s = make_spec(d)
+    pos = np.zeros(2)
+    fl = C.c_int32(0)
+    e = lib().orc_position_detector(C.byref(s), float(acceptance), _dp(pos), C.byref(fl))
+    return e, (float(pos[0]), float(pos[1])), bool(fl.value)
+
+
+def design_dump(d: dict) -> np.ndarray:
+    s = make_spec(d)
+    G = len(d["glasses"])
+    out = np.zeros(4 * G + 6 + 5 + 2)
+    e = lib().orc_design_dump(C.byref(s), _dp(out))
+    assert e == OK, e
+    return out
+
+
+def propagate(d: dict, wavelength: float, ray_u: float):
+    s = make_spec(d)
+    b = C.c_uint32(0)
+    t = C.c_double(0.0)
+    e = lib().orc_propagate(C.byref(s), float(wavelength), float(ray_u), C.byref(b), C.byref(t))
+    return e, b.value, t.value
+
+
+def propagation_path(d: dict, wavelength: float, initial_y: float) -> np.ndarray:
+    s = make_spec(d)
+    G = len(d["glasses"])
+    rows = np.zeros((G + 3, 4))
+    n = lib().orc_propagation_path(C.byref(s), float(wavelength), float(initial_y), _dp(rows))
+    return rows[: max(n, 0)]
+
+
+def fitness_adaptive(d: dict, max_n: int = 16384, max_m: int = 16384):
+    s = make_spec(d)
+    out = np.zeros(3)
+    e = lib().orc_fitness_adaptive(C.byref(s), max_n, max_m, _dp(out))
+    assert e == OK, e
+    return float(out[0]), float(out[1]), float(out[2])
+
+
+def p_dets_l_wavelength(d: dict, wavelength: float, max_m: int = 16384) -> np.ndarray:
+    s = make_spec(d)
+    out = np.zeros(int(d["bin_count"]))
+    e = lib().orc_p_dets_l_wavelength(C.byref(s), float(wavelength), max_m, _dp(out))
+    assert e == OK, e
+    return out
+
+
+def fitness_points(d: dict, lam_u, ray_u, nthreads: int = 1, want_p: bool = True):
+    """Fixed-N estimator on explicit points. Returns (p[W,B] or None, stats dict)."""
+    s = make_spec(d)
+    lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
+    ray_u = np.ascontiguousarray(ray_u, dtype=np.float64)
+    W, R, B = lam_u.size, ray_u.size, int(d["bin_count"])
+    p = np.zeros((W, B)) if want_p else None
+    st = np.zeros(4)
+    hits = C.c_uint64(0)
+    e = lib().orc_fitness_points(C.byref(s), _dp(lam_u), W, _dp(ray_u), R, int(nthreads),
+                                 _dp(p) if p is not None else None, _dp(st), C.byref(hits))
+    assert e == OK, e
+    return p, {"info": float(st[0]), "h_cond": float(st[1]), "h_det": float(st[2]),
+               "size": float(st[3]), "hits": int(hits.value)}
+
+
+def trace_pairs(d: dict, lam_u, ray_u):
+    s = make_spec(d)
+    lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
+    ray_u = np.ascontiguousarray(ray_u, dtype=np.float64)
+    n = lam_u.size
+    bins = np.zeros(n, dtype=np.uint32)
+    ts = np.zeros(n)
+    e = lib().orc_trace_pairs(C.byref(s), _dp(lam_u), _dp(ray_u), n,
+                              bins.ctypes.data_as(C.POINTER(C.c_uint32)), _dp(ts))
+    assert e == OK, e
+    return bins, ts
