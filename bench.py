@@ -1,0 +1,363 @@
+"""Benchmark of the compound-prism fitness path on GB300.
+
+Default workload (N=1): the plain one-design GPU call -- 6 prisms, 64 detector
+bins, 4096 QMC wavelengths x 1024 rays (4,194,304 rays per design), FP32 trace
+with FP64/int64 accumulation and entropy. A step is one gpu_fitness call of one
+design. Also measured on the same run: the batched population form (1024 designs of
+mixed G, B, W), reported under "forms".
+
+  value   designs/s with inputs resident on the device: 1 / (device time of the pass)
+  e2e     designs/s through the C ABI with host buffers (design + point tables H2D,
+          result D2H, inside the timed call)
+  roofline  FP32 ALU roofline of the dominant kernel (the trace kernel): algorithmic
+          FLOP of the fast path per evaluated ray x rays evaluated / kernel time,
+          against a live FP32 FMA throughput probe
+  cpu_baseline  the C oracle (the reference CPU algorithm restated) on all host cores,
+          on a bounded sample of the same design
+
+  --impl reference  times the reference's CPU path (the oracle port: the reference
+          itself is Rust and cannot be built here) on the same workload.
+
+Multi-GPU: designs are independent; each rank evaluates its own designs on its own
+GPU with no collective (weak scaling); rank 0 prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "compound-prism-designer_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "MI fitness designs/sec, batched-serving vs plain at <=1e-4 rel MI err; p50/p99 ms"
+G_PLAIN, B_PLAIN, W_PLAIN, R_PLAIN = 6, 64, 4096, 1024
+# FP32 arithmetic of fast_ray on its full path (exit face, refraction, Fresnel,
+# detector, binning): adds/muls count 1, FMAs 2; the 5 MUFU ops (2 sqrt, 3 reciprocal/
+# divide) are not counted. Derivation in the design doc.
+FLOP_PER_FAST_RAY = 110
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rk = int(os.environ.get("RANK", "0"))
+    lrk = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rk, lrk
+
+
+class Dist:
+    """Host-side barrier and max-reduction over ranks (gloo; no data-path collective)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_info()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.ws)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def l2_flusher():
+    """Writes 512 MiB (> the 129 MB L2) between timed steps."""
+    try:
+        import torch
+
+        buf = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+        def flush():
+            buf.fill_(1)
+            torch.cuda.synchronize()
+
+        return flush, "flushed between steps (512 MiB device write)"
+    except Exception as e:  # noqa: BLE001
+        return (lambda: None), f"not flushed ({type(e).__name__})"
+
+
+def plain_design(seed_offset=1):
+    import numpy as np
+    from compound_prism_designer import synth
+
+    rng = np.random.default_rng(20261203 + seed_offset)
+    spec, d, rej = synth.random_design(rng, G_PLAIN, B_PLAIN)
+    return spec, d
+
+
+def batched_population(n=1024, seed=20261205):
+    import numpy as np
+    from compound_prism_designer import synth
+
+    pop, rej = synth.population(seed, n)
+    rng = np.random.default_rng(seed + 1)
+    W = rng.integers(512, 4097, n)
+    return [s for s, _ in pop], W, rej
+
+
+def cpu_oracle_rate(d, W, R, target_s=10.0, nthreads=None):
+    """Oracle (reference CPU algorithm) on all host threads: designs/s extrapolated from
+    a bounded sample of the design's wavelengths (all R rays each)."""
+    import oracle as O
+
+    nthreads = nthreads or os.cpu_count() or 1
+    ray_u = O.qrng_points(0.5, R)
+    lam_all = O.qrng_points(0.5, W)
+    probe = min(W, max(nthreads, 16))
+    t0 = time.perf_counter()
+    O.fitness_points(d, lam_all[:probe], ray_u, nthreads=nthreads, want_p=False)
+    dt = time.perf_counter() - t0
+    S = int(min(W, max(probe, probe * target_s / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    O.fitness_points(d, lam_all[:S], ray_u, nthreads=nthreads, want_p=False)
+    dt = time.perf_counter() - t0
+    rate = S / (W * dt)
+    return {"value": rate, "unit": "designs/s", "cores": nthreads, "kind": "port",
+            "sample": f"{S} of {W} wavelengths x {R} rays of the benchmark design ({S * R} rays, {dt:.1f} s)"}
+
+
+def run_reference(args, dist):
+    """--impl reference: the reference CPU algorithm (oracle port) on the same workload."""
+    if dist.rank != 0:
+        return
+    spec, d = plain_design()
+    import oracle as O
+
+    nthreads = os.cpu_count() or 1
+    ray_u = O.qrng_points(0.5, R_PLAIN)
+    lam = O.qrng_points(0.5, W_PLAIN)
+    S = max(nthreads * 4, 64)
+    for _ in range(args.warmup):
+        O.fitness_points(d, lam[:S], ray_u, nthreads=nthreads, want_p=False)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        off = (k * S) % (W_PLAIN - S)
+        O.fitness_points(d, lam[off:off + S], ray_u, nthreads=nthreads, want_p=False)
+    dt = time.perf_counter() - t0
+    rate = args.steps * S / (W_PLAIN * dt)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "designs/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": plain_config("none (CPU)"),
+        "cpu_baseline": {"value": rate, "unit": "designs/s", "cores": nthreads, "kind": "port",
+                         "sample": f"each step {S} of {W_PLAIN} wavelengths x {R_PLAIN} rays"},
+        "e2e": {"value": rate, "unit": "designs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference is Rust (nightly, un-vendored git deps): not buildable here; the oracle restates "
+                "its CPU fitness path (src/fitness.rs) in C, f64, on all host threads",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def plain_config(l2):
+    return {"workload": f"plain gpu_fitness call, one design per call: {G_PLAIN} prisms, {B_PLAIN} bins, "
+                        f"{W_PLAIN} wavelengths x {R_PLAIN} rays ({W_PLAIN * R_PLAIN} rays)",
+            "prisms": G_PLAIN, "bins": B_PLAIN, "wavelengths": W_PLAIN, "rays_per_wavelength": R_PLAIN,
+            "trace": "fp32 with exact-f64 guard-band re-trace", "accumulation": "int64 fixed point + f64 entropy",
+            "l2": l2}
+
+
+def traffic_from_profiles():
+    """dram bytes per trace-kernel launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "trace_kernel_config1.md")
+    try:
+        txt = open(p).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extras", action="store_true", help="main line only (for profiler runs)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+        return
+
+    import numpy as np
+    import compound_prism_designer as cpd
+
+    ctx = cpd.Context(dist.local)
+    spec, d = plain_design()
+    flush, l2_note = l2_flusher()
+    seeds = [0.5]
+
+    def step():
+        t0 = time.perf_counter()
+        f = spec.gpu_fitness_full(seeds, max_n=W_PLAIN, nwarp=8, max_eval=R_PLAIN, context=ctx)
+        wall = time.perf_counter() - t0
+        ms, launches = ctx.last_timing()
+        h2d, d2h = ctx.last_transfer_bytes()
+        return f, wall, ms, launches, h2d, d2h
+
+    for _ in range(args.warmup):
+        step()
+        flush()
+    clocks = ClockSampler(dist.local)
+    dist.barrier()
+    clocks.start()
+    dev_ms, walls, launches_total = [], [], 0
+    t_start = time.perf_counter()
+    for _ in range(args.steps):
+        f, wall, ms, launches, h2d, d2h = step()
+        dev_ms.append(ms)
+        walls.append(wall)
+        launches_total += launches
+        flush()
+    t_total = time.perf_counter() - t_start
+    clk = clocks.stop()
+    dist.barrier()
+    dev_s = dist.max(sum(dev_ms) / 1e3)
+    wall_s = dist.max(sum(walls))
+    designs = dist.sum(float(args.steps))
+    value = designs / dev_s
+    e2e = designs / wall_s
+
+    extras = {}
+    if not args.no_extras and dist.rank == 0:
+        try:
+            ctx.set_profiling(True)
+            fp = spec.gpu_fitness_full(seeds, max_n=W_PLAIN, nwarp=8, max_eval=R_PLAIN, context=ctx)
+            kt = ctx.last_kernel_times()
+            ctx.set_profiling(False)
+            peak = max(ctx.fp32_peak_tflops(2048) for _ in range(3))
+            achieved = fp.fast_rays * FLOP_PER_FAST_RAY / (kt["trace"] * 1e-3) / 1e12
+            extras["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                                  "frac": achieved / peak, "traffic": traffic_from_profiles(),
+                                  "kernel": "trace_kernel", "kernel_ms": kt,
+                                  "fast_rays": fp.fast_rays, "flop_per_fast_ray": FLOP_PER_FAST_RAY,
+                                  "peak_source": "measured live: FP32 FMA probe on all SMs (cpd_measure_fp32_peak)",
+                                  "retraced": fp.retraced, "hits": fp.hits}
+        except Exception as e:  # noqa: BLE001
+            extras["roofline"] = {"error": repr(e)}
+        try:
+            pop, Ws, rej = batched_population()
+            for _ in range(2):
+                cpd.fitness_batch(pop, seeds=0.5, max_n=Ws, max_eval=R_PLAIN, context=ctx)
+            bt = []
+            bdev = []
+            for _ in range(3):
+                flush()
+                t0 = time.perf_counter()
+                outs = cpd.fitness_batch(pop, seeds=0.5, max_n=Ws, max_eval=R_PLAIN, context=ctx)
+                bt.append(time.perf_counter() - t0)
+                bdev.append(ctx.last_timing()[0])
+            nb = len(pop)
+            extras["forms"] = {"batched": {
+                "workload": f"{nb} designs, G in 2..6, B in 16..128, W in 512..4096, R={R_PLAIN}",
+                "designs_per_s_device": nb / (min(bdev) / 1e3), "designs_per_s_e2e": nb / min(bt),
+                "ms_device": min(bdev), "ms_e2e": min(bt), "rays": int(sum(int(w) for w in Ws) * R_PLAIN),
+                "speedup_vs_plain_e2e": (nb / min(bt)) / e2e}}
+        except Exception as e:  # noqa: BLE001
+            extras["forms"] = {"error": repr(e)}
+        try:
+            extras["cpu_baseline"] = cpu_oracle_rate(d, W_PLAIN, R_PLAIN)
+        except Exception as e:  # noqa: BLE001
+            extras["cpu_baseline"] = {"error": repr(e)}
+
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "designs/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": plain_config(l2_note),
+            "e2e": {"value": e2e, "unit": "designs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": 1e3 * wall_s / args.steps},
+            "gpu_launches": launches_total, "clocks": clk, "wall_s": t_total,
+            "mi": f.info, "retraced_per_step": f.retraced,
+        }
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

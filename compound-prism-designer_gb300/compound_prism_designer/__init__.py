@@ -1,0 +1,536 @@
+"""GB300 drop-in for the fitness path of jdtatz/compound-prism-designer.
+
+Same module name, classes, methods, argument names and defaults as the
+reference's pyo3 extension (src/pylib.rs; stub
+compound_prism_designer/compound_prism_designer.pyi), so an optimizer written
+against the reference (designer.py:203-300) runs unchanged. Every call goes
+through the C ABI of libcpd.so (include/cpd.h); gpu_fitness runs the
+sm_103a kernels and has no CPU fallback.
+
+Out of scope (they raise NotImplementedError): the 3-D FiberBeam/toric-lens
+variant on the GPU and the matplotlib drawing helpers (polygons, surfaces).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import threading
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+
+__all__ = [
+    "RayTraceError", "CudaError", "Glass", "DesignFitness", "Vector2D", "UnitVector2D",
+    "UniformWavelengthDistribution", "GaussianBeam", "FiberBeam", "CompoundPrism",
+    "position_detector_array", "DetectorArray", "Spectrometer", "Context", "default_context",
+    "fitness_batch", "TRACE_HYBRID", "TRACE_FP32", "TRACE_FP64",
+]
+
+TRACE_HYBRID = N.TRACE_HYBRID
+TRACE_FP32 = N.TRACE_FP32
+TRACE_FP64 = N.TRACE_FP64
+
+
+class RayTraceError(Exception):
+    """A geometric failure (src/spectrometer/ray.rs:10-16)."""
+
+
+class CudaError(Exception):
+    """A CUDA failure (src/pylib.rs:26-35)."""
+
+
+def _check(code: int, what: str = "") -> int:
+    if code in (N.OK, N.NOT_CONVERGED):
+        return code
+    msg = N.status_string(code)
+    if code in N.RAYTRACE_ERRORS:
+        raise RayTraceError(msg)
+    if code == N.CUDA_ERROR:
+        raise CudaError(f"{what}: {msg}" if what else msg)
+    if code == N.NOT_IMPLEMENTED:
+        raise NotImplementedError(msg)
+    raise ValueError(f"{what}: {msg}" if what else msg)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Glass:
+    """Glass(name, coefficents): the 6-coefficient Horner dispersion polynomial
+    (src/pylib.rs:37-95, src/spectrometer/glasscat.rs:7-22)."""
+
+    ORDER = 5
+
+    def __init__(self, name: str, coefficents):
+        c = np.ascontiguousarray(coefficents, dtype=np.float64).reshape(-1)
+        if c.size != self.ORDER + 1:
+            raise ValueError("Incorrect coefficents length")
+        self.name = str(name)
+        self._c = c
+
+    @property
+    def glass(self) -> np.ndarray:
+        return self._c.copy()
+
+    def __call__(self, w: float) -> float:
+        return N.lib.cpd_glass_index(_dp(self._c), float(w))
+
+    def __getnewargs__(self):
+        return (self.name, self._c.copy())
+
+    def __reduce__(self):
+        return (Glass, (self.name, self._c.copy()))
+
+    def __repr__(self):
+        return f"Glass(name={self.name!r}, coefficents={self._c.tolist()})"
+
+
+class DesignFitness:
+    """DesignFitness(size, info, deviation) (src/pylib.rs:103-153)."""
+
+    def __init__(self, size: float, info: float, deviation: float):
+        self.size = float(size)
+        self.info = float(info)
+        self.deviation = float(deviation)
+
+    def __getnewargs__(self):
+        return (self.size, self.info, self.deviation)
+
+    def __reduce__(self):
+        return (DesignFitness, self.__getnewargs__())
+
+    def __repr__(self):
+        return f"DesignFitness(size={self.size}, info={self.info}, deviation={self.deviation})"
+
+
+class Vector2D:
+    def __init__(self, x: float, y: float):
+        self.x = float(x)
+        self.y = float(y)
+
+    def __iter__(self):
+        return iter((self.x, self.y))
+
+    def __getnewargs__(self):
+        return (self.x, self.y)
+
+    def __repr__(self):
+        return f"Vector2D(x={self.x}, y={self.y})"
+
+
+class UnitVector2D(Vector2D):
+    def __init__(self, x: float, y: float):
+        # UnitVector::try_new: |v| within rmax 1e-3 of 1 (vector.rs:300-312, src/pylib.rs:215-220)
+        n = math.hypot(x, y)
+        if not abs(n - 1.0) <= 1e-3 * max(n, 1.0):
+            raise ValueError("x^2 + y^2 != 1")
+        super().__init__(x, y)
+
+    def __repr__(self):
+        return f"UnitVector2D(x={self.x}, y={self.y})"
+
+
+class UniformWavelengthDistribution:
+    """UniformWavelengthDistribution(bounds) (src/pylib.rs:290-331)."""
+
+    def __init__(self, bounds):
+        lo, hi = (float(b) for b in bounds)
+        if hi < lo:
+            raise ValueError("lower bound > upper bound")
+        self.bounds = (lo, hi)
+
+    def __getnewargs__(self):
+        return (self.bounds,)
+
+
+class GaussianBeam:
+    """GaussianBeam(width, y_mean) (src/pylib.rs:357-385)."""
+
+    def __init__(self, width: float, y_mean: float):
+        self.width = float(width)
+        self.y_mean = float(y_mean)
+
+    def __getnewargs__(self):
+        return (self.width, self.y_mean)
+
+    def __repr__(self):
+        return f"GaussianBeam(width={self.width}, y_mean={self.y_mean})"
+
+
+class FiberBeam:
+    """FiberBeam(core_radius, numerical_aperture, center_y) (src/pylib.rs:387-430).
+    Constructible for API compatibility; the 3-D fiber-beam trace is not built."""
+
+    def __init__(self, core_radius: float, numerical_aperture: float, center_y: float):
+        self.core_radius = float(core_radius)
+        self.numerical_aperture = float(numerical_aperture)
+        self.center_y = float(center_y)
+
+    @property
+    def y_mean(self) -> float:
+        return self.center_y
+
+    @property
+    def width(self) -> float:
+        return self.core_radius
+
+    def __getnewargs__(self):
+        return (self.core_radius, self.numerical_aperture, self.center_y)
+
+
+def _fill_prism(p: N.SpectrometerParams, glasses, angles, lengths, curvature, height, width, ar_coated):
+    G = len(glasses)
+    p.nglass = G
+    p.ar_coated = int(bool(ar_coated))
+    for g, glass in enumerate(glasses):
+        for i, c in enumerate(glass._c):
+            p.glass[g][i] = float(c)
+    for i, a in enumerate(angles):
+        p.angles[i] = float(a)
+    for i, l in enumerate(lengths):
+        p.lengths[i] = float(l)
+    p.curvature = float(curvature)
+    p.height = float(height)
+    p.width = float(width)
+
+
+class CompoundPrism:
+    """CompoundPrism(glasses, angles, lengths, curvature, height, width, ar_coated)
+    (src/pylib.rs:658-812)."""
+
+    def __init__(self, glasses: Sequence[Glass], angles, lengths, curvature, height: float, width: float,
+                 ar_coated: bool):
+        glasses = list(glasses)
+        angles = [float(a) for a in np.asarray(angles, dtype=np.float64).reshape(-1)]
+        lengths = [float(l) for l in np.asarray(lengths, dtype=np.float64).reshape(-1)]
+        # argument checks of SizedCompoundPrism::new (src/pylib.rs:524-540)
+        if len(angles) < 2:
+            raise ValueError("`angles` must have at least 2 elements")
+        if len(glasses) > N.MAX_GLASS:
+            raise ValueError(f"Maximum of {N.MAX_GLASS} prisms are allowed")
+        if len(glasses) != len(angles) - 1:
+            raise ValueError("len(glasses) + 1 != len(angles)")
+        if len(glasses) != len(lengths):
+            raise ValueError("len(glasses) != len(lengths)")
+        if isinstance(curvature, (tuple, list)):
+            raise NotImplementedError("the 3-D toric-lens compound prism is not built")
+        self.glasses = glasses
+        self.angles = angles
+        self.lengths = lengths
+        self.curvature = float(curvature)
+        self.height = float(height)
+        self.width = float(width)
+        self.ar_coated = bool(ar_coated)
+        # the prism tables alone (a placeholder detector makes the design complete)
+        p = N.SpectrometerParams()
+        self._fill(p)
+        p.bin_count, p.bin_size, p.linear_slope, p.det_length = 1, 1.0, 1.0, 1.0
+        p.wavelength_bounds[0], p.wavelength_bounds[1] = 0.5, 0.5
+        d = N.Design()
+        _check(N.lib.cpd_design_build(C.byref(p), C.byref(d)), "CompoundPrism")
+        self._design = d
+
+    def _fill(self, p: N.SpectrometerParams):
+        _fill_prism(p, self.glasses, self.angles, self.lengths, self.curvature, self.height, self.width,
+                    self.ar_coated)
+
+    def __getnewargs__(self):
+        return (self.glasses, self.angles, self.lengths, self.curvature, self.height, self.width, self.ar_coated)
+
+    def __reduce__(self):
+        return (CompoundPrism, self.__getnewargs__())
+
+    def exit_ray(self, y: float, wavelength: float):
+        out = np.zeros(4)
+        _check(N.lib.cpd_exit_ray(C.byref(self._design), float(y), float(wavelength), _dp(out)))
+        return Vector2D(out[0], out[1]), UnitVector2D(out[2], out[3])
+
+    def final_midpt_and_normal(self):
+        """(arc mid point, unit vector at the last angle) (src/pylib.rs:782-793)."""
+        d = self._design
+        a = self.angles[-1]
+        return Vector2D(d.exit_bound_center[0], d.exit_bound_center[1]), UnitVector2D(math.cos(a), math.sin(a))
+
+    def surfaces(self):
+        raise NotImplementedError("drawing helpers are not part of the GPU fitness path")
+
+    def polygons(self):
+        raise NotImplementedError("drawing helpers are not part of the GPU fitness path")
+
+    def __repr__(self):
+        return (f"CompoundPrism(glasses={[g.name for g in self.glasses]}, angles={self.angles}, "
+                f"lengths={self.lengths}, curvature={self.curvature}, height={self.height}, "
+                f"width={self.width}, ar_coated={self.ar_coated})")
+
+
+def _fill_source(p: N.SpectrometerParams, wavelengths, beam):
+    if not isinstance(wavelengths, UniformWavelengthDistribution):
+        raise TypeError("wavelengths must be a UniformWavelengthDistribution")
+    p.wavelength_bounds[0], p.wavelength_bounds[1] = wavelengths.bounds
+    if isinstance(beam, GaussianBeam):
+        p.beam_width = beam.width
+        p.beam_y_mean = beam.y_mean
+    elif isinstance(beam, FiberBeam):
+        raise NotImplementedError("No kernel compiled for this Spectrometer")
+    else:
+        raise TypeError("beam must be a GaussianBeam")
+
+
+def position_detector_array(length: float, angle: float, compound_prism: CompoundPrism, wavelengths, beam,
+                            acceptance: float):
+    """position_detector_array (src/pylib.rs:815-838)."""
+    p = N.SpectrometerParams()
+    compound_prism._fill(p)
+    _fill_source(p, wavelengths, beam)
+    p.det_length = float(length)
+    p.det_angle = float(angle)
+    pos = np.zeros(2)
+    fl = C.c_int32(0)
+    _check(N.lib.cpd_position_detector_array(C.byref(p), float(acceptance), _dp(pos), C.byref(fl)))
+    return (float(pos[0]), float(pos[1])), bool(fl.value)
+
+
+class DetectorArray:
+    """DetectorArray(bin_count, bin_size, linear_slope, linear_intercept, length,
+    max_incident_angle, angle, position, flipped) (src/pylib.rs:840-955)."""
+
+    def __init__(self, bin_count: int, bin_size: float, linear_slope: float, linear_intercept: float,
+                 length: float, max_incident_angle: float, angle: float, position, flipped: bool):
+        self.bin_count = int(bin_count)
+        self.bin_size = float(bin_size)
+        self.linear_slope = float(linear_slope)
+        self.linear_intercept = float(linear_intercept)
+        self.length = float(length)
+        self.max_incident_angle = float(max_incident_angle)
+        self.angle = float(angle)
+        self.position = (float(position[0]), float(position[1]))
+        self.flipped = bool(flipped)
+
+    def __getnewargs__(self):
+        return (self.bin_count, self.bin_size, self.linear_slope, self.linear_intercept, self.length,
+                self.max_incident_angle, self.angle, self.position, self.flipped)
+
+    def __reduce__(self):
+        return (DetectorArray, self.__getnewargs__())
+
+
+class Context:
+    """A GPU context (one per device): stream, pooled device buffers, captured CUDA
+    graphs. The reference keeps one cached context behind a mutex
+    (src/cuda_fitness.rs:322-363); this one is thread-safe too."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(N.lib.cpd_context_create(int(device), C.byref(h)), "cpd_context_create")
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            N.lib.cpd_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_launch_shape(self, ray_tile: int = 0, warps_per_cta: int = 0):
+        _check(N.lib.cpd_set_launch_shape(self._h, int(ray_tile), int(warps_per_cta)))
+
+    def launch_shape(self):
+        rt, w = C.c_uint32(0), C.c_uint32(0)
+        _check(N.lib.cpd_get_launch_shape(self._h, C.byref(rt), C.byref(w)))
+        return rt.value, w.value
+
+    def last_timing(self):
+        ms = C.c_double(0.0)
+        n = C.c_uint32(0)
+        _check(N.lib.cpd_last_timing(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def set_profiling(self, on: bool = True):
+        _check(N.lib.cpd_set_profiling(self._h, int(bool(on))))
+
+    def last_kernel_times(self) -> dict:
+        ms = np.zeros(4)
+        _check(N.lib.cpd_last_kernel_times(self._h, _dp(ms)))
+        return dict(zip(("setup", "trace", "retrace", "entropy"), ms.tolist()))
+
+    def last_transfer_bytes(self):
+        h, d = C.c_uint64(0), C.c_uint64(0)
+        _check(N.lib.cpd_last_transfer_bytes(self._h, C.byref(h), C.byref(d)))
+        return h.value, d.value
+
+    def fp32_peak_tflops(self, iters: int = 4096) -> float:
+        t = C.c_double(0.0)
+        _check(N.lib.cpd_measure_fp32_peak(self._h, int(iters), C.byref(t)))
+        return t.value
+
+
+_contexts: dict[int, Context] = {}
+_ctx_lock = threading.Lock()
+
+
+def default_context(device: int = 0) -> Context:
+    with _ctx_lock:
+        ctx = _contexts.get(device)
+        if ctx is None:
+            ctx = Context(device)
+            _contexts[device] = ctx
+        return ctx
+
+
+class Spectrometer:
+    """Spectrometer(compound_prism, detector_array, wavelengths, beam) (src/pylib.rs:957-1170)."""
+
+    def __init__(self, compound_prism: CompoundPrism, detector_array: DetectorArray, wavelengths, beam):
+        self.compound_prism = compound_prism
+        self.detector_array = detector_array
+        self.wavelengths = wavelengths
+        self.beam = beam
+        self._design = None
+
+    def __getnewargs__(self):
+        return (self.compound_prism, self.detector_array, self.wavelengths, self.beam)
+
+    def __reduce__(self):
+        return (Spectrometer, self.__getnewargs__())
+
+    def params(self) -> N.SpectrometerParams:
+        p = N.SpectrometerParams()
+        self.compound_prism._fill(p)
+        _fill_source(p, self.wavelengths, self.beam)
+        da = self.detector_array
+        p.bin_count = da.bin_count
+        p.bin_size = da.bin_size
+        p.linear_slope = da.linear_slope
+        p.linear_intercept = da.linear_intercept
+        p.det_length = da.length
+        p.max_incident_angle = da.max_incident_angle
+        p.det_angle = da.angle
+        p.det_position[0], p.det_position[1] = da.position
+        p.det_flipped = int(da.flipped)
+        return p
+
+    @property
+    def design(self) -> N.Design:
+        """The built f64 design tables (cpd_design) this spectrometer evaluates."""
+        if self._design is None:
+            d = N.Design()
+            _check(N.lib.cpd_design_build(C.byref(self.params()), C.byref(d)), "Spectrometer")
+            self._design = d
+        return self._design
+
+    @property
+    def position(self):
+        d = self.design
+        return (d.det_position[0], d.det_position[1])
+
+    @property
+    def direction(self):
+        d = self.design
+        return (d.det_direction[0], d.det_direction[1])
+
+    def cpu_fitness(self, *, max_n: int = 16_384, max_m: int = 16_384) -> DesignFitness:
+        """The reference's adaptive f64 host estimator (src/pylib.rs:1008-1026)."""
+        f = N.Fitness()
+        _check(N.lib.cpd_fitness_cpu(C.byref(self.design), int(max_n), int(max_m), C.byref(f)))
+        return DesignFitness(f.size, f.info, f.deviation)
+
+    def gpu_fitness(self, seeds, *, max_n: int = 256, nwarp: int = 2, max_eval: int = 16_384,
+                    context: Optional[Context] = None) -> Optional[DesignFitness]:
+        """GPU fitness (src/pylib.rs:1085-1135): None if the SEM stop was not met."""
+        f = self.gpu_fitness_full(seeds, max_n=max_n, nwarp=nwarp, max_eval=max_eval, context=context)
+        if f.status == N.NOT_CONVERGED:
+            return None
+        return DesignFitness(f.size, f.info, f.deviation)
+
+    def gpu_fitness_full(self, seeds, *, max_n: int = 256, nwarp: int = 2, max_eval: int = 16_384,
+                         context: Optional[Context] = None) -> N.Fitness:
+        seeds = np.ascontiguousarray(np.atleast_1d(seeds), dtype=np.float64)
+        ctx = context or default_context()
+        f = N.Fitness()
+        _check(N.lib.cpd_fitness_gpu(ctx.handle, C.byref(self.design), _dp(seeds), seeds.size, int(max_n),
+                                     int(nwarp), int(max_eval), C.byref(f)), "gpu_fitness")
+        return f
+
+    def gpu_fitness_points(self, lam_u, ray_u, *, mode: int = TRACE_HYBRID, want_p: bool = False,
+                           context: Optional[Context] = None):
+        """Fixed-N estimator on explicit wavelength and ray u-points (parity entry)."""
+        lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
+        ray_u = np.ascontiguousarray(ray_u, dtype=np.float64)
+        ctx = context or default_context()
+        f = N.Fitness()
+        p = np.zeros((lam_u.size, self.detector_array.bin_count)) if want_p else None
+        _check(N.lib.cpd_fitness_gpu_points(ctx.handle, C.byref(self.design), _dp(lam_u), lam_u.size, _dp(ray_u),
+                                            ray_u.size, int(mode), C.byref(f),
+                                            _dp(p) if p is not None else None), "gpu_fitness_points")
+        return f, p
+
+    def trace_rays(self, lam_u, ray_u, *, mode: int = TRACE_HYBRID, context: Optional[Context] = None):
+        """One ray per (lam_u[i], ray_u[i]): (bins, t, retraced) (propagation_test_kernel twin)."""
+        lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
+        ray_u = np.ascontiguousarray(ray_u, dtype=np.float64)
+        n = lam_u.size
+        bins = np.zeros(n, dtype=np.uint32)
+        ts = np.zeros(n)
+        fl = np.zeros(n, dtype=np.uint8)
+        ctx = context or default_context()
+        _check(N.lib.cpd_trace_rays(ctx.handle, C.byref(self.design), _dp(lam_u), _dp(ray_u), n, int(mode),
+                                    bins.ctypes.data_as(C.POINTER(C.c_uint32)), _dp(ts),
+                                    fl.ctypes.data_as(C.POINTER(C.c_uint8))), "trace_rays")
+        return bins, ts, fl.astype(bool)
+
+    def transmission_probability(self, wavelengths, *, max_m: int = 16_384,
+                                 context: Optional[Context] = None) -> np.ndarray:
+        """p(d|lambda) for each given wavelength (src/pylib.rs:1028-1058), max_m rays each."""
+        w = np.ascontiguousarray(wavelengths, dtype=np.float64).reshape(-1)
+        ctx = context or default_context()
+        out = np.zeros((w.size, self.detector_array.bin_count))
+        _check(N.lib.cpd_transmission_probability(ctx.handle, C.byref(self.design), _dp(w), w.size, int(max_m),
+                                                  _dp(out)), "transmission_probability")
+        return out
+
+    def ray_trace(self, wavelength: float, inital_y: float) -> np.ndarray:
+        """Propagation path rows (x, y, ux, uy) (src/pylib.rs:1060-1083)."""
+        G = len(self.compound_prism.glasses)
+        rows = np.zeros((G + 3, 4))
+        n = C.c_uint32(0)
+        _check(N.lib.cpd_ray_trace(C.byref(self.design), float(wavelength), float(inital_y), _dp(rows),
+                                   C.byref(n)))
+        return rows[: n.value].copy()
+
+    def __repr__(self):
+        return (f"Spectrometer({self.compound_prism!r}, detector_array={self.detector_array.__dict__}, "
+                f"wavelengths={self.wavelengths.bounds}, beam={self.beam!r})")
+
+
+def fitness_batch(spectrometers: Sequence[Spectrometer], *, seeds=None, max_n=256, max_eval=16_384,
+                  mode: int = TRACE_HYBRID, context: Optional[Context] = None):
+    """Batched GPU fitness of many designs in one launch sequence (no reference
+    counterpart). max_n, max_eval and seeds may be scalars or per-design sequences.
+    Returns a list of cpd_fitness records (status OK or NOT_CONVERGED per design)."""
+    n = len(spectrometers)
+    designs = (N.Design * n)()
+    items = (N.BatchItem * n)()
+    mn = np.broadcast_to(np.asarray(max_n), (n,))
+    me = np.broadcast_to(np.asarray(max_eval), (n,))
+    sd = np.broadcast_to(np.asarray(0.5 if seeds is None else seeds, dtype=np.float64), (n,))
+    for i, s in enumerate(spectrometers):
+        designs[i] = s.design
+        items[i].seed = float(sd[i])
+        items[i].max_n = int(mn[i])
+        items[i].max_eval = int(me[i])
+    outs = (N.Fitness * n)()
+    ctx = context or default_context()
+    _check(N.lib.cpd_fitness_gpu_batch(ctx.handle, designs, items, n, int(mode), outs), "fitness_batch")
+    return list(outs)

@@ -1,0 +1,172 @@
+"""ctypes binding of the C ABI in include/cpd.h (libcpd.so).
+
+The library is the product: the GPU fitness path is its CUDA code and nothing
+here falls back to a Python or CPU implementation. If the shared library is
+missing, importing this module raises ImportError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.environ.get("CPD_LIBRARY", os.path.join(PKG_ROOT, "_build", "libcpd.so"))
+
+MAX_GLASS = 6
+MAX_BINS = 1024
+MAX_WAVELENGTHS = 65536
+MAX_RAYS = 1 << 22
+
+# cpd_status
+OK = 0
+NOT_CONVERGED = 1
+RAYTRACE_NO_SURFACE_INTERSECTION = 2
+RAYTRACE_OUT_OF_BOUNDS = 3
+RAYTRACE_TOTAL_INTERNAL_REFLECTION = 4
+RAYTRACE_ANGULAR_RESPONSE_TOO_WEAK = 5
+INVALID_ARGUMENT = 6
+CUDA_ERROR = 7
+TIMEOUT = 8
+NO_CAPACITY = 9
+NOT_IMPLEMENTED = 10
+RAYTRACE_ERRORS = (RAYTRACE_NO_SURFACE_INTERSECTION, RAYTRACE_OUT_OF_BOUNDS,
+                   RAYTRACE_TOTAL_INTERNAL_REFLECTION, RAYTRACE_ANGULAR_RESPONSE_TOO_WEAK)
+
+TRACE_HYBRID = 0
+TRACE_FP32 = 1
+TRACE_FP64 = 2
+
+
+class SpectrometerParams(C.Structure):
+    _fields_ = [
+        ("nglass", C.c_int32),
+        ("ar_coated", C.c_int32),
+        ("glass", (C.c_double * 6) * MAX_GLASS),
+        ("angles", C.c_double * (MAX_GLASS + 1)),
+        ("lengths", C.c_double * MAX_GLASS),
+        ("curvature", C.c_double),
+        ("height", C.c_double),
+        ("width", C.c_double),
+        ("bin_count", C.c_uint32),
+        ("det_flipped", C.c_int32),
+        ("bin_size", C.c_double),
+        ("linear_slope", C.c_double),
+        ("linear_intercept", C.c_double),
+        ("det_length", C.c_double),
+        ("max_incident_angle", C.c_double),
+        ("det_angle", C.c_double),
+        ("det_position", C.c_double * 2),
+        ("wavelength_bounds", C.c_double * 2),
+        ("beam_width", C.c_double),
+        ("beam_y_mean", C.c_double),
+    ]
+
+
+class Design(C.Structure):
+    _fields_ = [
+        ("nglass", C.c_int32),
+        ("bin_count", C.c_uint32),
+        ("ar_coated", C.c_int32),
+        ("reserved", C.c_int32),
+        ("glass", (C.c_double * 6) * MAX_GLASS),
+        ("face_point", (C.c_double * 2) * MAX_GLASS),
+        ("face_normal", (C.c_double * 2) * MAX_GLASS),
+        ("height", C.c_double),
+        ("exit_center", C.c_double * 2),
+        ("exit_radius", C.c_double),
+        ("exit_bound_center", C.c_double * 2),
+        ("exit_bound_r2", C.c_double),
+        ("bin_size", C.c_double),
+        ("linear_slope", C.c_double),
+        ("linear_intercept", C.c_double),
+        ("min_ci", C.c_double),
+        ("det_length", C.c_double),
+        ("det_normal", C.c_double * 2),
+        ("det_position", C.c_double * 2),
+        ("det_direction", C.c_double * 2),
+        ("wavelength_bounds", C.c_double * 2),
+        ("beam_width", C.c_double),
+        ("beam_y_mean", C.c_double),
+        ("size", C.c_double),
+        ("deviation", C.c_double),
+    ]
+
+
+class Fitness(C.Structure):
+    _fields_ = [
+        ("size", C.c_double),
+        ("info", C.c_double),
+        ("deviation", C.c_double),
+        ("h_cond", C.c_double),
+        ("h_det", C.c_double),
+        ("max_sem", C.c_double),
+        ("rays", C.c_uint64),
+        ("hits", C.c_uint64),
+        ("retraced", C.c_uint64),
+        ("fast_rays", C.c_uint64),
+        ("wavelengths", C.c_uint32),
+        ("status", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("seed", C.c_double), ("max_n", C.c_uint32), ("max_eval", C.c_uint32)]
+
+
+_dp = C.POINTER(C.c_double)
+_up = C.POINTER(C.c_uint32)
+_ctxp = C.c_void_p
+
+# (name, restype, argtypes) of every symbol include/cpd.h declares.
+SIGNATURES = [
+    ("cpd_abi_version", C.c_int, []),
+    ("cpd_status_string", C.c_char_p, [C.c_int]),
+    ("cpd_position_detector_array", C.c_int, [C.POINTER(SpectrometerParams), C.c_double, _dp, C.POINTER(C.c_int32)]),
+    ("cpd_design_build", C.c_int, [C.POINTER(SpectrometerParams), C.POINTER(Design)]),
+    ("cpd_exit_ray", C.c_int, [C.POINTER(Design), C.c_double, C.c_double, _dp]),
+    ("cpd_ray_trace", C.c_int, [C.POINTER(Design), C.c_double, C.c_double, _dp, _up]),
+    ("cpd_fitness_cpu", C.c_int, [C.POINTER(Design), C.c_uint64, C.c_uint64, C.POINTER(Fitness)]),
+    ("cpd_norminv", C.c_double, [C.c_double]),
+    ("cpd_glass_index", C.c_double, [_dp, C.c_double]),
+    ("cpd_context_create", C.c_int, [C.c_int, C.POINTER(_ctxp)]),
+    ("cpd_context_destroy", None, [_ctxp]),
+    ("cpd_fitness_gpu", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                  C.POINTER(Fitness)]),
+    ("cpd_fitness_gpu_points", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, _dp, C.c_uint32, C.c_uint32,
+                                         C.POINTER(Fitness), _dp]),
+    ("cpd_transmission_probability", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, C.c_uint32, _dp]),
+    ("cpd_trace_rays", C.c_int, [_ctxp, C.POINTER(Design), _dp, _dp, C.c_uint32, C.c_uint32, _up, _dp,
+                                 C.POINTER(C.c_uint8)]),
+    ("cpd_fitness_gpu_batch", C.c_int, [_ctxp, C.POINTER(Design), C.POINTER(BatchItem), C.c_uint32, C.c_uint32,
+                                        C.POINTER(Fitness)]),
+    ("cpd_set_launch_shape", C.c_int, [_ctxp, C.c_uint32, C.c_uint32]),
+    ("cpd_get_launch_shape", C.c_int, [_ctxp, _up, _up]),
+    ("cpd_last_timing", C.c_int, [_ctxp, _dp, _up]),
+    ("cpd_measure_fp32_peak", C.c_int, [_ctxp, C.c_uint32, _dp]),
+    ("cpd_set_profiling", C.c_int, [_ctxp, C.c_int]),
+    ("cpd_last_kernel_times", C.c_int, [_ctxp, _dp]),
+    ("cpd_last_transfer_bytes", C.c_int, [_ctxp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"libcpd.so not found at {LIB_PATH}: build it first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(LIB_PATH)
+    for name, res, args in SIGNATURES:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def status_string(code: int) -> str:
+    return lib.cpd_status_string(code).decode()

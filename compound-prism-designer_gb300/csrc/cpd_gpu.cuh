@@ -1,0 +1,99 @@
+// cpd_gpu.cuh -- device-side job descriptors and kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "cpd_model.h"
+
+namespace cpd {
+
+// One design in a launch sequence. Offsets index the launch's shared buffers.
+struct alignas(16) DesignJob {
+    uint32_t W;          // wavelength rows this pass
+    uint32_t R;          // rays per wavelength (estimator divisor)
+    uint32_t Rz;         // rays in the sorted table (R minus non-finite start heights)
+    uint32_t B;          // detector bins
+    uint64_t row_off;    // first global wavelength row (LamParams index)
+    uint64_t hist_off;   // first histogram cell (rows x B, u64)
+    uint64_t lam_off;    // first wavelength u-point
+    uint64_t ray_off;    // first entry of the sorted ray tables
+    uint64_t acc_off;    // first per-bin accumulator (B cells in each of S1, S2)
+    uint64_t item_off;   // first trace work item
+    uint64_t tile_off;   // first entropy tile
+    uint32_t nchunk;     // ray chunks per 32-wavelength block
+    uint32_t tile_rows;  // wavelength rows per entropy tile
+    uint32_t ntiles;
+    uint32_t pad;
+};
+
+// A ray whose FP32 result fell inside a guard band: (design, wavelength row, ray).
+struct alignas(16) QEntry {
+    uint32_t design, k, j, pad;
+};
+
+// Per-launch control words (zeroed before every pass).
+struct Control {
+    unsigned long long item_counter;
+    unsigned long long queue_count;
+    unsigned int overflow;
+    unsigned int pad;
+};
+
+// Per-design accumulators that persist across the seeds of one call.
+struct DesignAcc {
+    unsigned long long H;         // sum over rows and bins of -p log2 p, 2^-40 units
+    unsigned long long hits;      // rays that reached a bin
+    unsigned long long retraced;  // rays re-traced in exact f64
+    unsigned long long rows;      // wavelength rows accumulated
+    unsigned long long fast;      // rays evaluated by the FP32 fast path
+};
+
+// Per-design result of the fused finalize (cumulative over passes).
+struct DesignOut {
+    double info, h_cond, h_det, max_sem;
+    unsigned long long hits, retraced, rows, fast;
+    int32_t converged;
+    int32_t pad;
+};
+
+struct LaunchArgs {
+    const DevDesign *designs;
+    const DesignJob *jobs;
+    uint32_t njobs;
+    uint64_t total_rows;
+    uint64_t total_items;
+    uint64_t total_tiles;
+    const double *lam_u;
+    const double *z64;
+    const float *z32;     // (hi, lo) f32 pairs of the sorted z table
+    LamParams *lp;
+    unsigned long long *hist;
+    unsigned long long *S1;
+    unsigned long long *S2;
+    DesignAcc *acc;
+    unsigned int *tiles_done;     // per design, entropy tiles finished this pass (zeroed per pass)
+    DesignOut *out;
+    Control *ctl;
+    QEntry *queue;
+    uint32_t qcap;
+    uint32_t ray_tile;
+    uint32_t mode;        // CPD_TRACE_*
+    Guards guards;
+    double yguard_rel;
+    double *p_out;        // optional W x B for the single design of the launch
+};
+
+// Launches setup -> trace -> retrace -> entropy on `stream`. Returns the number of
+// kernel launches issued. If `ev` is given (5 events), ev[i] is recorded before
+// kernel i and ev[4] after the last one.
+int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaStream_t stream,
+                cudaEvent_t *ev = nullptr);
+
+// One thread per (lam_u[i], z[i]) pair: the twin of propagation_test_kernel.
+void launch_trace_pairs(const DevDesign *d, const double *lam_u, const double *z64, uint32_t n, uint32_t mode,
+                        uint32_t *bins, double *ts, uint8_t *flags, cudaStream_t stream);
+
+// FP32 FMA throughput probe.
+void launch_fma_peak(float *out, uint32_t iters, int blocks, int threads, cudaStream_t stream);
+
+}  // namespace cpd

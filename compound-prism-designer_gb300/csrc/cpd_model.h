@@ -1,0 +1,693 @@
+// cpd_model.h -- the spectrometer model shared by host C++ and device CUDA code.
+//
+// Three layers:
+//  * Exact f64 model (namespace cpd::x): the reference's per-ray trace
+//    (src/spectrometer/ray.rs:309-499, geometry.rs:124-216, spectrometer.rs:265-303)
+//    with every rounding step made explicit. On the device the arithmetic uses
+//    the _rn intrinsics (no contraction); on the host this header is compiled with
+//    -ffp-contract=off. Both therefore give the reference's own f64 results bit
+//    for bit, given the same tables. Transcendentals (log in the inverse normal
+//    CDF, sin/cos in design construction) are evaluated on the host only.
+//  * Per-wavelength setup (lambda_setup): all rays of one wavelength leave the
+//    Gaussian beam with direction (1,0) (Ray::new_from_start, ray.rs:277-279), and
+//    every face before the curved exit face is flat, so the direction and the s/p
+//    transmittances after each flat face are the same for every ray of that
+//    wavelength (the same f64 operations on the same operands). Positions on the
+//    flat faces are affine in the start height y, so the set of rays that clears
+//    every flat face is an interval of y, and, with the ray table sorted by
+//    z = norminv(u), a contiguous range of ray indices.
+//  * FP32 fast path (fast_ray): per ray, only the exit face and the detector,
+//    with a guard margin on every decision; a ray inside any guard band is
+//    reported FLAG and re-traced with the exact model.
+#pragma once
+
+#include <cstdint>
+#include <cmath>
+
+#include "../../include/cpd.h"
+
+#if defined(__CUDACC__)
+#define CPD_HD __host__ __device__ __forceinline__
+#define CPD_HDN __host__ __device__
+#else
+#define CPD_HD inline
+#define CPD_HDN
+#endif
+
+namespace cpd {
+
+// 1/phi, the 1-D R1 sequence step (qrng.rs:156-158, kernel.rs:107-108).
+constexpr double kAlpha = 1.0 / 1.61803398874989484820458683436563;
+// Fixed-point scale of a ray's transmittance in the per-(wavelength, bin) sums.
+constexpr double kTScale = 1099511627776.0;          // 2^40
+constexpr double kTScaleInv = 1.0 / 1099511627776.0;
+// Fixed-point scales of the per-design accumulators.
+constexpr double kPScale = 70368744177664.0;         // 2^46, sum over wavelengths of p and p^2
+constexpr double kPScaleInv = 1.0 / 70368744177664.0;
+constexpr double kHScale = 1099511627776.0;          // 2^40, sum of -p log2 p
+constexpr double kHScaleInv = 1.0 / 1099511627776.0;
+
+// Outcome of a ray.
+enum : int { RAY_LOST = 0, RAY_HIT = 1, RAY_FLAG = 2 };
+
+// ----------------------------------------------------------------- device tables
+
+// FP32 constants of the fast path (per design).
+struct alignas(16) FastConst {
+    float inv_rc;      // 1 / exit-face radius
+    float rho;         // exit-face bound radius
+    float rho2;        // bound radius^2
+    float dnfx, dnfy, dufx, dufy;  // detector normal and direction
+    float min_ci, L, c0, slope, inv_slope, bin_size;
+    float bw;          // beam width
+    int32_t ar;
+    uint32_t B;
+};
+
+// Per design, on the device: the exact f64 tables plus the FP32 constants.
+struct alignas(16) DevDesign {
+    int32_t G;
+    uint32_t B;
+    int32_t ar;
+    int32_t pad0;
+    double glass[CPD_MAX_GLASS][6];
+    double ppx[CPD_MAX_GLASS], ppy[CPD_MAX_GLASS], pnx[CPD_MAX_GLASS], pny[CPD_MAX_GLASS];
+    double height;
+    double ccx, ccy, crad, cbx, cby, cbr2;
+    double bin_size, slope, intercept, min_ci, L;
+    double dnx, dny, dpx, dpy, dux, duy;
+    double wmin, wmax, bw, bym;
+    FastConst fc;
+};
+
+// Per (design, wavelength), written by lambda_setup. The FP32 fast path works in
+// differences from one reference ray of the wavelength, traced in f64 through the
+// exit face and onto the detector: every per-ray quantity is the reference value
+// plus a difference computed with a cancellation-free identity, so the FP32 error
+// scales with the (small) difference, not with the absolute coordinates or the
+// distance to the detector.
+struct alignas(16) LamParams {
+    float zref_hi, zref_lo;     // z of the reference ray (f32 hi + lo parts)
+    float w1x, w1y;             // d(position on the last flat face)/dy
+    float dx, dy;               // direction entering the exit face (same for every ray)
+    float ts, tp;               // s/p transmittance entering the exit face
+    float dlx2, dly2;           // 2 (w_ref - c): ray point on the last face relative to the centre
+    float ud2, disc, sd;        // reference: 2 d.(w - c), discriminant, its square root
+    float sigma;                // root sign: s = -ud + sigma*sd
+    float s, px2, py2, mb;      // reference root, 2 p_ref (rel. bound centre), |p|^2 - rho^2
+    float nx, ny;               // reference exit-face normal (c - p)/Rc
+    float ci, ci2, crsq, cr;    // reference cosines (ci2 = 2 ci)
+    float r, r2, kk;            // n_last, n_last^2, r ci - cr
+    float cid, gn, T, du, pos;  // reference detector cosine, (p - P).N, gn/cid, d'.u, position
+    uint32_t core_lo, core_hi;  // sorted-ray range that clears every flat face (fast path)
+    uint32_t band_lo, band_hi;  // [band_lo, core_lo) and [core_hi, band_hi): guard bands
+    uint32_t all_exact;         // no usable reference ray: every core ray is re-traced exactly
+    uint32_t pad[3];
+};
+
+// ----------------------------------------------------------------- exact f64 ops
+
+namespace x {
+CPD_HD double add(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+    return __dadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+CPD_HD double sub(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+    return __dsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+CPD_HD double mul(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+CPD_HD double div(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+    return __ddiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+CPD_HD double sqrt_(double a)
+{
+#if defined(__CUDA_ARCH__)
+    return __dsqrt_rn(a);
+#else
+    return std::sqrt(a);
+#endif
+}
+CPD_HD double fma_(double a, double b, double c)
+{
+#if defined(__CUDA_ARCH__)
+    return __fma_rn(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+CPD_HD double sqr(double a) { return mul(a, a); }
+CPD_HD double trunc_(double a)
+{
+#if defined(__CUDA_ARCH__)
+    return ::trunc(a);
+#else
+    return std::trunc(a);
+#endif
+}
+CPD_HD bool sign_positive(double a)
+{
+#if defined(__CUDA_ARCH__)
+    return !signbit(a);
+#else
+    return !std::signbit(a);
+#endif
+}
+
+// Horner with fused multiply-add from the highest-degree coefficient
+// (Glass::calc_n, glasscat.rs:17-22).
+CPD_HD double calc_n(const double *c, double w)
+{
+    double s = c[0];
+#pragma unroll
+    for (int i = 1; i < 6; i++) s = fma_(s, w, c[i]);
+    return s;
+}
+
+// UniformDistribution::inverse_cdf (distribution.rs:32-34).
+CPD_HD double wavelength(const DevDesign &D, double u) { return add(D.wmin, mul(sub(D.wmax, D.wmin), u)); }
+
+// GaussianBeam 2-D inverse_cdf (spectrometer.rs:26-30) given z = norminv(u).
+CPD_HD double beam_y(const DevDesign &D, double z) { return sub(D.bym, mul(D.bw, z)); }
+
+struct Ray {
+    double ox, oy, dx, dy, ts, tp;
+};
+
+CPD_HD double dot(double ax, double ay, double bx, double by) { return add(mul(ax, bx), mul(ay, by)); }
+
+// Ray::refract (ray.rs:309-367). Returns false on total internal reflection.
+CPD_HD bool refract(Ray &r, double nx, double ny, double n1, double n2, bool ar)
+{
+    double ci = -dot(r.dx, r.dy, nx, ny);
+    double rr = div(n1, n2);
+    double cr_sq = sub(1.0, mul(sqr(rr), sub(1.0, sqr(ci))));
+    if (cr_sq < 0.0) return false;
+    double cr = sqrt_(cr_sq);
+    double k = sub(mul(rr, ci), cr);
+    double vx = add(mul(r.dx, rr), mul(nx, k));
+    double vy = add(mul(r.dy, rr), mul(ny, k));
+    if (ar && ci > 0.5) {
+        r.ts = mul(r.ts, 0.99);
+        r.tp = mul(r.tp, 0.99);
+    } else {
+        double a = mul(n1, ci), b = mul(n2, cr);
+        double rs = sqr(div(sub(a, b), add(a, b)));
+        double c = mul(n1, cr), e = mul(n2, ci);
+        double rp = sqr(div(sub(c, e), add(c, e)));
+        r.ts = mul(r.ts, sub(1.0, rs));
+        r.tp = mul(r.tp, sub(1.0, rp));
+    }
+    r.dx = vx;
+    r.dy = vy;
+    return true;
+}
+
+// Error codes of the exact trace: 0 or a CPD_RAYTRACE_* status.
+constexpr int kNoHit = CPD_RAYTRACE_NO_SURFACE_INTERSECTION;
+constexpr int kTIR = CPD_RAYTRACE_TOTAL_INTERNAL_REFLECTION;
+constexpr int kWeak = CPD_RAYTRACE_ANGULAR_RESPONSE_TOO_WEAK;
+
+// Flat face k: HyperPlane::intersection with PrismBounds (geometry.rs:124-145, 62-67),
+// translate (ray.rs:281-294), refract. On error the ray is left unchanged.
+CPD_HD int flat_face(const DevDesign &D, int k, Ray &r, double n1, double n2)
+{
+    double nx = D.pnx[k], ny = D.pny[k];
+    double ci = dot(r.dx, r.dy, nx, ny);
+    if (ci == 0.0) return kNoHit;
+    double d = div(dot(sub(D.ppx[k], r.ox), sub(D.ppy[k], r.oy), nx, ny), ci);
+    if (!(d >= 0.0)) return kNoHit;
+    double hy = fma_(r.dy, d, r.oy);
+    if (!(0.0 <= hy && hy <= D.height)) return kNoHit;
+    Ray n = r;
+    n.ox = fma_(r.dx, d, r.ox);
+    n.oy = hy;
+    if (!refract(n, nx, ny, n1, n2, D.ar != 0)) return kTIR;
+    r = n;
+    return 0;
+}
+
+CPD_HD bool in_bound(const DevDesign &D, double px, double py)
+{
+    double ex = sub(px, D.cbx), ey = sub(py, D.cby);
+    return dot(ex, ey, ex, ey) <= D.cbr2;
+}
+
+// Curved exit face: SphericalLikeSurface::intersection + RadialBounds
+// (geometry.rs:161-216, 85-91), translate, refract into air. On error the ray is
+// left unchanged.
+CPD_HD int exit_face(const DevDesign &D, Ray &r, double n1)
+{
+    double deltax = sub(r.ox, D.ccx), deltay = sub(r.oy, D.ccy);
+    double ud = dot(r.dx, r.dy, deltax, deltay);
+    double disc = add(sub(sqr(ud), dot(deltax, deltay, deltax, deltay)), sqr(D.crad));
+    if (!(disc > 0.0)) return kNoHit;
+    double sd = sqrt_(disc);
+    double d1 = sub(-ud, sd), d2 = add(-ud, sd);
+    double p1x = fma_(r.dx, d1, r.ox), p1y = fma_(r.dy, d1, r.oy);
+    double px, py;
+    if (sign_positive(d1) && in_bound(D, p1x, p1y)) {
+        px = p1x;
+        py = p1y;
+    } else {
+        double p2x = fma_(r.dx, d2, r.ox), p2y = fma_(r.dy, d2, r.oy);
+        if (sign_positive(d2) && in_bound(D, p2x, p2y)) {
+            px = p2x;
+            py = p2y;
+        } else {
+            return kNoHit;
+        }
+    }
+    double nx = div(sub(D.ccx, px), D.crad), ny = div(sub(D.ccy, py), D.crad);
+    Ray n = r;
+    n.ox = px;
+    n.oy = py;
+    if (!refract(n, nx, ny, n1, 1.0, D.ar != 0)) return kTIR;
+    r = n;
+    return 0;
+}
+
+// Detector: Ray::intersect_detector_array + LinearDetectorArray::{intersection,
+// bin_index} (ray.rs:390-402, spectrometer.rs:265-303), euclid_div_rem and the
+// saturating f64->u32 cast (utils.rs:177-192).
+CPD_HD int detector(const DevDesign &D, const Ray &r, uint32_t &bin, double &t, double *hx = nullptr,
+                    double *hy = nullptr)
+{
+    double ci = -dot(r.dx, r.dy, D.dnx, D.dny);
+    if (ci <= D.min_ci) return kWeak;
+    double d = div(dot(sub(r.ox, D.dpx), sub(r.oy, D.dpy), D.dnx, D.dny), ci);
+    double px = fma_(r.dx, d, r.ox), py = fma_(r.dy, d, r.oy);
+    if (hx) {
+        *hx = px;
+        *hy = py;
+    }
+    double pos = dot(sub(px, D.dpx), sub(py, D.dpy), D.dux, D.duy);
+    if (pos < 0.0 || D.L < pos) return kNoHit;
+    double a = sub(pos, D.intercept);
+    double q = trunc_(div(a, D.slope));
+    double rem = sub(a, mul(q, D.slope));
+    if (rem < 0.0) {
+        q = D.slope > 0.0 ? sub(q, 1.0) : add(q, 1.0);
+        rem = add(rem, D.slope < 0.0 ? -D.slope : D.slope);
+    }
+    uint32_t b;
+    if (!(q == q) || q <= 0.0) b = 0;
+    else if (q >= 4294967295.0) b = 4294967295u;
+    else b = (uint32_t)q;
+    if (b < D.B && rem < D.bin_size) {
+        bin = b;
+        t = mul(add(r.ts, r.tp), 0.5);
+        return 0;
+    }
+    return kNoHit;
+}
+
+// CompoundPrism::propagate (ray.rs:485-499). `faces` counts the faces the ray
+// passed (for the propagation path); returns 0 or the first error.
+CPD_HD int prism(const DevDesign &D, double lambda, Ray &r, int *faces = nullptr)
+{
+    double n1 = calc_n(D.glass[0], lambda);
+    int e = flat_face(D, 0, r, 1.0, n1);
+    if (e) return e;
+    if (faces) *faces = 1;
+    for (int k = 1; k < D.G; k++) {
+        double n2 = calc_n(D.glass[k], lambda);
+        e = flat_face(D, k, r, n1, n2);
+        if (e) return e;
+        if (faces) *faces = k + 1;
+        n1 = n2;
+    }
+    e = exit_face(D, r, n1);
+    if (!e && faces) *faces = D.G + 1;
+    return e;
+}
+
+// Spectrometer::propagate (spectrometer.rs:421-427): exact f64 trace of one ray.
+// Returns 0 (hit: bin, t) or the RayTraceError code.
+CPD_HD int trace(const DevDesign &D, double lambda, double y, uint32_t &bin, double &t)
+{
+    Ray r{0.0, y, 1.0, 0.0, 1.0, 1.0};
+    int e = prism(D, lambda, r);
+    if (e) return e;
+    return detector(D, r, bin, t);
+}
+}  // namespace x
+
+// ----------------------------------------------------------------- per-wavelength setup
+
+// Guard widths of the fast path. A decision whose FP32 margin is inside its guard
+// is not trusted: the ray is re-traced with the exact model. The widths are
+// upper bounds on the FP32 error of each margin measured over random designs,
+// times a safety factor ("guard bands").
+struct Guards {
+    float pos;     // mm, detector coordinate vs 0, L and every bin edge
+    float cosine;  // exit-face cr^2, AR threshold 0.5, detector min_ci
+    float dist;    // mm, exit-face root sign
+    float rel;     // relative: discriminant, radial bound
+};
+// Measured over 40 random designs x 131k rays (host emulation of this code against
+// the exact trace): no wrong decision at 0.1x these widths, the first at 0.03x.
+CPD_HD Guards default_guards() { return Guards{1.0e-4f, 1.0e-5f, 1.0e-4f, 1.0e-5f}; }
+
+// Relative guard of the y-interval ends: both sides are f64, so a few ulps suffice.
+constexpr double kYGuardRel = 1e-11;
+
+// Splits an f64 into f32 hi + lo parts (hi + lo == v to about 2^-48 relative).
+CPD_HD void split_f32(double v, float &hi, float &lo)
+{
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// Traces candidate reference rays of the core range in f64 through the exit face and
+// onto the detector line, and stores the first one for which every quantity the fast
+// path differentiates is defined: a secant exit intersection inside the bound, no total
+// internal reflection and a detector cosine above 0.05. (ax, ay) + (bx, by)*y is the
+// position on the last flat face, (dx, dy) the direction entering the exit face,
+// r the index of the last glass. Returns false if no candidate qualifies.
+CPD_HDN inline bool reference_ray(const DevDesign &D, const double *zs, LamParams &P, double ax, double ay,
+                                  double bx, double by, double dx, double dy, double r)
+{
+    const uint32_t lo = P.core_lo, n = P.core_hi - P.core_lo;
+    const double vx = D.cbx - D.ccx, vy = D.cby - D.ccy;  // bound centre m minus sphere centre c
+    const double rc = D.crad, rho2 = D.cbr2;
+    const double qx = D.dpx - D.cbx, qy = D.dpy - D.cby;  // detector position minus m
+    const unsigned char at16[9] = {8, 4, 12, 2, 6, 10, 14, 1, 15};
+    for (int c = 0; c < 9; c++) {
+        uint32_t j = lo + (uint32_t)(((uint64_t)n * at16[c]) / 16u);
+        if (j >= P.core_hi) j = P.core_hi - 1;
+        const double z = zs[j];
+        const double y = D.bym - D.bw * z;
+        const double wx = ax + bx * y - D.cbx, wy = ay + by * y - D.cby;  // relative to m
+        const double ex_ = wx + vx, ey_ = wy + vy;                         // relative to c
+        const double ud = dx * ex_ + dy * ey_;
+        const double cq = (ex_ * ex_ + ey_ * ey_) - rc * rc;
+        const double disc = ud * ud - cq;
+        if (!(disc > 0.0)) continue;
+        const double sd = sqrt(disc);
+        const double d1 = -ud - sd, d2 = -ud + sd;
+        double sigma, s;
+        const double p1x = wx + dx * d1, p1y = wy + dy * d1;
+        const double p2x = wx + dx * d2, p2y = wy + dy * d2;
+        if (d1 >= 0.0 && p1x * p1x + p1y * p1y <= rho2) {
+            sigma = -1.0;
+            s = d1;
+        } else if (d2 >= 0.0 && p2x * p2x + p2y * p2y <= rho2) {
+            sigma = 1.0;
+            s = d2;
+        } else {
+            continue;
+        }
+        const double px = wx + dx * s, py = wy + dy * s;
+        const double mb = (px * px + py * py) - rho2;
+        const double nx = -(vx + px) / rc, ny = -(vy + py) / rc;
+        const double ci = -(dx * nx + dy * ny);
+        const double crsq = 1.0 - r * r * (1.0 - ci * ci);
+        if (!(crsq > 1e-6)) continue;
+        const double cr = sqrt(crsq);
+        const double kk = r * ci - cr;
+        const double ox = r * dx + kk * nx, oy = r * dy + kk * ny;
+        const double cid = -(ox * D.dnx + oy * D.dny);
+        if (!(cid > 0.05)) continue;
+        const double gx = px - qx, gy = py - qy;
+        const double gn = gx * D.dnx + gy * D.dny, gu = gx * D.dux + gy * D.duy;
+        const double T = gn / cid;
+        const double du = ox * D.dux + oy * D.duy;
+        const double pos = gu + du * T;
+        split_f32(z, P.zref_hi, P.zref_lo);
+        P.dlx2 = (float)(2.0 * ex_);
+        P.dly2 = (float)(2.0 * ey_);
+        P.ud2 = (float)(2.0 * ud);
+        P.disc = (float)disc;
+        P.sd = (float)sd;
+        P.sigma = (float)sigma;
+        P.s = (float)s;
+        P.px2 = (float)(2.0 * px);
+        P.py2 = (float)(2.0 * py);
+        P.mb = (float)mb;
+        P.nx = (float)nx;
+        P.ny = (float)ny;
+        P.ci = (float)ci;
+        P.ci2 = (float)(2.0 * ci);
+        P.crsq = (float)crsq;
+        P.cr = (float)cr;
+        P.r = (float)r;
+        P.r2 = (float)(r * r);
+        P.kk = (float)kk;
+        P.cid = (float)cid;
+        P.gn = (float)gn;
+        P.T = (float)T;
+        P.du = (float)du;
+        P.pos = (float)pos;
+        return true;
+    }
+    return false;
+}
+
+// Computes the per-wavelength parameters from the exact f64 flat-face chain, given
+// the sorted ray table zs[0..R) (ascending z = norminv(u)). Returns false if no ray of
+// this wavelength clears the flat faces (all lost); band ranges may still be non-empty.
+CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double *zs, uint32_t R,
+                                 LamParams &P, double yguard_rel = kYGuardRel)
+{
+    using namespace x;
+    {
+        // zero every field (the struct is plain data)
+        uint32_t *w = reinterpret_cast<uint32_t *>(&P);
+        for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
+    }
+    // direction/transmittance, exactly as the sequential trace computes them
+    double dx = 1.0, dy = 0.0, ts = 1.0, tp = 1.0;
+    // position affine in y: o(y) = (ax + bx*y, ay + by*y)
+    double ax = 0.0, ay = 0.0, bx = 0.0, by = 1.0;
+    double ylo = -INFINITY, yhi = INFINITY, glo = 0.0, ghi = 0.0;
+    double n1 = 1.0;
+    bool all_band = false;  // a y-independent constraint sits inside its guard: every ray is re-traced
+    auto constrain = [&](double c0, double c1, double scale) -> bool {
+        // c0 + c1*y >= 0 (up to rounding); returns false if no y satisfies it
+        double g = yguard_rel * (scale + 1.0);
+        if (c1 == 0.0) {
+            if (c0 < g && c0 > -g) all_band = true;
+            return c0 > -g;
+        }
+        double ys = -c0 / c1;
+        double gy = g / (c1 < 0.0 ? -c1 : c1);
+        if (c1 > 0.0) {
+            if (ys > ylo) { ylo = ys; glo = gy; }
+        } else {
+            if (ys < yhi) { yhi = ys; ghi = gy; }
+        }
+        return true;
+    };
+    bool ok = true;
+    for (int k = 0; k < D.G && ok; k++) {
+        double n2 = calc_n(D.glass[k], lambda);
+        double nx = D.pnx[k], ny = D.pny[k];
+        double ci = dot(dx, dy, nx, ny);
+        if (ci == 0.0) return false;
+        // dist(y) = ((P - o(y)).N)/ci = e0 + e1*y
+        double e0 = ((D.ppx[k] - ax) * nx + (D.ppy[k] - ay) * ny) / ci;
+        double e1 = -(bx * nx + by * ny) / ci;
+        double sc = (e0 < 0 ? -e0 : e0) + 30.0 * (e1 < 0 ? -e1 : e1) + D.height;
+        ok = ok && constrain(e0, e1, sc);                       // dist >= 0
+        double hy0 = ay + dy * e0, hy1 = by + dy * e1;          // hit y = hy0 + hy1*y
+        ok = ok && constrain(hy0, hy1, sc);                      // 0 <= hit y
+        ok = ok && constrain(D.height - hy0, -hy1, sc);          // hit y <= height
+        ax = ax + dx * e0;
+        ay = hy0;
+        bx = bx + dx * e1;
+        by = hy1;
+        Ray r{0.0, 0.0, dx, dy, ts, tp};
+        if (!refract(r, nx, ny, n1, n2, D.ar != 0)) return false;  // TIR: the same for every ray
+        dx = r.dx;
+        dy = r.dy;
+        ts = r.ts;
+        tp = r.tp;
+        n1 = n2;
+    }
+    if (!ok) return false;
+    // sorted-ray index ranges. y_j = bym - bw*z_j is monotone in j.
+    auto ycount = [&](double thr, bool above) -> uint32_t {
+        // number of j (from the low-z end if bw > 0) with y_j > thr (above) or >= thr
+        uint32_t lo = 0, hi = R;
+        // y decreasing in j when bw > 0
+        bool dec = D.bw > 0.0;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            double yj = beam_y(D, zs[mid]);
+            bool pred = above ? (yj > thr) : (yj >= thr);
+            // predicate true on a prefix when dec
+            if (dec ? pred : !pred) lo = mid + 1;
+            else hi = mid;
+        }
+        return lo;
+    };
+    if (all_band) {
+        P.band_lo = P.core_lo = P.core_hi = 0;
+        P.band_hi = R;
+    } else if (D.bw == 0.0) {
+        // every ray starts at the same height
+        double y = D.bym;
+        if (y < ylo - glo || y > yhi + ghi) return false;
+        if ((y < ylo + glo) || (y > yhi - ghi)) {
+            P.band_lo = 0;
+            P.core_lo = P.core_hi = 0;
+            P.band_hi = R;
+        } else {
+            P.band_lo = P.core_lo = 0;
+            P.core_hi = P.band_hi = R;
+        }
+    } else if (D.bw > 0.0) {
+        // j increasing <=> y decreasing: [yhi+g .. yhi-g] band first, core, [ylo+g .. ylo-g] band
+        P.band_lo = ycount(yhi + ghi, true);
+        P.core_lo = ycount(yhi - ghi, true);
+        P.core_hi = ycount(ylo + glo, false);
+        P.band_hi = ycount(ylo - glo, false);
+    } else {
+        P.band_lo = ycount(ylo - glo, false);
+        P.core_lo = ycount(ylo + glo, false);
+        P.core_hi = ycount(yhi - ghi, true);
+        P.band_hi = ycount(yhi + ghi, true);
+    }
+    if (P.core_hi < P.core_lo) P.core_hi = P.core_lo;
+    if (P.band_hi < P.core_hi) P.band_hi = P.core_hi;
+    if (P.band_lo > P.core_lo) P.band_lo = P.core_lo;
+    P.w1x = (float)bx;
+    P.w1y = (float)by;
+    P.dx = (float)dx;
+    P.dy = (float)dy;
+    P.ts = (float)ts;
+    P.tp = (float)tp;
+    if (P.core_hi > P.core_lo && !reference_ray(D, zs, P, ax, ay, bx, by, dx, dy, n1)) P.all_exact = 1;
+    return P.band_hi > P.band_lo;
+}
+
+// ----------------------------------------------------------------- FP32 fast path
+
+CPD_HD float fabs_f(float a) { return a < 0.f ? -a : a; }
+
+CPD_HD float sqrt_fast(float a)
+{
+#if defined(__CUDA_ARCH__)
+    return __fsqrt_rn(a);
+#else
+    return std::sqrt(a);
+#endif
+}
+CPD_HD float div_fast(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fdividef(a, b);
+#else
+    return a / b;
+#endif
+}
+
+// One ray through the exit face and onto the detector in FP32, as differences from
+// the wavelength's reference ray. (zhi, zlo) is the ray's z = norminv(u) split into
+// f32 parts; the ray is known to clear every flat face. Returns RAY_HIT with (bin, t),
+// RAY_LOST, or RAY_FLAG when any decision is inside its guard band.
+CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, float zhi, float zlo, uint32_t &bin,
+                    float &t)
+{
+    // start-height difference from the reference ray: y = bym - bw z
+    const float dz = (P.zref_hi - zhi) + (P.zref_lo - zlo);
+    const float dyy = D.bw * dz;
+    const float dwx = P.w1x * dyy, dwy = P.w1y * dyy;
+    // exit face: s^2 + 2 ud s + cq = 0, ud = d.(w - c), cq = |w - c|^2 - Rc^2
+    const float dud = fmaf(P.dx, dwx, P.dy * dwy);
+    const float dcq = fmaf(dwx, P.dlx2 + dwx, dwy * (P.dly2 + dwy));
+    const float ddisc = fmaf(dud, P.ud2 + dud, -dcq);
+    const float disc = P.disc + ddisc;
+    if (disc <= g.rel * P.disc) return disc > -g.rel * P.disc ? RAY_FLAG : RAY_LOST;
+    const float sd = sqrt_fast(disc);
+    // the other root is 2 sd away along the ray: outside the bound when sd > rho
+    bool flag = sd < 1.01f * D.rho;
+    const float dsd = div_fast(ddisc, sd + P.sd);
+    const float ds = fmaf(P.sigma, dsd, -dud);
+    const float s = P.s + ds;
+    flag |= fabs_f(s) < g.dist;
+    const float dpx = fmaf(P.dx, ds, dwx), dpy = fmaf(P.dy, ds, dwy);
+    const float mb = P.mb + fmaf(dpx, P.px2 + dpx, dpy * (P.py2 + dpy));
+    flag |= fabs_f(mb) < g.rel * D.rho2;
+    if (s < 0.f || mb > 0.f) return flag ? RAY_FLAG : RAY_LOST;
+    // refraction into air at the exit face, normal n = (c - p)/Rc
+    const float dnx = -dpx * D.inv_rc, dny = -dpy * D.inv_rc;
+    const float dci = -fmaf(P.dx, dnx, P.dy * dny);
+    const float ci = P.ci + dci;
+    const float dcr2 = P.r2 * dci * (P.ci2 + dci);
+    const float crsq = P.crsq + dcr2;
+    if (crsq < g.cosine) return crsq > -g.cosine ? RAY_FLAG : RAY_LOST;
+    const float cr = sqrt_fast(crsq);
+    const float dcr = div_fast(dcr2, cr + P.cr);
+    const float dkk = fmaf(P.r, dci, -dcr);
+    const float nx = P.nx + dnx, ny = P.ny + dny;
+    const float dex = fmaf(P.kk, dnx, dkk * nx), dey = fmaf(P.kk, dny, dkk * ny);
+    float ts = P.ts, tp = P.tp;
+    if (D.ar) flag |= fabs_f(ci - 0.5f) < g.cosine;
+    if (D.ar && ci > 0.5f) {
+        ts *= 0.99f;
+        tp *= 0.99f;
+    } else {
+        // 1 - Rs = 4 n1 n2 ci cr / (n1 ci + n2 cr)^2, 1 - Rp likewise with ci<->cr (n2 = 1)
+        const float r = P.r;
+        const float a = fmaf(r, ci, cr), b = fmaf(r, cr, ci);
+        const float a2 = a * a, b2 = b * b;
+        const float inv = div_fast(4.f * r * ci * cr, a2 * b2);
+        ts *= b2 * inv;
+        tp *= a2 * inv;
+    }
+    // detector line
+    const float dcid = -fmaf(dex, D.dnfx, dey * D.dnfy);
+    const float cid = P.cid + dcid;
+    if (cid <= D.min_ci + g.cosine) return cid > D.min_ci - g.cosine ? RAY_FLAG : RAY_LOST;
+    const float dgn = fmaf(dpx, D.dnfx, dpy * D.dnfy);
+    const float dgu = fmaf(dpx, D.dufx, dpy * D.dufy);
+    const float ddu = fmaf(dex, D.dufx, dey * D.dufy);
+    const float dT = div_fast(fmaf(dgn, P.cid, -P.gn * dcid), cid * P.cid);
+    const float dpos = fmaf(ddu, P.T + dT, fmaf(P.du, dT, dgu));
+    const float pos = P.pos + dpos;
+    if (pos < -g.pos || pos > D.L + g.pos) return RAY_LOST;
+    flag |= pos < g.pos || pos > D.L - g.pos;
+    const float xx = pos - D.c0;
+    float qf = floorf(xx * D.inv_slope);
+    float rem = fmaf(-qf, D.slope, xx);
+    if (rem < 0.f) {
+        qf -= 1.f;
+        rem += D.slope;
+    } else if (rem >= D.slope) {
+        qf += 1.f;
+        rem -= D.slope;
+    }
+    flag |= rem < g.pos || rem > D.slope - g.pos || fabs_f(rem - D.bin_size) < g.pos;
+    if (flag) return RAY_FLAG;
+    const uint32_t b = qf <= 0.f ? 0u : (uint32_t)qf;
+    if (b < D.B && rem < D.bin_size) {
+        bin = b;
+        t = (ts + tp) * 0.5f;
+        return RAY_HIT;
+    }
+    return RAY_LOST;
+}
+
+}  // namespace cpd

@@ -1,0 +1,226 @@
+/*
+ * cpd.h -- C ABI of the GB300 compound-prism spectrometer fitness library.
+ *
+ * This is the drop-in boundary for the fitness path of
+ * jdtatz/compound-prism-designer. Every entry point takes plain pointers and
+ * sizes and returns a cpd_status; nothing throws across the ABI. Each
+ * declaration names the reference interface it replaces (paths inside the
+ * reference project). A Rust -sys crate, a ctypes stub or a pyo3 shim binds
+ * this header unchanged (INTEGRATION.md shows the bindings).
+ *
+ * Units: lengths in millimetres, wavelengths in micrometres, angles in radians.
+ */
+#ifndef CPD_H
+#define CPD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CPD_ABI_VERSION 1
+#define CPD_MAX_GLASS 6            /* MAX_GLASS, src/pylib.rs:458 */
+#define CPD_MAX_BINS 1024
+#define CPD_MAX_WAVELENGTHS 65536  /* per design per call (max_n) */
+#define CPD_MAX_RAYS (1u << 22)    /* per wavelength (max_eval / max_m) */
+
+/* Status codes. The four RAYTRACE_* values are the variants of
+ * RayTraceError (src/spectrometer/ray.rs:10-16); NOT_CONVERGED is the `None`
+ * that cuda_fitness returns when the SEM stop is not met
+ * (src/cuda_fitness.rs:403-422). */
+typedef enum cpd_status {
+    CPD_OK = 0,
+    CPD_NOT_CONVERGED = 1,
+    CPD_RAYTRACE_NO_SURFACE_INTERSECTION = 2,
+    CPD_RAYTRACE_OUT_OF_BOUNDS = 3,
+    CPD_RAYTRACE_TOTAL_INTERNAL_REFLECTION = 4,
+    CPD_RAYTRACE_ANGULAR_RESPONSE_TOO_WEAK = 5,
+    CPD_INVALID_ARGUMENT = 6,
+    CPD_CUDA_ERROR = 7,
+    CPD_TIMEOUT = 8,
+    CPD_NO_CAPACITY = 9,
+    CPD_NOT_IMPLEMENTED = 10
+} cpd_status;
+
+/* Everything the reference's pyo3 constructors take for one 2-D spectrometer:
+ * CompoundPrism (src/pylib.rs:690-754), DetectorArray (src/pylib.rs:870-902),
+ * UniformWavelengthDistribution (src/pylib.rs:306-316), GaussianBeam
+ * (src/pylib.rs:365-372). */
+typedef struct cpd_spectrometer_params {
+    int32_t nglass;                        /* G, 1..6 (len(glasses)) */
+    int32_t ar_coated;
+    double glass[CPD_MAX_GLASS][6];        /* Glass coefficients, highest degree first */
+    double angles[CPD_MAX_GLASS + 1];      /* G+1 face angles */
+    double lengths[CPD_MAX_GLASS];         /* G separation lengths */
+    double curvature;                      /* signed normalized curvature of the exit face */
+    double height, width;
+    uint32_t bin_count;
+    int32_t det_flipped;
+    double bin_size, linear_slope, linear_intercept, det_length, max_incident_angle, det_angle;
+    double det_position[2];
+    double wavelength_bounds[2];
+    double beam_width, beam_y_mean;
+} cpd_spectrometer_params;
+
+/* A built design: the f64 surface and detector tables the fitness kernels read.
+ * Plain data; copy it freely. Built by cpd_design_build. */
+typedef struct cpd_design {
+    int32_t nglass;
+    uint32_t bin_count;
+    int32_t ar_coated;
+    int32_t reserved;
+    double glass[CPD_MAX_GLASS][6];
+    double face_point[CPD_MAX_GLASS][2];   /* entry face and inner faces */
+    double face_normal[CPD_MAX_GLASS][2];
+    double height;
+    double exit_center[2], exit_radius;    /* CurvedPlane exit face */
+    double exit_bound_center[2], exit_bound_r2;
+    double bin_size, linear_slope, linear_intercept, min_ci, det_length;
+    double det_normal[2], det_position[2], det_direction[2];
+    double wavelength_bounds[2];
+    double beam_width, beam_y_mean;
+    double size, deviation;                /* size_and_deviation (spectrometer.rs:429-437) */
+} cpd_design;
+
+/* Result of one fitness evaluation: DesignFitness (src/fitness.rs:36-41) plus
+ * diagnostics. */
+typedef struct cpd_fitness {
+    double size, info, deviation;
+    double h_cond;          /* mean over wavelengths of sum_d p log2 p  (= -H(D|L)) */
+    double h_det;           /* sum_d pbar log2 pbar                     (= -H(D))   */
+    double max_sem;         /* max over bins of the SEM of p(d|lambda) across wavelengths */
+    uint64_t rays;          /* rays evaluated */
+    uint64_t hits;          /* rays that reached a detector bin */
+    uint64_t retraced;      /* rays re-traced in exact f64 (guard band) */
+    uint64_t fast_rays;     /* rays evaluated by the FP32 fast path (exit face + detector) */
+    uint32_t wavelengths;   /* wavelength rows accumulated */
+    int32_t status;         /* CPD_OK or CPD_NOT_CONVERGED */
+} cpd_fitness;
+
+/* Trace precision of the GPU estimator. */
+enum {
+    CPD_TRACE_HYBRID = 0,   /* FP32 trace; rays within a guard band of any decision
+                               threshold are re-traced in exact f64 (default) */
+    CPD_TRACE_FP32 = 1,     /* FP32 trace only, no re-trace (precision study) */
+    CPD_TRACE_FP64 = 2      /* every ray in exact f64 (precision study reference) */
+};
+
+typedef struct cpd_context cpd_context;
+
+/* ---------------------------------------------------------------- host side */
+
+int cpd_abi_version(void);
+const char *cpd_status_string(int status);
+
+/* position_detector_array (src/pylib.rs:815-838 -> detector_array_positioning,
+ * src/spectrometer/spectrometer.rs:322-364). Reads the prism, source, det_length
+ * and det_angle fields of `p`. */
+int cpd_position_detector_array(const cpd_spectrometer_params *p, double acceptance,
+                                double position_out[2], int32_t *flipped_out);
+
+/* Builds the design tables: CompoundPrism::new (src/spectrometer/ray.rs:137-183),
+ * LinearDetectorArray::new (src/spectrometer/spectrometer.rs:183-219) and the
+ * argument checks of SizedCompoundPrism::new (src/pylib.rs:514-561). */
+int cpd_design_build(const cpd_spectrometer_params *p, cpd_design *out);
+
+/* CompoundPrism.exit_ray (src/pylib.rs:563-573): out = {x, y, dir x, dir y}. */
+int cpd_exit_ray(const cpd_design *d, double y, double wavelength, double out[4]);
+
+/* Spectrometer.ray_trace / propagation_path (src/pylib.rs:1061-1083,
+ * spectrometer.rs:439-464): rows of (x, y, dir x, dir y), at most G+3. */
+int cpd_ray_trace(const cpd_design *d, double wavelength, double initial_y, double *rows,
+                  uint32_t *nrows);
+
+/* Spectrometer.cpu_fitness (src/pylib.rs:1010-1026 -> src/fitness.rs:130-147):
+ * the reference's adaptive f64 estimator on the host. An explicit CPU method of
+ * the reference API; the GPU entry points never call it. */
+int cpd_fitness_cpu(const cpd_design *d, uint64_t max_n, uint64_t max_m, cpd_fitness *out);
+
+/* The f64 inverse normal CDF the ray tables use (src/spectrometer/erf.rs:62-73). */
+double cpd_norminv(double u);
+
+/* Glass.__call__ -> Glass::calc_n (src/pylib.rs:76-78, src/spectrometer/glasscat.rs:17-22):
+ * index of refraction at wavelength w (micrometres) from the 6 Horner coefficients. */
+double cpd_glass_index(const double coeffs[6], double w);
+
+/* ---------------------------------------------------------------- GPU side */
+
+/* CudaFitnessContext::new / quick_init / set_cached_cuda_context
+ * (src/cuda_fitness.rs:187-197, 324-329, 362-363): one context per GPU; owns a
+ * stream, pooled device buffers and captured CUDA graphs. Thread-safe. */
+int cpd_context_create(int device, cpd_context **out);
+void cpd_context_destroy(cpd_context *ctx);
+
+/* cuda_fitness (src/cuda_fitness.rs:347-423), Spectrometer.gpu_fitness
+ * (src/pylib.rs:1088-1135): for each seed, max_n wavelengths
+ * u_i = fract(seed + i/phi) and max_eval rays u_j = fract(seed + (j+1)/phi);
+ * p(d|lambda) accumulated in FP64; stops at the first seed after which every
+ * bin's SEM across wavelengths is <= 5e-3 (status CPD_OK), else
+ * CPD_NOT_CONVERGED with the estimate of all seeds. nwarp is the block-shape
+ * hint of the reference (warps per CTA). */
+int cpd_fitness_gpu(cpd_context *ctx, const cpd_design *d, const double *seeds, uint32_t nseeds,
+                    uint32_t max_n, uint32_t nwarp, uint32_t max_eval, cpd_fitness *out);
+
+/* Fixed-N estimator on explicit point sets (the parity entry point): W wavelength
+ * u-points and R ray u-points, every wavelength traced with all R rays
+ * (prob_dets_given_wavelengths, src/spectrometer/kernel.rs:89-193, on given
+ * points). p_out (optional, W*B, row-major) receives p(d|lambda). trace_mode is a
+ * CPD_TRACE_* value. */
+int cpd_fitness_gpu_points(cpd_context *ctx, const cpd_design *d, const double *lam_u, uint32_t W,
+                           const double *ray_u, uint32_t R, uint32_t trace_mode, cpd_fitness *out,
+                           double *p_out);
+
+/* Spectrometer.transmission_probability (src/pylib.rs:1029-1058): p(d|lambda) for
+ * explicit wavelengths, max_m rays each (fixed N: no early SEM stop).
+ * out is n*B row-major. */
+int cpd_transmission_probability(cpd_context *ctx, const cpd_design *d, const double *wavelengths,
+                                 uint32_t n, uint32_t max_m, double *out);
+
+/* launch_propagation_test / propagation_test_kernel (src/cuda_fitness.rs:247-317,
+ * src/spectrometer/kernel.rs:195-224): one ray per (lam_u[i], ray_u[i]) pair.
+ * bins[i] = bin index or bin_count for a lost ray; ts[i] = transmittance;
+ * flags[i] (optional) = 1 where the ray was re-traced in exact f64. */
+int cpd_trace_rays(cpd_context *ctx, const cpd_design *d, const double *lam_u, const double *ray_u,
+                   uint32_t n, uint32_t trace_mode, uint32_t *bins, double *ts, uint8_t *flags);
+
+/* Per-design sampling plan of a batched launch. */
+typedef struct cpd_batch_item {
+    double seed;        /* point-set seed, as cpd_fitness_gpu */
+    uint32_t max_n;     /* W, wavelengths */
+    uint32_t max_eval;  /* R, rays per wavelength */
+} cpd_batch_item;
+
+/* Batched form (no reference counterpart; the reference evaluates one design per
+ * call, designer.py:267-300): n designs of mixed G, B, W, R in one captured
+ * launch sequence. outs[i].status is CPD_OK or CPD_NOT_CONVERGED per design. */
+int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items,
+                          uint32_t n, uint32_t trace_mode, cpd_fitness *outs);
+
+/* Launch-shape tuning of the batched/plain kernels (ray tile = rays per lane per
+ * work item, warps per CTA). 0 leaves a value unchanged. */
+int cpd_set_launch_shape(cpd_context *ctx, uint32_t ray_tile, uint32_t warps_per_cta);
+int cpd_get_launch_shape(cpd_context *ctx, uint32_t *ray_tile, uint32_t *warps_per_cta);
+
+/* Device time of the last GPU call's kernels (CUDA events on the context stream), ms,
+ * and the number of kernel launches it issued. */
+int cpd_last_timing(cpd_context *ctx, double *kernel_ms, uint32_t *launches);
+
+/* Per-kernel timing: when on, each pass is launched without graph replay and CUDA
+ * events bracket every kernel; cpd_last_kernel_times then returns the last pass's
+ * {setup, trace, retrace, entropy} device times in ms. */
+int cpd_set_profiling(cpd_context *ctx, int on);
+int cpd_last_kernel_times(cpd_context *ctx, double ms[4]);
+
+/* Host->device and device->host bytes the last GPU call copied. */
+int cpd_last_transfer_bytes(cpd_context *ctx, uint64_t *h2d, uint64_t *d2h);
+
+/* FP32 FMA throughput probe: runs a dependent-chain-free FMA kernel for `iters`
+ * iterations on every SM and returns the achieved TFLOP/s (roofline peak). */
+int cpd_measure_fp32_peak(cpd_context *ctx, uint32_t iters, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

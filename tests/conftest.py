@@ -13,6 +13,14 @@ for p in (ROOT, PKG_DIR, os.path.join(ROOT, "oracle")):
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
+# Build (or refresh) the product library and the oracle before any test imports them.
+import build_ext  # noqa: E402  (compound-prism-designer_gb300/build_ext.py)
+
+build_ext.build()
+import oracle as _oracle  # noqa: E402
+
+_oracle.build()
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")

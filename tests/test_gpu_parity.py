@@ -1,0 +1,207 @@
+"""GPU parity: the CUDA fitness path against the C oracle on identical points.
+
+Tolerances (the benchmark spec):
+* hit-bin index: exactly equal for every ray (the hybrid trace re-traces every ray
+  inside a guard band of any decision in exact f64, bit-identical to the oracle);
+* transmittance of a ray: FP32 fast path within 2e-6 relative, exact-f64 re-traced
+  rays bit-identical;
+* p(d|lambda): within 1e-6 absolute;
+* mutual information: within 1e-4 relative (the observed error is stated per case).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import compound_prism_designer as cpd
+from compound_prism_designer import synth
+
+pytestmark = pytest.mark.gpu
+
+ALPHA = 1.0 / 1.61803398874989484820458683436563
+NTHREADS = max(1, min(16, os.cpu_count() or 1))
+
+
+@pytest.fixture(scope="module")
+def designs(f1):
+    rng = np.random.default_rng(20261203)
+    out = [("F1", synth.spectrometer_from_dict(f1), f1)]
+    for G, B in [(2, 16), (3, 32), (4, 64), (5, 128), (6, 64), (6, 128), (1, 32)]:
+        s, d, _ = synth.random_design(rng, G, B)
+        out.append((f"G{G}B{B}", s, d))
+    return out
+
+
+def _pairs(n, seed):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(0.0, 1.0, n), rng.uniform(1e-9, 1.0 - 1e-9, n)
+
+
+def test_trace_rays_hybrid_bins_equal_oracle(designs):
+    for name, s, d in designs:
+        lam_u, ray_u = _pairs(16384, 1)
+        bins, ts, flag = s.trace_rays(lam_u, ray_u, mode=cpd.TRACE_HYBRID)
+        bo, to = O.trace_pairs(d, lam_u, ray_u)
+        assert np.array_equal(bins, bo), (name, np.nonzero(bins != bo)[0][:10])
+        hit = bo < d["bin_count"]
+        rel = np.abs(ts[hit] - to[hit]) / to[hit]
+        assert rel.max(initial=0) <= 2e-6, (name, rel.max())
+        assert np.array_equal(ts[flag], to[flag]), name
+
+
+def test_trace_rays_fp64_bit_identical(designs):
+    for name, s, d in designs:
+        lam_u, ray_u = _pairs(4096, 2)
+        bins, ts, _ = s.trace_rays(lam_u, ray_u, mode=cpd.TRACE_FP64)
+        bo, to = O.trace_pairs(d, lam_u, ray_u)
+        assert np.array_equal(bins, bo), name
+        assert np.array_equal(ts, to), name
+
+
+def _check_fitness(s, d, W, R, seed=0.5, mode=cpd.TRACE_HYBRID, p_tol=1e-6, mi_tol=1e-4):
+    lam_u = O.qrng_points(seed, W)
+    ray_u = O.qrng_points(seed, R)
+    f, p = s.gpu_fitness_points(lam_u, ray_u, mode=mode, want_p=True)
+    po, st = O.fitness_points(d, lam_u, ray_u, nthreads=NTHREADS)
+    err_p = np.abs(p - po).max()
+    mi_rel = abs(f.info - st["info"]) / max(abs(st["info"]), 1e-300)
+    assert err_p <= p_tol, (err_p, W, R)
+    # relative bound, with an absolute floor for MI = 0 (one wavelength): the fixed-point
+    # accumulators quantize each p log2 p to 2^-40
+    assert abs(f.info - st["info"]) <= mi_tol * abs(st["info"]) + 1e-9, (f.info, st["info"], mi_rel)
+    assert f.hits == st["hits"]
+    assert f.rays == W * R and f.wavelengths == W
+    return err_p, mi_rel, f
+
+
+def test_fitness_points_reference_cpu_config(designs):
+    # config 0 shape: 3 prisms, 32 bins, 64 wavelengths x 256 rays
+    rng = np.random.default_rng(100)
+    s, d, _ = synth.random_design(rng, 3, 32)
+    err_p, mi_rel, f = _check_fitness(s, d, 64, 256)
+    print(f"config0: max |dp| {err_p:.2e}, MI rel err {mi_rel:.2e}, retraced {f.retraced}")
+
+
+def test_fitness_points_all_designs(designs):
+    for name, s, d in designs:
+        err_p, mi_rel, f = _check_fitness(s, d, 256, 1024)
+        print(f"{name}: max |dp| {err_p:.2e}, MI rel err {mi_rel:.2e}, retraced {f.retraced}/{f.rays}")
+
+
+def test_fitness_points_plain_gpu_config_full_size():
+    # config 1: 6 prisms, 64 bins, 4096 wavelengths x 1024 rays (4.2M rays)
+    rng = np.random.default_rng(20261204)
+    s, d, _ = synth.random_design(rng, 6, 64)
+    err_p, mi_rel, f = _check_fitness(s, d, 4096, 1024)
+    print(f"config1: max |dp| {err_p:.2e}, MI rel err {mi_rel:.2e}, retraced {f.retraced}")
+
+
+def test_fp64_mode_fitness_tight(designs):
+    for name, s, d in designs[:4]:
+        _check_fitness(s, d, 64, 512, mode=cpd.TRACE_FP64, p_tol=1e-12, mi_tol=1e-10)
+
+
+def test_fp32_mode_close_to_oracle(designs):
+    # the FP32-only study mode is not held to exact bins; it must stay close
+    for name, s, d in designs[:3]:
+        lam_u = O.qrng_points(0.5, 128)
+        ray_u = O.qrng_points(0.5, 512)
+        f, _ = s.gpu_fitness_points(lam_u, ray_u, mode=cpd.TRACE_FP32)
+        _, st = O.fitness_points(d, lam_u, ray_u, nthreads=NTHREADS)
+        assert abs(f.info - st["info"]) <= 1e-2 * max(abs(st["info"]), 1e-3)
+        assert f.retraced == 0
+
+
+def test_gpu_fitness_seed_policy_equals_points(designs):
+    name, s, d = designs[3]
+    seed = 0.3141
+    W, R = 256, 1024
+    full = s.gpu_fitness_full([seed], max_n=W, max_eval=R)
+    # the documented point policy: u_i = fract(fma(i, 1/phi, seed)), rays from i = 1
+    lam = _policy_points(seed, 0, W)
+    ray = _policy_points(seed, 1, R)
+    f2, _ = s.gpu_fitness_points(lam, ray)
+    assert full.info == f2.info and full.h_det == f2.h_det
+    po, st = O.fitness_points(d, lam, ray, nthreads=NTHREADS)
+    assert abs(full.info - st["info"]) <= 1e-4 * abs(st["info"])
+
+
+def _policy_points(seed, first, n):
+    import math
+    from fractions import Fraction
+
+    def fma(a, b, c):  # correctly rounded a*b + c
+        return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+    out = []
+    for i in range(first, first + n):
+        v = fma(float(i), ALPHA, seed)
+        out.append(v - math.trunc(v))
+    return np.array(out)
+
+
+def test_gpu_fitness_convergence_semantics(designs):
+    name, s, d = designs[0]
+    # 8 wavelengths cannot meet the 5e-3 SEM stop on every bin: None, as the reference returns
+    assert s.gpu_fitness([0.2], max_n=8, max_eval=256) is None
+    f = s.gpu_fitness_full([0.2, 0.7], max_n=8, max_eval=256)
+    assert f.status == 1 and f.wavelengths == 16
+
+
+def test_batch_equals_single_bitwise(designs):
+    specs = [s for _, s, _ in designs]
+    mn = [64 + 32 * i for i in range(len(specs))]
+    outs = cpd.fitness_batch(specs, seeds=0.4, max_n=mn, max_eval=512)
+    for i, s in enumerate(specs):
+        alone = s.gpu_fitness_full([0.4], max_n=mn[i], max_eval=512)
+        assert outs[i].info == alone.info, i
+        assert outs[i].h_det == alone.h_det and outs[i].hits == alone.hits
+
+
+def test_launch_shapes_give_identical_bits(designs):
+    name, s, d = designs[5]
+    ctx = cpd.default_context()
+    lam_u = O.qrng_points(0.5, 128)
+    ray_u = O.qrng_points(0.5, 1024)
+    ref = None
+    old = ctx.launch_shape()
+    try:
+        for rt, w in [(8, 2), (32, 8), (128, 4), (1024, 8), (5, 1)]:
+            ctx.set_launch_shape(rt, w)
+            f, p = s.gpu_fitness_points(lam_u, ray_u, want_p=True)
+            if ref is None:
+                ref = (f.info, p)
+            assert f.info == ref[0] and np.array_equal(p, ref[1]), (rt, w)
+    finally:
+        ctx.set_launch_shape(*old)
+
+
+def test_transmission_probability_vs_oracle(designs):
+    name, s, d = designs[0]
+    w = np.linspace(0.5, 0.82, 17)
+    p = s.transmission_probability(w, max_m=1024)
+    dd = dict(d)
+    dd["wavelength_bounds"] = (0.0, 1.0)
+    po, _ = O.fitness_points(dd, w, O.qrng_points(0.5, 1024))
+    assert np.abs(p - po).max() <= 1e-6
+
+
+def test_edge_cases(designs):
+    name, s, d = designs[1]
+    # one wavelength, one ray; ragged sizes
+    for W, R in [(1, 1), (1, 33), (33, 1), (31, 97)]:
+        _check_fitness(s, d, W, R)
+    # a detector moved far off the beam: every ray is lost, MI is 0
+    dd = dict(d)
+    dd["det_position"] = (d["det_position"][0] + 1e4, d["det_position"][1] + 1e4)
+    s2 = synth.spectrometer_from_dict(dd)
+    f, p = s2.gpu_fitness_points(O.qrng_points(0.5, 16), O.qrng_points(0.5, 64), want_p=True)
+    assert f.hits == 0 and not p.any() and f.info == 0.0
+
+
+def test_repeat_calls_identical(designs):
+    name, s, d = designs[2]
+    a = s.gpu_fitness_full([0.6], max_n=128, max_eval=2048)
+    b = s.gpu_fitness_full([0.6], max_n=128, max_eval=2048)
+    assert a.as_dict() == b.as_dict()
