@@ -131,6 +131,7 @@ SIGNATURES = [
     ("cpd_fitness_cpu", C.c_int, [C.POINTER(Design), C.c_uint64, C.c_uint64, C.POINTER(Fitness)]),
     ("cpd_norminv", C.c_double, [C.c_double]),
     ("cpd_glass_index", C.c_double, [_dp, C.c_double]),
+    ("cpd_entropy_log2", C.c_int, [C.c_uint64, _dp]),
     ("cpd_context_create", C.c_int, [C.c_int, C.POINTER(_ctxp)]),
     ("cpd_context_destroy", None, [_ctxp]),
     ("cpd_fitness_gpu", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,

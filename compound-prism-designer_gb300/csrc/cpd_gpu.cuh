@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include "cpd_ff.h"
 #include "cpd_model.h"
 
 namespace cpd {
@@ -24,6 +25,8 @@ struct alignas(16) DesignJob {
     uint32_t tile_rows;  // wavelength rows per entropy tile
     uint32_t ntiles;
     uint32_t pad;
+    float unit_hi, unit_lo;  // p per count unit, 2^-31 / R, float-float
+    float lu_hi, lu_lo;      // log2 of that unit, float-float
 };
 
 // A ray whose FP32 result fell inside a guard band: (design, wavelength row, ray).
@@ -67,6 +70,7 @@ struct LaunchArgs {
     const double *z64;
     const float *z32;     // (hi, lo) f32 pairs of the sorted z table
     LamParams *lp;
+    ExactLam *lx;         // per row: exact flat-face data for the re-trace
     unsigned long long *hist;
     unsigned long long *S1;
     unsigned long long *S2;
@@ -81,6 +85,7 @@ struct LaunchArgs {
     Guards guards;
     double yguard_rel;
     double *p_out;        // optional W x B for the single design of the launch
+    const float *logtab;  // float-float log2 table (cpd_ff.h), 4 x 256 floats
 };
 
 // Launches setup -> trace -> retrace -> entropy on `stream`. Returns the number of

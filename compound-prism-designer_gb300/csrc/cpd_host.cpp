@@ -7,6 +7,7 @@
 #include <cstring>
 #include <vector>
 
+#include "cpd_ff.h"
 #include "cpd_host.h"
 #include "cpd_model.h"
 
@@ -219,6 +220,21 @@ const char *cpd_status_string(int s)
 double cpd_norminv(double u) { return cpd::norminv(u); }
 
 double cpd_glass_index(const double coeffs[6], double w) { return x::calc_n(coeffs, w); }
+
+int cpd_entropy_log2(uint64_t count, double out[2])
+{
+    if (!out || count == 0) return CPD_INVALID_ARGUMENT;
+    static float tab[4 * ff::kLogTable];
+    static bool ready = [] {
+        ff::make_log_table(tab);
+        return true;
+    }();
+    (void)ready;
+    const ff::F2 l = ff::log2_u64(count, tab);
+    out[0] = l.hi;
+    out[1] = l.lo;
+    return CPD_OK;
+}
 
 int cpd_position_detector_array(const cpd_spectrometer_params *p, double acceptance, double position_out[2],
                                 int32_t *flipped_out)

@@ -49,7 +49,7 @@ __device__ __forceinline__ void push_ray(const LaunchArgs &a, uint32_t d, uint32
     else atomicOr(&a.ctl->overflow, 1u);
 }
 
-__global__ void __launch_bounds__(128) setup_kernel(const LaunchArgs a)
+__global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
 {
     const uint64_t row = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (row >= a.total_rows) return;
@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const LaunchArgs a)
     const DevDesign &D = a.designs[d];
     const double lambda = x::wavelength(D, a.lam_u[J.lam_off + k]);
     LamParams P;
-    lambda_setup(D, lambda, a.z64 + J.ray_off, J.Rz, P, a.yguard_rel);
+    lambda_setup(D, lambda, a.z64 + J.ray_off, J.Rz, P, a.yguard_rel, a.lx + row);
     if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
         for (uint32_t j = P.band_lo; j < P.band_hi; j++) push_ray(a, d, k, j);
         P.core_lo = P.core_hi = 0;
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const LaunchArgs a)
     a.lp[row] = P;
 }
 
-__global__ void __launch_bounds__(256) trace_kernel(const LaunchArgs a)
+__global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
 {
     const uint32_t lane = threadIdx.x & 31u;
     for (;;) {
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const LaunchArgs a)
                     cur = bin;
                     sum = 0ull;
                 }
-                sum += __float2ull_rn(t * 1099511627776.0f);
+                sum += t_fixed(t);
                 nhit++;
             } else if (r == RAY_FLAG) {
                 push_ray(a, d, k, j);
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const LaunchArgs a)
     }
 }
 
-__global__ void __launch_bounds__(128) retrace_kernel(const LaunchArgs a)
+__global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
 {
     const unsigned long long qn = a.ctl->queue_count;
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
@@ -137,12 +137,11 @@ __global__ void __launch_bounds__(128) retrace_kernel(const LaunchArgs a)
         const QEntry e = a.queue[i];
         const DevDesign &D = a.designs[e.design];
         const DesignJob &J = a.jobs[e.design];
-        const double lambda = x::wavelength(D, a.lam_u[J.lam_off + e.k]);
         const double y = x::beam_y(D, a.z64[J.ray_off + e.j]);
         uint32_t bin = 0;
         double t = 0.0;
-        if (x::trace(D, lambda, y, bin, t) == 0) {
-            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, __double2ull_rn(t * kTScale));
+        if (x::trace_lam(D, a.lx[J.row_off + e.k], y, bin, t) == 0) {
+            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, (unsigned long long)t_fixed64(t));
             atomicAdd(&a.acc[e.design].hits, 1ull);
         }
         atomicAdd(&a.acc[e.design].retraced, 1ull);
@@ -170,8 +169,9 @@ __device__ void finalize(const LaunchArgs &a, uint32_t d, const DesignJob &J)
     const double e2 = 5e-3 * 5e-3;
     double hdet = 0.0, msem = 0.0;
     int conv = 1;
+    const double p_unit = kTScaleInv / (double)J.R;  // p per count unit
     for (uint32_t b = tid; b < J.B; b += blockDim.x) {
-        const double s1 = (double)__ldcg(&a.S1[J.acc_off + b]) * kPScaleInv;
+        const double s1 = (double)__ldcg(&a.S1[J.acc_off + b]) * p_unit;  // sum over rows of p
         const double s2 = (double)__ldcg(&a.S2[J.acc_off + b]) * kPScaleInv;
         const double pbar = s1 / n;
         if (pbar > 0.0) hdet += pbar * log2(pbar);
@@ -214,15 +214,22 @@ __device__ void finalize(const LaunchArgs &a, uint32_t d, const DesignJob &J)
     }
 }
 
+// Thread -> (bin, row group) map of an entropy tile: for B <= 256 each thread owns one
+// bin and every (256/B)-th row of the tile; for wider detectors each thread owns the
+// bins tid, tid+256, ... of every row. Per-thread partial sums are therefore fixed by
+// B alone, whatever else shares the launch.
 __global__ void __launch_bounds__(kEntropyThreads) entropy_kernel(const LaunchArgs a)
 {
     extern __shared__ unsigned long long sm[];  // S1[B], S2[B] of this tile
     __shared__ unsigned long long hsum;
     __shared__ int last;
+    __shared__ float tab[4 * ff::kLogTable];
     const uint32_t tid = threadIdx.x;
     // A pass whose re-trace queue overflowed is re-run by the host: leave every
     // accumulator untouched.
     if (a.ctl->overflow || a.ctl->queue_count > a.qcap) return;
+    for (uint32_t i = tid; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
+    __syncthreads();
     for (uint64_t tile = blockIdx.x; tile < a.total_tiles; tile += gridDim.x) {
         const uint32_t d = find_job<F_TILE>(a.jobs, a.njobs, tile);
         const DesignJob J = a.jobs[d];
@@ -233,24 +240,38 @@ __global__ void __launch_bounds__(kEntropyThreads) entropy_kernel(const LaunchAr
         for (uint32_t b = tid; b < 2 * B; b += blockDim.x) sm[b] = 0ull;
         if (tid == 0) hsum = 0ull;
         __syncthreads();
-        unsigned long long hl = 0ull;
-        const uint32_t nent = (r1 - r0) * B;
-        const double inv_r = 1.0 / (double)J.R;
-        unsigned long long *base = a.hist + J.hist_off + (uint64_t)r0 * B;
-        for (uint32_t e = tid; e < nent; e += blockDim.x) {
-            const unsigned long long c = base[e];
-            double p = 0.0;
-            if (c) {
-                base[e] = 0ull;  // leaves the histogram zeroed for the next pass
-                p = (double)c * kTScaleInv * inv_r;
-                const double h = p * log2(p);
-                hl += __double2ull_rn(-h * kHScale);
-                const uint32_t bin = e % B;
-                atomicAdd(&sm[bin], __double2ull_rn(p * kPScale));
-                atomicAdd(&sm[B + bin], __double2ull_rn(p * p * kPScale));
+        const double p_unit = kTScaleInv / (double)J.R;
+        const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
+        unsigned long long *base = a.hist + J.hist_off;
+        const uint32_t groups = B <= (uint32_t)kEntropyThreads ? (uint32_t)kEntropyThreads / B : 1u;
+        const uint32_t grp = tid / (B <= (uint32_t)kEntropyThreads ? B : (uint32_t)kEntropyThreads);
+        const uint32_t bin0 = B <= (uint32_t)kEntropyThreads ? tid % B : tid;
+        ff::F2 h{0.f, 0.f};
+        if (grp < groups) {
+            for (uint32_t b = bin0; b < B; b += kEntropyThreads) {
+                unsigned long long c1 = 0ull;
+                ff::F2 q2{0.f, 0.f};
+                for (uint32_t row = r0 + grp; row < r1; row += groups) {
+                    unsigned long long *cell = base + (uint64_t)row * B + b;
+                    const unsigned long long c = *cell;
+                    if (c) {
+                        *cell = 0ull;  // leaves the histogram zeroed for the next pass
+                        // p = c unit and p log2 p in float-float (FP32 pipe)
+                        const ff::F2 p = ff::mul(ff::from_u64(c), unit);
+                        const ff::F2 lp = ff::add(ff::log2_u64(c, tab), lu);
+                        h = ff::add(h, ff::mul(p, lp));
+                        q2 = ff::add(q2, ff::mul(p, p));
+                        c1 += c;
+                    }
+                    if (a.p_out) a.p_out[(uint64_t)row * B + b] = (double)c * p_unit;
+                }
+                if (c1) {
+                    atomicAdd(&sm[b], c1);
+                    atomicAdd(&sm[B + b], __double2ull_rn(((double)q2.hi + (double)q2.lo) * kPScale));
+                }
             }
-            if (a.p_out) a.p_out[(uint64_t)r0 * B + e] = p;
         }
+        unsigned long long hl = __double2ull_rn(-((double)h.hi + (double)h.lo) * kHScale);
         hl = warp_sum_u64(hl);
         if ((tid & 31u) == 0 && hl) atomicAdd(&hsum, hl);
         __syncthreads();
@@ -355,8 +376,9 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     int launches = 0;
     if (ev) cudaEventRecord(ev[0], stream);
     if (a.total_rows) {
-        const uint32_t blocks = (uint32_t)((a.total_rows + 127) / 128);
-        setup_kernel<<<blocks, 128, 0, stream>>>(a);
+        // one warp per block: f64-pipe bound, so spreading rows over every SM matters
+        const uint32_t blocks = (uint32_t)((a.total_rows + 31) / 32);
+        setup_kernel<<<blocks, 32, 0, stream>>>(a);
         launches++;
     }
     if (ev) cudaEventRecord(ev[1], stream);
@@ -372,7 +394,7 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         launches++;
     }
     if (ev) cudaEventRecord(ev[2], stream);
-    retrace_kernel<<<(unsigned)(num_sms * 4), 128, 0, stream>>>(a);
+    retrace_kernel<<<(unsigned)(num_sms * 8), 32, 0, stream>>>(a);
     launches++;
     if (ev) cudaEventRecord(ev[3], stream);
     if (a.total_tiles) {

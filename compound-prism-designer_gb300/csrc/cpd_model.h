@@ -23,6 +23,7 @@
 
 #include <cstdint>
 #include <cmath>
+#include <cstring>
 
 #include "../../include/cpd.h"
 
@@ -38,14 +39,37 @@ namespace cpd {
 
 // 1/phi, the 1-D R1 sequence step (qrng.rs:156-158, kernel.rs:107-108).
 constexpr double kAlpha = 1.0 / 1.61803398874989484820458683436563;
-// Fixed-point scale of a ray's transmittance in the per-(wavelength, bin) sums.
-constexpr double kTScale = 1099511627776.0;          // 2^40
-constexpr double kTScaleInv = 1.0 / 1099511627776.0;
-// Fixed-point scales of the per-design accumulators.
-constexpr double kPScale = 70368744177664.0;         // 2^46, sum over wavelengths of p and p^2
+// Fixed-point scale of a ray's transmittance t in [0, 1]: one u32 per ray (2^31 t,
+// truncated), summed into u64 per (wavelength, bin) cell and per bin over wavelengths.
+// The sums are integers, so they do not depend on the order rays are accumulated in.
+// A cell holds at most R 2^31 <= 2^53; a per-bin sum over W rows at most W R 2^31,
+// which stays below 2^63 while W R <= 2^32 (checked on the host).
+constexpr double kTScale = 2147483648.0;             // 2^31
+constexpr double kTScaleInv = 1.0 / 2147483648.0;
+// Fixed-point scales of the per-design accumulators of p^2 and -p log2 p.
+constexpr double kPScale = 70368744177664.0;         // 2^46, sum over wavelengths of p^2
 constexpr double kPScaleInv = 1.0 / 70368744177664.0;
 constexpr double kHScale = 1099511627776.0;          // 2^40, sum of -p log2 p
 constexpr double kHScaleInv = 1.0 / 1099511627776.0;
+
+// 2^31 t for t in [0, 1], rounded to nearest (ties up), with integer operations only
+// (no conversion instruction): t = 1.m x 2^(e-127) so 2^31 t = (1.m 2^23) x 2^(e-119).
+CPD_HD uint32_t t_fixed(float t)
+{
+#if defined(__CUDA_ARCH__)
+    const uint32_t b = __float_as_uint(t);
+#else
+    uint32_t b;
+    std::memcpy(&b, &t, 4);
+#endif
+    const int e = (int)(b >> 23) - 119;
+    const uint32_t m = (b & 0x7fffffu) | 0x800000u;
+    if (e >= 0) return m << (e > 8 ? 8 : e);
+    return e > -25 ? (m + (1u << (-e - 1))) >> (-e) : 0u;
+}
+
+// The same quantization of an f64 transmittance (exact re-trace path).
+CPD_HD uint32_t t_fixed64(double t) { return (uint32_t)(t * kTScale + 0.5); }
 
 // Outcome of a ray.
 enum : int { RAY_LOST = 0, RAY_HIT = 1, RAY_FLAG = 2 };
@@ -103,6 +127,16 @@ struct alignas(16) LamParams {
     uint32_t band_lo, band_hi;  // [band_lo, core_lo) and [core_hi, band_hi): guard bands
     uint32_t all_exact;         // no usable reference ray: every core ray is re-traced exactly
     uint32_t pad[3];
+};
+
+// Exact per-face data of one wavelength, written by lambda_setup for the re-trace. The
+// sequential f64 trace computes these from the same operands for every ray of the
+// wavelength, so they are the values it would compute for any one ray.
+struct ExactLam {
+    double dx[CPD_MAX_GLASS], dy[CPD_MAX_GLASS];  // direction after face k
+    double ci[CPD_MAX_GLASS];                     // dot(direction entering face k, N_k)
+    double cr[CPD_MAX_GLASS];                     // refraction cosine at face k
+    double n[CPD_MAX_GLASS];                      // index of glass k
 };
 
 // ----------------------------------------------------------------- exact f64 ops
@@ -351,6 +385,50 @@ CPD_HD int trace(const DevDesign &D, double lambda, double y, uint32_t &bin, dou
     if (e) return e;
     return detector(D, r, bin, t);
 }
+
+// The same exact trace with the wavelength's flat-face directions, cosines and glass
+// indices taken from E (written by lambda_setup): every operation whose operands differ
+// between rays -- the face intersections, the transmittance products, the exit face and
+// the detector -- is still done with the reference's operations, so the result is
+// bit-identical to trace(). The wavelength's flat faces do not reflect totally (else
+// lambda_setup drops it).
+CPD_HD int trace_lam(const DevDesign &D, const ExactLam &E, double y, uint32_t &bin, double &t)
+{
+    Ray r{0.0, y, 1.0, 0.0, 1.0, 1.0};
+    double n1 = 1.0;
+    for (int k = 0; k < D.G; k++) {
+        const double nx = D.pnx[k], ny = D.pny[k];
+        const double ci = E.ci[k];
+        if (ci == 0.0) return kNoHit;
+        const double d = div(dot(sub(D.ppx[k], r.ox), sub(D.ppy[k], r.oy), nx, ny), ci);
+        if (!(d >= 0.0)) return kNoHit;
+        const double hy = fma_(r.dy, d, r.oy);
+        if (!(0.0 <= hy && hy <= D.height)) return kNoHit;
+        r.ox = fma_(r.dx, d, r.ox);
+        r.oy = hy;
+        // Ray::refract (ray.rs:309-367) with the wavelength's direction and cosines
+        const double n2 = E.n[k];
+        const double cir = -ci;
+        const double cr = E.cr[k];
+        if (D.ar && cir > 0.5) {
+            r.ts = mul(r.ts, 0.99);
+            r.tp = mul(r.tp, 0.99);
+        } else {
+            const double a = mul(n1, cir), b = mul(n2, cr);
+            const double rs = sqr(div(sub(a, b), add(a, b)));
+            const double c = mul(n1, cr), e = mul(n2, cir);
+            const double rp = sqr(div(sub(c, e), add(c, e)));
+            r.ts = mul(r.ts, sub(1.0, rs));
+            r.tp = mul(r.tp, sub(1.0, rp));
+        }
+        r.dx = E.dx[k];
+        r.dy = E.dy[k];
+        n1 = n2;
+    }
+    const int e = exit_face(D, r, n1);
+    if (e) return e;
+    return detector(D, r, bin, t);
+}
 }  // namespace x
 
 // ----------------------------------------------------------------- per-wavelength setup
@@ -467,8 +545,14 @@ CPD_HDN inline bool reference_ray(const DevDesign &D, const double *zs, LamParam
 // Computes the per-wavelength parameters from the exact f64 flat-face chain, given
 // the sorted ray table zs[0..R) (ascending z = norminv(u)). Returns false if no ray of
 // this wavelength clears the flat faces (all lost); band ranges may still be non-empty.
+// If E is given it receives the exact per-face data for the re-trace.
+//
+// f64 costs about 80 FP32 operations here (70-cycle DFMA latency, ~700-cycle divide
+// and square root), so only the direction chain -- which the exact re-trace and every
+// per-wavelength decision reuse bit for bit -- is formed with the reference's exact
+// operations; the y interval is accurate to ~1e-14 and guarded at 1e-11.
 CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double *zs, uint32_t R,
-                                 LamParams &P, double yguard_rel = kYGuardRel)
+                                 LamParams &P, double yguard_rel = kYGuardRel, ExactLam *E = nullptr)
 {
     using namespace x;
     {
@@ -476,68 +560,113 @@ CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double
         uint32_t *w = reinterpret_cast<uint32_t *>(&P);
         for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
     }
+    double nk[CPD_MAX_GLASS];
+    for (int k = 0; k < D.G; k++) nk[k] = calc_n(D.glass[k], lambda);  // independent chains
     // direction/transmittance, exactly as the sequential trace computes them
     double dx = 1.0, dy = 0.0, ts = 1.0, tp = 1.0;
     // position affine in y: o(y) = (ax + bx*y, ay + by*y)
     double ax = 0.0, ay = 0.0, bx = 0.0, by = 1.0;
-    double ylo = -INFINITY, yhi = INFINITY, glo = 0.0, ghi = 0.0;
     double n1 = 1.0;
+    // Tightest bounds y >= -L0/L1 (L1 > 0) and y <= U0/U1 (U1 > 0), kept as fractions and
+    // compared by cross-multiplication so that only the two winners are divided.
+    double L0 = 0.0, L1 = 0.0, Lg = 0.0, U0 = 0.0, U1 = 0.0, Ug = 0.0;
     bool all_band = false;  // a y-independent constraint sits inside its guard: every ray is re-traced
-    auto constrain = [&](double c0, double c1, double scale) -> bool {
-        // c0 + c1*y >= 0 (up to rounding); returns false if no y satisfies it
-        double g = yguard_rel * (scale + 1.0);
+    bool ok = true;
+    auto constrain = [&](double c0, double c1, double scale) {
+        // c0 + c1*y >= 0 (up to rounding)
+        const double g = yguard_rel * (scale + 1.0);
         if (c1 == 0.0) {
             if (c0 < g && c0 > -g) all_band = true;
-            return c0 > -g;
-        }
-        double ys = -c0 / c1;
-        double gy = g / (c1 < 0.0 ? -c1 : c1);
-        if (c1 > 0.0) {
-            if (ys > ylo) { ylo = ys; glo = gy; }
+            if (!(c0 > -g)) ok = false;
+        } else if (c1 > 0.0) {
+            if (L1 == 0.0 || c0 * L1 < L0 * c1) {
+                L0 = c0;
+                L1 = c1;
+                Lg = g;
+            }
         } else {
-            if (ys < yhi) { yhi = ys; ghi = gy; }
+            const double u1 = -c1;
+            if (U1 == 0.0 || c0 * U1 < U0 * u1) {
+                U0 = c0;
+                U1 = u1;
+                Ug = g;
+            }
         }
-        return true;
     };
-    bool ok = true;
-    for (int k = 0; k < D.G && ok; k++) {
-        double n2 = calc_n(D.glass[k], lambda);
-        double nx = D.pnx[k], ny = D.pny[k];
-        double ci = dot(dx, dy, nx, ny);
+    for (int k = 0; k < D.G; k++) {
+        const double n2 = nk[k];
+        const double nx = D.pnx[k], ny = D.pny[k];
+        const double ci = dot(dx, dy, nx, ny);
         if (ci == 0.0) return false;
         // dist(y) = ((P - o(y)).N)/ci = e0 + e1*y
-        double e0 = ((D.ppx[k] - ax) * nx + (D.ppy[k] - ay) * ny) / ci;
-        double e1 = -(bx * nx + by * ny) / ci;
-        double sc = (e0 < 0 ? -e0 : e0) + 30.0 * (e1 < 0 ? -e1 : e1) + D.height;
-        ok = ok && constrain(e0, e1, sc);                       // dist >= 0
-        double hy0 = ay + dy * e0, hy1 = by + dy * e1;          // hit y = hy0 + hy1*y
-        ok = ok && constrain(hy0, hy1, sc);                      // 0 <= hit y
-        ok = ok && constrain(D.height - hy0, -hy1, sc);          // hit y <= height
+        const double inv = 1.0 / ci;
+        const double e0 = ((D.ppx[k] - ax) * nx + (D.ppy[k] - ay) * ny) * inv;
+        const double e1 = -(bx * nx + by * ny) * inv;
+        const double sc = (e0 < 0 ? -e0 : e0) + 30.0 * (e1 < 0 ? -e1 : e1) + D.height;
+        constrain(e0, e1, sc);                                   // dist >= 0
+        const double hy0 = ay + dy * e0, hy1 = by + dy * e1;     // hit y = hy0 + hy1*y
+        constrain(hy0, hy1, sc);                                 // 0 <= hit y
+        constrain(D.height - hy0, -hy1, sc);                     // hit y <= height
         ax = ax + dx * e0;
         ay = hy0;
         bx = bx + dx * e1;
         by = hy1;
-        Ray r{0.0, 0.0, dx, dy, ts, tp};
-        if (!refract(r, nx, ny, n1, n2, D.ar != 0)) return false;  // TIR: the same for every ray
-        dx = r.dx;
-        dy = r.dy;
-        ts = r.ts;
-        tp = r.tp;
+        // Ray::refract's direction with its exact operations (the TIR and AR decisions and
+        // every later face depend on it); the s/p transmittances feed only the FP32 fast
+        // path, so they are formed in FP32 (1 - R without cancellation).
+        const double ci_r = -ci;  // -dot(d, N) of Ray::refract: the same dot product
+        const double rr = div(n1, n2);
+        const double cr_sq = sub(1.0, mul(sqr(rr), sub(1.0, sqr(ci_r))));
+        if (cr_sq < 0.0) return false;  // TIR: the same for every ray
+        const double cr = sqrt_(cr_sq);
+        const double kq = sub(mul(rr, ci_r), cr);
+        const double vx = add(mul(dx, rr), mul(nx, kq));
+        const double vy = add(mul(dy, rr), mul(ny, kq));
+        if (D.ar && ci_r > 0.5) {
+            ts *= 0.99;
+            tp *= 0.99;
+        } else {
+            const float f1 = (float)n1, f2 = (float)n2, fc = (float)ci_r, fr = (float)cr;
+            const float a = f1 * fc + f2 * fr, b = f1 * fr + f2 * fc;
+            const float k4 = 4.f * f1 * f2 * fc * fr;
+            ts *= (double)(k4 / (a * a));
+            tp *= (double)(k4 / (b * b));
+        }
+        if (E) {
+            E->dx[k] = vx;
+            E->dy[k] = vy;
+            E->ci[k] = ci;
+            E->cr[k] = cr;
+            E->n[k] = n2;
+        }
+        dx = vx;
+        dy = vy;
         n1 = n2;
     }
     if (!ok) return false;
-    // sorted-ray index ranges. y_j = bym - bw*z_j is monotone in j.
-    auto ycount = [&](double thr, bool above) -> uint32_t {
-        // number of j (from the low-z end if bw > 0) with y_j > thr (above) or >= thr
+    const double ylo = L1 > 0.0 ? -L0 / L1 : -INFINITY, glo = L1 > 0.0 ? Lg / L1 : 0.0;
+    const double yhi = U1 > 0.0 ? U0 / U1 : INFINITY, ghi = U1 > 0.0 ? Ug / U1 : 0.0;
+    // Sorted-ray index ranges. y_j = bym - bw z_j is monotone in z, so the index of a
+    // height threshold T is the number of z_j below (bym - T)/bw. The guard widths are
+    // many orders above the f64 rounding of that inversion, so the count is taken on
+    // the z table with integer-ordered keys (no f64 arithmetic per search step).
+    auto zkey = [](double v) -> int64_t {
+        int64_t b;
+#if defined(__CUDA_ARCH__)
+        b = __double_as_longlong(v);
+#else
+        std::memcpy(&b, &v, 8);
+#endif
+        return b >= 0 ? b : (int64_t)(0x8000000000000000ull - (uint64_t)b);
+    };
+    auto ycount = [&](double thr, bool) -> uint32_t {
+        const double zt = (D.bym - thr) / D.bw;
+        if (zt != zt) return 0u;
+        const int64_t key = zkey(zt);
         uint32_t lo = 0, hi = R;
-        // y decreasing in j when bw > 0
-        bool dec = D.bw > 0.0;
         while (lo < hi) {
-            uint32_t mid = (lo + hi) >> 1;
-            double yj = beam_y(D, zs[mid]);
-            bool pred = above ? (yj > thr) : (yj >= thr);
-            // predicate true on a prefix when dec
-            if (dec ? pred : !pred) lo = mid + 1;
+            const uint32_t mid = (lo + hi) >> 1;
+            if (zkey(zs[mid]) < key) lo = mid + 1;
             else hi = mid;
         }
         return lo;

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -93,8 +94,8 @@ struct cpd_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;
     // device buffers
-    DevBuf designs, jobs, lam_u, z64, z32, lp, hist, S1, S2, acc, tiles, out, ctl, queue, pout;
-    DevBuf pair_lam, pair_z, pair_bins, pair_ts, pair_flags, peak;
+    DevBuf designs, jobs, lam_u, z64, z32, lp, lx, hist, S1, S2, acc, tiles, out, ctl, queue, pout;
+    DevBuf pair_lam, pair_z, pair_bins, pair_ts, pair_flags, peak, logtab;
     // pinned staging
     HostBuf h_designs, h_jobs, h_lam, h_z64, h_z32, h_out, h_ctl, h_pout, h_pairs;
     bool hist_dirty = true;
@@ -180,6 +181,8 @@ int run_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode,
         J.nchunk = std::max<uint32_t>(1u, (J.Rz + ctx->ray_tile - 1) / ctx->ray_tile);
         J.tile_rows = tile_rows_for(J.B);
         J.ntiles = (J.W + J.tile_rows - 1) / J.tile_rows;
+        ff::split(kTScaleInv / (double)J.R, J.unit_hi, J.unit_lo);
+        ff::split(-31.0 - std::log2((double)J.R), J.lu_hi, J.lu_lo);
         rows += J.W;
         hist += (uint64_t)J.W * J.B;
         lam += J.W;
@@ -213,6 +216,7 @@ int run_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode,
     CPD_TRY(ctx->z64.ensure(sizeof(double) * std::max<uint64_t>(ray, 1)));
     CPD_TRY(ctx->z32.ensure(2 * sizeof(float) * std::max<uint64_t>(ray, 1)));
     CPD_TRY(ctx->lp.ensure(sizeof(LamParams) * std::max<uint64_t>(rows, 1)));
+    CPD_TRY(ctx->lx.ensure(sizeof(ExactLam) * std::max<uint64_t>(rows, 1)));
     CPD_TRY(ctx->hist.ensure(hist_bytes));
     if (ctx->hist.cap != old_hist) ctx->hist_dirty = true;
     CPD_TRY(ctx->S1.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
@@ -255,6 +259,7 @@ int run_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode,
     a.z64 = ctx->z64.as<double>();
     a.z32 = ctx->z32.as<float>();
     a.lp = ctx->lp.as<LamParams>();
+    a.lx = ctx->lx.as<ExactLam>();
     a.hist = ctx->hist.as<unsigned long long>();
     a.S1 = ctx->S1.as<unsigned long long>();
     a.S2 = ctx->S2.as<unsigned long long>();
@@ -274,6 +279,7 @@ int run_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode,
         a.yguard_rel = kYGuardRel;
     }
     a.p_out = p_out_host ? ctx->pout.as<double>() : nullptr;
+    a.logtab = ctx->logtab.as<float>();
 
     // The device work of a pass, captured once per signature and replayed.
     std::vector<uint8_t> key(sizeof(a) + 3 * sizeof(uint32_t));
@@ -398,6 +404,16 @@ int cpd_context_create(int device, cpd_context **out)
             delete ctx;
             return CPD_CUDA_ERROR;
         }
+    {
+        std::vector<float> tab(4 * ff::kLogTable);
+        ff::make_log_table(tab.data());
+        if (ctx->logtab.ensure(sizeof(float) * tab.size()) != cudaSuccess ||
+            cudaMemcpy(ctx->logtab.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice) !=
+                cudaSuccess) {
+            delete ctx;
+            return CPD_CUDA_ERROR;
+        }
+    }
     *out = ctx;
     return CPD_OK;
 }
@@ -408,9 +424,10 @@ void cpd_context_destroy(cpd_context *ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
-    for (DevBuf *b : {&ctx->designs, &ctx->jobs, &ctx->lam_u, &ctx->z64, &ctx->z32, &ctx->lp, &ctx->hist, &ctx->S1,
+    for (DevBuf *b : {&ctx->designs, &ctx->jobs, &ctx->lam_u, &ctx->z64, &ctx->z32, &ctx->lp, &ctx->lx, &ctx->hist, &ctx->S1,
                       &ctx->S2, &ctx->acc, &ctx->tiles, &ctx->out, &ctx->ctl, &ctx->queue, &ctx->pout,
-                      &ctx->pair_lam, &ctx->pair_z, &ctx->pair_bins, &ctx->pair_ts, &ctx->pair_flags, &ctx->peak})
+                      &ctx->pair_lam, &ctx->pair_z, &ctx->pair_bins, &ctx->pair_ts, &ctx->pair_flags, &ctx->peak,
+                      &ctx->logtab})
         b->release();
     for (HostBuf *b : {&ctx->h_designs, &ctx->h_jobs, &ctx->h_lam, &ctx->h_z64, &ctx->h_z32, &ctx->h_out, &ctx->h_ctl,
                        &ctx->h_pout, &ctx->h_pairs})

@@ -141,6 +141,11 @@ int cpd_fitness_cpu(const cpd_design *d, uint64_t max_n, uint64_t max_m, cpd_fit
 /* The f64 inverse normal CDF the ray tables use (src/spectrometer/erf.rs:62-73). */
 double cpd_norminv(double u);
 
+/* No reference counterpart: the float-float log2 of an integer count that the GPU
+ * entropy sums use (FP32-pipe arithmetic, table-driven), evaluated on the host with the
+ * same code, for accuracy checks. out = {hi, lo}; log2(count) ~= hi + lo. */
+int cpd_entropy_log2(uint64_t count, double out[2]);
+
 /* Glass.__call__ -> Glass::calc_n (src/pylib.rs:76-78, src/spectrometer/glasscat.rs:17-22):
  * index of refraction at wavelength w (micrometres) from the 6 Horner coefficients. */
 double cpd_glass_index(const double coeffs[6], double w);
