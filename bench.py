@@ -184,16 +184,11 @@ def cpu_oracle_rate(d, W, R, target_s=10.0, nthreads=None):
     nthreads = nthreads or os.cpu_count() or 1
     ray_u = O.qrng_points(0.5, R)
     lam_all = O.qrng_points(0.5, W)
-    probe = min(W, max(nthreads, 16))
-    t0 = time.perf_counter()
-    O.fitness_points(d, lam_all[:probe], ray_u, nthreads=nthreads, want_p=False)
-    dt = time.perf_counter() - t0
-    S = int(max(probe, probe * target_s / max(dt, 1e-6)))  # wavelengths to evaluate, may exceed W
+    # whole designs until target_s of CPU time has elapsed (at least one)
     done, t0 = 0, time.perf_counter()
-    while done < S:
-        n = min(W, S - done)
-        O.fitness_points(d, lam_all[:n], ray_u, nthreads=nthreads, want_p=False)
-        done += n
+    while done == 0 or time.perf_counter() - t0 < target_s:
+        O.fitness_points(d, lam_all, ray_u, nthreads=nthreads, want_p=False)
+        done += W
     dt = time.perf_counter() - t0
     rate = done / (W * dt)
     return {"value": rate, "unit": "designs/s", "cores": nthreads, "kind": "port",
@@ -244,7 +239,7 @@ def plain_config(l2):
 
 def traffic_from_profiles():
     """dram bytes per trace-kernel launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "trace_kernel_config1.md")
+    p = os.path.join(ROOT, "profiles", "fitness_pass_config1.md")
     try:
         txt = open(p).read()
     except OSError:
