@@ -138,6 +138,8 @@ SIGNATURES = [
                                   C.POINTER(Fitness)]),
     ("cpd_fitness_gpu_points", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, _dp, C.c_uint32, C.c_uint32,
                                          C.POINTER(Fitness), _dp]),
+    ("cpd_fitness_gpu_points_static", C.c_int, [C.POINTER(Design), _dp, C.c_uint32, _dp, C.c_uint32, C.c_uint32,
+                                                C.POINTER(Fitness), _dp]),
     ("cpd_transmission_probability", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, C.c_uint32, _dp]),
     ("cpd_trace_rays", C.c_int, [_ctxp, C.POINTER(Design), _dp, _dp, C.c_uint32, C.c_uint32, _up, _dp,
                                  C.POINTER(C.c_uint8)]),

@@ -1,0 +1,213 @@
+// cpd_static.cu -- a fitness entry point that allocates no device memory.
+//
+// Some callers cannot allocate device memory themselves. Examples:
+// * a host application that owns the GPU's memory budget and forbids plug-in libraries
+//   from calling cudaMalloc;
+// * a latency-critical loop that must not take the device-wide synchronisation a
+//   cudaMalloc/cudaFree can imply.
+// cpd_fitness_gpu_points_static serves them. It runs the same kernels as
+// cpd_fitness_gpu_points, with every intermediate buffer carved out of one file-scope
+// device array of fixed size (limits below). The caller passes host inputs and outputs
+// only, and no context is needed. The first call on a device resolves the array's
+// device address (cudaGetSymbolAddress) and loads the log2 table into it, so that first
+// call should come before any stream capture. Calls share the array, which keeps the
+// last call's contents; each call clears what must start at zero. Calls that overlap on
+// the GPU race on it; calls from threads of one process are serialised per device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "cpd_gpu.cuh"
+#include "cpd_host.h"
+
+namespace cpd {
+namespace {
+
+// Limits of one call (the scratch array is sized for them).
+constexpr uint32_t kStaticMaxW = 1024;    // wavelengths
+constexpr uint32_t kStaticMaxR = 4096;    // rays per wavelength
+constexpr uint32_t kStaticMaxB = 128;     // detector bins
+constexpr uint32_t kStaticQueue = 32768;  // guard-band rays re-traced in one call
+
+constexpr size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kOffDesign = 0;
+constexpr size_t kOffJob = kOffDesign + al256(sizeof(DevDesign));
+constexpr size_t kOffCtl = kOffJob + al256(sizeof(DesignJob));
+constexpr size_t kOffAcc = kOffCtl + al256(sizeof(Control));
+constexpr size_t kOffTiles = kOffAcc + al256(sizeof(DesignAcc));
+constexpr size_t kOffOut = kOffTiles + al256(sizeof(unsigned int));
+constexpr size_t kOffS1 = kOffOut + al256(sizeof(DesignOut));
+constexpr size_t kOffS2 = kOffS1 + al256(8 * kStaticMaxB);
+constexpr size_t kOffLog = kOffS2 + al256(8 * kStaticMaxB);
+constexpr size_t kOffLam = kOffLog + al256(sizeof(float) * 4 * ff::kLogTable);
+constexpr size_t kOffZ64 = kOffLam + al256(8 * kStaticMaxW);
+constexpr size_t kOffZ32 = kOffZ64 + al256(8 * kStaticMaxR);
+constexpr size_t kOffLp = kOffZ32 + al256(8 * kStaticMaxR);
+constexpr size_t kOffLx = kOffLp + al256(sizeof(LamParams) * kStaticMaxW);
+constexpr size_t kOffHist = kOffLx + al256(sizeof(ExactLam) * kStaticMaxW);
+constexpr size_t kOffPout = kOffHist + al256(8 * (size_t)kStaticMaxW * kStaticMaxB);
+constexpr size_t kOffQueue = kOffPout + al256(8 * (size_t)kStaticMaxW * kStaticMaxB);
+constexpr size_t kScratchBytes = kOffQueue + al256(sizeof(QEntry) * kStaticQueue);  // about 3 MiB
+
+// The scratch array. Every GPU that loads this library holds one copy until exit.
+// In host code `g_scratch` is only a handle for cudaGetSymbolAddress, never a device
+// address: the kernels receive the address that call returns.
+static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+
+struct DeviceState {
+    unsigned char *base = nullptr;  // device address of g_scratch on this device
+    int sms = 0;
+    bool ready = false;
+    std::mutex call;                // one call at a time per device within this process
+};
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mu;
+DeviceState g_dev[kMaxDevices];
+
+// Once per device, with that device current: resolve the array's device address and
+// load the float-float log2 table into it.
+int static_setup(int dev, DeviceState *&st)
+{
+    if (dev < 0 || dev >= kMaxDevices) return CPD_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    st = &g_dev[dev];
+    if (st->ready) return CPD_OK;
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return CPD_CUDA_ERROR;
+    if (cudaDeviceGetAttribute(&st->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return CPD_CUDA_ERROR;
+    float tab[4 * ff::kLogTable];
+    ff::make_log_table(tab);
+    if (cudaMemcpy(static_cast<unsigned char *>(p) + kOffLog, tab, sizeof(tab), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+        return CPD_CUDA_ERROR;
+    st->base = static_cast<unsigned char *>(p);
+    st->ready = true;
+    return CPD_OK;
+}
+
+}  // namespace
+}  // namespace cpd
+
+using namespace cpd;
+
+extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *lam_u, uint32_t W,
+                                             const double *ray_u, uint32_t R, uint32_t trace_mode,
+                                             cpd_fitness *out, double *p_out)
+{
+    if (!d || !lam_u || !ray_u || !out || W == 0 || R == 0 || trace_mode > CPD_TRACE_FP64) return CPD_INVALID_ARGUMENT;
+    if (d->nglass < 1 || d->nglass > CPD_MAX_GLASS || d->bin_count < 1) return CPD_INVALID_ARGUMENT;
+    if (W > kStaticMaxW || R > kStaticMaxR || d->bin_count > kStaticMaxB) return CPD_NO_CAPACITY;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return CPD_CUDA_ERROR;
+    DeviceState *st = nullptr;
+    int e = static_setup(dev, st);
+    if (e) return e;
+    std::lock_guard<std::mutex> lk(st->call);
+
+    // host-side tables in fixed storage (no allocation)
+    static thread_local double z64[kStaticMaxR];
+    static thread_local float z32[2 * kStaticMaxR];
+    uint32_t Rz = 0;
+    for (uint32_t j = 0; j < R; j++) {
+        const double z = norminv(ray_u[j]);
+        if (std::isfinite(z)) z64[Rz++] = z;
+    }
+    std::sort(z64, z64 + Rz);
+    for (uint32_t j = 0; j < Rz; j++) {
+        z32[2 * j] = (float)z64[j];
+        z32[2 * j + 1] = (float)(z64[j] - (double)z32[2 * j]);
+    }
+    DevDesign D;
+    design_to_dev(*d, D);
+    DesignJob J;
+    std::memset(&J, 0, sizeof(J));
+    const uint32_t ray_tile = 32;
+    J.W = W;
+    J.R = R;
+    J.Rz = Rz;
+    J.B = D.B;
+    J.nchunk = std::max<uint32_t>(1u, (Rz + ray_tile - 1) / ray_tile);
+    J.tile_rows = std::max<uint32_t>(1u, 1024u / J.B);
+    J.ntiles = (W + J.tile_rows - 1) / J.tile_rows;
+    ff::split(kTScaleInv / (double)R, J.unit_hi, J.unit_lo);
+    ff::split(-31.0 - std::log2((double)R), J.lu_hi, J.lu_lo);
+
+    unsigned char *b = st->base;
+    const size_t cells = (size_t)W * D.B;
+    if (cudaMemcpy(b + kOffDesign, &D, sizeof(D), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b + kOffJob, &J, sizeof(J), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b + kOffLam, lam_u, 8 * (size_t)W, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (Rz && cudaMemcpy(b + kOffZ64, z64, 8 * (size_t)Rz, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        (Rz && cudaMemcpy(b + kOffZ32, z32, 8 * (size_t)Rz, cudaMemcpyHostToDevice) != cudaSuccess))
+        return CPD_CUDA_ERROR;
+    // the array keeps the previous call's contents: clear everything that must start at zero
+    if (cudaMemset(b + kOffCtl, 0, sizeof(Control)) != cudaSuccess ||
+        cudaMemset(b + kOffAcc, 0, sizeof(DesignAcc)) != cudaSuccess ||
+        cudaMemset(b + kOffTiles, 0, sizeof(unsigned int)) != cudaSuccess ||
+        cudaMemset(b + kOffS1, 0, 8 * (size_t)D.B) != cudaSuccess ||
+        cudaMemset(b + kOffS2, 0, 8 * (size_t)D.B) != cudaSuccess ||
+        cudaMemset(b + kOffHist, 0, 8 * cells) != cudaSuccess)
+        return CPD_CUDA_ERROR;
+
+    LaunchArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.designs = reinterpret_cast<const DevDesign *>(b + kOffDesign);
+    a.jobs = reinterpret_cast<const DesignJob *>(b + kOffJob);
+    a.njobs = 1;
+    a.total_rows = W;
+    a.total_items = (uint64_t)((W + 31) / 32) * J.nchunk;
+    a.total_tiles = J.ntiles;
+    a.lam_u = reinterpret_cast<const double *>(b + kOffLam);
+    a.z64 = reinterpret_cast<const double *>(b + kOffZ64);
+    a.z32 = reinterpret_cast<const float *>(b + kOffZ32);
+    a.lp = reinterpret_cast<LamParams *>(b + kOffLp);
+    a.lx = reinterpret_cast<ExactLam *>(b + kOffLx);
+    a.hist = reinterpret_cast<unsigned long long *>(b + kOffHist);
+    a.S1 = reinterpret_cast<unsigned long long *>(b + kOffS1);
+    a.S2 = reinterpret_cast<unsigned long long *>(b + kOffS2);
+    a.acc = reinterpret_cast<DesignAcc *>(b + kOffAcc);
+    a.tiles_done = reinterpret_cast<unsigned int *>(b + kOffTiles);
+    a.out = reinterpret_cast<DesignOut *>(b + kOffOut);
+    a.ctl = reinterpret_cast<Control *>(b + kOffCtl);
+    a.queue = reinterpret_cast<QEntry *>(b + kOffQueue);
+    a.qcap = kStaticQueue;
+    a.ray_tile = ray_tile;
+    a.mode = trace_mode;
+    if (trace_mode == CPD_TRACE_FP32) {
+        a.guards = Guards{0.f, 0.f, 0.f, 0.f};
+        a.yguard_rel = 0.0;
+    } else {
+        a.guards = default_guards();
+        a.yguard_rel = kYGuardRel;
+    }
+    a.p_out = p_out ? reinterpret_cast<double *>(b + kOffPout) : nullptr;
+    a.logtab = reinterpret_cast<const float *>(b + kOffLog);
+    launch_pass(a, st->sms, 8, 0);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(0) != cudaSuccess) return CPD_CUDA_ERROR;
+
+    Control ctl;
+    DesignOut o;
+    if (cudaMemcpy(&ctl, b + kOffCtl, sizeof(ctl), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(&o, b + kOffOut, sizeof(o), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return CPD_CUDA_ERROR;
+    if (ctl.overflow || ctl.queue_count > kStaticQueue) return CPD_NO_CAPACITY;
+    if (p_out && cudaMemcpy(p_out, b + kOffPout, 8 * cells, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return CPD_CUDA_ERROR;
+    std::memset(out, 0, sizeof(*out));
+    out->size = d->size;
+    out->deviation = d->deviation;
+    out->info = o.info;
+    out->h_cond = o.h_cond;
+    out->h_det = o.h_det;
+    out->max_sem = o.max_sem;
+    out->rays = (uint64_t)W * R;
+    out->hits = o.hits;
+    out->retraced = o.retraced;
+    out->fast_rays = o.fast;
+    out->wavelengths = (uint32_t)o.rows;
+    out->status = CPD_OK;
+    return CPD_OK;
+}

@@ -177,6 +177,24 @@ int cpd_fitness_gpu_points(cpd_context *ctx, const cpd_design *d, const double *
                            const double *ray_u, uint32_t R, uint32_t trace_mode, cpd_fitness *out,
                            double *p_out);
 
+/* No counterpart in the reference. The same fixed-N estimator as
+ * cpd_fitness_gpu_points, for callers that cannot allocate device memory: a host
+ * application that owns the GPU's memory budget and forbids plug-in libraries to
+ * allocate, or a latency-critical loop that must not pay the device-wide
+ * synchronisation a cudaMalloc/cudaFree can bring. It calls no allocator: every
+ * intermediate buffer lives in one file-scope device array of about 3 MiB, which every
+ * GPU that loads the library holds until the process exits. Inputs and outputs are host
+ * pointers; no context is used; the work runs on the legacy default stream of the
+ * current device and the call returns when it is done. Limits per call: W <= 1024
+ * wavelengths, R <= 4096 rays, bin_count <= 128, at most 32768 guard-band rays re-traced;
+ * larger requests return CPD_NO_CAPACITY. The first call on a device resolves the
+ * array's device address and loads a table into it, so make that first call before any
+ * stream capture. Every call shares the array, which keeps the previous call's contents;
+ * each call clears what must start at zero. Calls that overlap on the GPU race on the
+ * array; calls from threads of one process are serialised per device. */
+int cpd_fitness_gpu_points_static(const cpd_design *d, const double *lam_u, uint32_t W, const double *ray_u,
+                                  uint32_t R, uint32_t trace_mode, cpd_fitness *out, double *p_out);
+
 /* Spectrometer.transmission_probability (src/pylib.rs:1029-1058): p(d|lambda) for
  * explicit wavelengths, max_m rays each (fixed N: no early SEM stop).
  * out is n*B row-major. */
