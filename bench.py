@@ -3,8 +3,10 @@
 Default workload (N=1): the plain one-design GPU call -- 6 prisms, 64 detector
 bins, 4096 QMC wavelengths x 1024 rays (4,194,304 rays per design), FP32 trace
 with FP64/int64 accumulation and entropy. A step is one gpu_fitness call of one
-design. Also measured on the same run: the batched population form (1024 designs of
-mixed G, B, W), reported under "forms".
+design. Also measured on the same run, under "forms": the batched population form
+(1024 designs of mixed G, B, W in one captured launch sequence) and the serving form
+(a continuous-batching server fed by a synthetic generational optimizer: designs/s,
+p50/p99 request latency).
 
   value   designs/s with inputs resident on the device: 1 / (device time of the pass)
   e2e     designs/s through the C ABI with host buffers (design + point tables H2D,
@@ -196,6 +198,53 @@ def cpu_oracle_rate(d, W, R, target_s=10.0, nthreads=None):
                       f"({done * R} rays, {dt:.1f} s, {nthreads} threads)"}
 
 
+def serving_form(ctx, generations=200):
+    """The serving loop fed by the synthetic generational optimizer: 200 generations,
+    batch sizes 64..2048, 128 wavelengths x 8192 rays per design (the reference
+    optimizer's gpu_fitness sampling), once with batches submitted back to back
+    (capacity) and once as a Poisson process at 70% of that capacity (latency). Beside
+    it, the plain one-design call on the same sampling."""
+    import numpy as np
+    import compound_prism_designer as cpd
+    from compound_prism_designer import _native as N
+    from compound_prism_designer import generations as gen
+
+    W, R = 128, 8192
+    out = {"workload": f"{generations} generations, batch sizes uniform 64..2048, G in 2..6, B in 16..128, "
+                       f"{W} wavelengths x {R} rays per design, one seed per generation"}
+    # plain call, same sampling, one design per call (ray table cached: same seed)
+    rng = np.random.default_rng(11)
+    cat = gen.glass_catalog(rng, 64)
+    pop = gen.initial_population(rng, 256, cat)
+    designs, ok = gen.build(pop, cat)
+    dd = [N.Design.from_buffer_copy(designs[i].tobytes()) for i in range(len(designs))]
+    seeds = np.array([0.5])
+    f = N.Fitness()
+    for i in range(8):
+        N.lib.cpd_fitness_gpu(ctx.handle, dd[i], seeds.ctypes.data_as(N._dp), 1, W, 2, R, f)
+    t0 = time.perf_counter()
+    for x in dd:
+        N.lib.cpd_fitness_gpu(ctx.handle, x, seeds.ctypes.data_as(N._dp), 1, W, 2, R, f)
+    plain = len(dd) / (time.perf_counter() - t0)
+    out["plain_designs_per_s"] = plain
+    with cpd.Server(mem_budget_bytes=8 << 30, slots=2, max_designs_per_pass=256, context=ctx) as sv:
+        gen.serve(sv, generations=5, seed=1)  # warm-up: buffers, caches
+        sat = gen.serve(sv, generations=generations, seed=2)
+        cap = sat["designs_per_s"]
+        mean_gap = sat["mean_batch"] / (0.7 * cap)
+        poi = gen.serve(sv, generations=generations, seed=3, mean_interarrival_s=mean_gap)
+        st = sv.stats()
+    for r in (sat, poi):
+        r.pop("latency_ms")
+    out["back_to_back"] = sat
+    out["poisson_70pct"] = dict(poi, mean_interarrival_ms=1e3 * mean_gap)
+    out["designs_per_s"] = cap
+    out["p50_ms"], out["p99_ms"] = poi["p50_ms"], poi["p99_ms"]
+    out["speedup_vs_plain"] = cap / plain
+    out["server_stats"] = st
+    return out
+
+
 def run_reference(args, dist):
     """--impl reference: the reference CPU algorithm (oracle port) on the same workload."""
     if dist.rank != 0:
@@ -338,6 +387,10 @@ def main():
                 "speedup_vs_plain_e2e": (nb / min(bt)) / e2e}}
         except Exception as e:  # noqa: BLE001
             extras["forms"] = {"error": repr(e)}
+        try:
+            extras.setdefault("forms", {})["serving"] = serving_form(ctx)
+        except Exception as e:  # noqa: BLE001
+            extras.setdefault("forms", {})["serving"] = {"error": repr(e)}
         try:
             extras["cpu_baseline"] = cpu_oracle_rate(d, W_PLAIN, R_PLAIN)
         except Exception as e:  # noqa: BLE001

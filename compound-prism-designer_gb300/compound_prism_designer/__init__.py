@@ -25,7 +25,7 @@ __all__ = [
     "RayTraceError", "CudaError", "Glass", "DesignFitness", "Vector2D", "UnitVector2D",
     "UniformWavelengthDistribution", "GaussianBeam", "FiberBeam", "CompoundPrism",
     "position_detector_array", "DetectorArray", "Spectrometer", "Context", "default_context",
-    "fitness_batch", "TRACE_HYBRID", "TRACE_FP32", "TRACE_FP64",
+    "fitness_batch", "build_designs", "Server", "TRACE_HYBRID", "TRACE_FP32", "TRACE_FP64",
 ]
 
 TRACE_HYBRID = N.TRACE_HYBRID
@@ -534,3 +534,109 @@ def fitness_batch(spectrometers: Sequence[Spectrometer], *, seeds=None, max_n=25
     ctx = context or default_context()
     _check(N.lib.cpd_fitness_gpu_batch(ctx.handle, designs, items, n, int(mode), outs), "fitness_batch")
     return list(outs)
+
+
+def build_designs(params: np.ndarray, acceptance: float = 0.0):
+    """Builds a whole generation of designs from an array of N.PARAMS_DTYPE records (no
+    reference counterpart; the reference builds one Spectrometer per call,
+    designer.py:203-265). With acceptance in (0, 1] each detector is placed by
+    position_detector_array first. Returns (designs, status): an N.DESIGN_DTYPE array and
+    the per-design status codes (0 = built)."""
+    params = np.ascontiguousarray(params, dtype=N.PARAMS_DTYPE)
+    n = params.size
+    designs = np.zeros(n, dtype=N.DESIGN_DTYPE)
+    status = np.zeros(n, dtype=np.int32)
+    _check(N.lib.cpd_design_build_batch(params.ctypes.data, n, float(acceptance), designs.ctypes.data,
+                                        status.ctypes.data_as(C.POINTER(C.c_int32))), "build_designs")
+    return designs, status
+
+
+def _design_array(designs) -> np.ndarray:
+    if isinstance(designs, np.ndarray):
+        return np.ascontiguousarray(designs, dtype=N.DESIGN_DTYPE)
+    out = np.zeros(len(designs), dtype=N.DESIGN_DTYPE)
+    for i, s in enumerate(designs):
+        d = s.design if isinstance(s, Spectrometer) else s
+        out[i] = np.frombuffer(bytes(d), dtype=N.DESIGN_DTYPE)[0]
+    return out
+
+
+class Server:
+    """Continuous-batching fitness server on one GPU (no reference counterpart).
+
+    Requests arrive from any thread with submit(); a native worker admits their designs
+    in arrival order into passes while the device bytes of the designs in flight stay
+    within mem_budget_bytes, and keeps up to `slots` passes in flight on separate
+    streams. Each design's result is bitwise the one it gets alone."""
+
+    def __init__(self, mem_budget_bytes: int = 8 << 30, slots: int = 2, max_designs_per_pass: int = 256,
+                 context: Optional[Context] = None):
+        self._ctx = context or default_context()
+        h = C.c_void_p()
+        _check(N.lib.cpd_server_create(self._ctx.handle, int(mem_budget_bytes), int(slots),
+                                       int(max_designs_per_pass), C.byref(h)), "cpd_server_create")
+        self._h = h
+        self._sizes: dict[int, int] = {}
+        self._lock = threading.Lock()
+
+    def submit(self, designs, *, seeds=0.5, max_n=128, max_eval=8192, mode: int = TRACE_HYBRID) -> int:
+        """Queues designs (Spectrometers or an N.DESIGN_DTYPE array); max_n, max_eval and
+        seeds may be scalars or per-design sequences. Returns the request id at once."""
+        d = _design_array(designs)
+        n = d.size
+        items = np.zeros(n, dtype=N.BATCH_ITEM_DTYPE)
+        items["seed"] = np.broadcast_to(np.asarray(seeds, dtype=np.float64), (n,))
+        items["max_n"] = np.broadcast_to(np.asarray(max_n), (n,))
+        items["max_eval"] = np.broadcast_to(np.asarray(max_eval), (n,))
+        rid = C.c_uint64(0)
+        _check(N.lib.cpd_server_submit(self._h, d.ctypes.data, items.ctypes.data, n, int(mode), C.byref(rid)),
+               "cpd_server_submit")
+        with self._lock:
+            self._sizes[rid.value] = n
+        return rid.value
+
+    def wait(self, request_id: int, timeout: Optional[float] = None):
+        """Waits for a request (timeout in seconds, None = forever). Returns (results,
+        latency_ms): an N.FITNESS_DTYPE array (status NOT_CONVERGED marks a design whose
+        SEM stayed above 5e-3) and the time from submit to completion. Raises
+        TimeoutError when the timeout passes first; the request stays queued."""
+        with self._lock:
+            n = self._sizes[request_id]
+        outs = np.zeros(n, dtype=N.FITNESS_DTYPE)
+        lat = C.c_double(0.0)
+        remaining = math.inf if timeout is None else float(timeout)
+        while True:
+            step = min(remaining, 1.0)
+            rc = N.lib.cpd_server_wait(self._h, request_id, outs.ctypes.data, step * 1e3, C.byref(lat))
+            if rc != N.TIMEOUT:
+                break
+            remaining -= step
+            if remaining <= 0:
+                raise TimeoutError(f"request {request_id} not done")
+        with self._lock:
+            del self._sizes[request_id]
+        _check(rc, "cpd_server_wait")
+        return outs, lat.value
+
+    def stats(self) -> dict:
+        v = [C.c_uint64(0) for _ in range(4)]
+        _check(N.lib.cpd_server_stats(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(("designs_done", "passes", "max_passes_in_flight", "pending_designs"),
+                        (x.value for x in v)))
+
+    def close(self):
+        if self._h:
+            N.lib.cpd_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

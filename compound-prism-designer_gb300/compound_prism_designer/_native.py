@@ -126,6 +126,7 @@ SIGNATURES = [
     ("cpd_status_string", C.c_char_p, [C.c_int]),
     ("cpd_position_detector_array", C.c_int, [C.POINTER(SpectrometerParams), C.c_double, _dp, C.POINTER(C.c_int32)]),
     ("cpd_design_build", C.c_int, [C.POINTER(SpectrometerParams), C.POINTER(Design)]),
+    ("cpd_design_build_batch", C.c_int, [C.c_void_p, C.c_uint32, C.c_double, C.c_void_p, C.POINTER(C.c_int32)]),
     ("cpd_exit_ray", C.c_int, [C.POINTER(Design), C.c_double, C.c_double, _dp]),
     ("cpd_ray_trace", C.c_int, [C.POINTER(Design), C.c_double, C.c_double, _dp, _up]),
     ("cpd_fitness_cpu", C.c_int, [C.POINTER(Design), C.c_uint64, C.c_uint64, C.POINTER(Fitness)]),
@@ -152,7 +153,22 @@ SIGNATURES = [
     ("cpd_set_profiling", C.c_int, [_ctxp, C.c_int]),
     ("cpd_last_kernel_times", C.c_int, [_ctxp, _dp]),
     ("cpd_last_transfer_bytes", C.c_int, [_ctxp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("cpd_server_create", C.c_int, [_ctxp, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(C.c_void_p)]),
+    ("cpd_server_submit", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                    C.POINTER(C.c_uint64)]),
+    ("cpd_server_wait", C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_double, _dp]),
+    ("cpd_server_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                   C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("cpd_server_destroy", None, [C.c_void_p]),
 ]
+
+# numpy mirrors of the records, for whole-generation arrays passed by pointer
+import numpy as _np  # noqa: E402
+
+PARAMS_DTYPE = _np.dtype(SpectrometerParams)
+DESIGN_DTYPE = _np.dtype(Design)
+FITNESS_DTYPE = _np.dtype(Fitness)
+BATCH_ITEM_DTYPE = _np.dtype(BatchItem)
 
 
 def _load():

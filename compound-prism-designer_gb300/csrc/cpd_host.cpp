@@ -317,6 +317,22 @@ int cpd_design_build(const cpd_spectrometer_params *p, cpd_design *out)
     return CPD_OK;
 }
 
+int cpd_design_build_batch(const cpd_spectrometer_params *p, uint32_t n, double acceptance, cpd_design *out,
+                           int32_t *status)
+{
+    if ((!p || !out || !status) && n) return CPD_INVALID_ARGUMENT;
+    if (acceptance != 0.0 && !(acceptance > 0.0 && acceptance <= 1.0)) return CPD_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < n; i++) {
+        cpd_spectrometer_params q = p[i];
+        int e = CPD_OK;
+        if (acceptance > 0.0) e = cpd_position_detector_array(&q, acceptance, q.det_position, &q.det_flipped);
+        if (!e) e = cpd_design_build(&q, &out[i]);
+        if (e) std::memset(&out[i], 0, sizeof(cpd_design));
+        status[i] = e;
+    }
+    return CPD_OK;
+}
+
 int cpd_exit_ray(const cpd_design *d, double y, double wavelength, double out[4])
 {
     if (!d || !out) return CPD_INVALID_ARGUMENT;

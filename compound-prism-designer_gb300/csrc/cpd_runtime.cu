@@ -1,12 +1,18 @@
-// cpd_runtime.cu -- the GPU side of the C ABI: context, pooled buffers, ray-table
-// cache, pass planning and CUDA-graph replay of the per-pass launch sequence.
+// cpd_runtime.cu -- the GPU side of the C ABI: contexts, per-pass slots (stream,
+// pooled device buffers, pinned staging, captured CUDA graph), the ray-table cache,
+// the synchronous entry points and the continuous-batching server.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "cpd_gpu.cuh"
@@ -81,6 +87,56 @@ struct RayTable {
     std::vector<double> z64;
     std::vector<float> z32;
 };
+using RayTablePtr = std::shared_ptr<const RayTable>;
+
+// Everything one pass needs on the device, plus its staging and its captured graph.
+// A context owns one slot (the synchronous calls); a server owns several, so that
+// passes overlap on the device.
+struct PassSlot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
+    cudaEvent_t kev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    DevBuf designs, jobs, lam_u, z64, z32, lp, lx, hist, S1, S2, acc, tiles, out, ctl, queue, pout;
+    HostBuf h_designs, h_jobs, h_lam, h_z64, h_z32, h_out, h_ctl;
+    bool hist_dirty = true;
+    uint32_t qcap = 1u << 18;
+    std::vector<uint8_t> graph_key;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_launches = 0;
+    // the pass in flight / last finished
+    uint32_t n = 0;
+    uint64_t hist_cells = 0;
+    double *p_out_host = nullptr;
+    bool profiled = false;
+    int launches = 0;
+    double last_ms = 0.0;
+    uint64_t h2d = 0, d2h = 0;
+    double kernel_ms[4] = {0, 0, 0, 0};
+
+    cudaError_t create()
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreate(&ev0);
+        if (e == cudaSuccess) e = cudaEventCreate(&ev1);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+        for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&kev[i]);
+        return e;
+    }
+    void destroy()
+    {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+        for (DevBuf *b : {&designs, &jobs, &lam_u, &z64, &z32, &lp, &lx, &hist, &S1, &S2, &acc, &tiles, &out, &ctl,
+                          &queue, &pout})
+            b->release();
+        for (HostBuf *b : {&h_designs, &h_jobs, &h_lam, &h_z64, &h_z32, &h_out, &h_ctl}) b->release();
+        for (cudaEvent_t *ev : {&ev0, &ev1, &done, &kev[0], &kev[1], &kev[2], &kev[3], &kev[4]})
+            if (*ev) cudaEventDestroy(*ev), *ev = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
 
 }  // namespace
 }  // namespace cpd
@@ -90,54 +146,42 @@ using namespace cpd;
 struct cpd_context {
     int device = 0;
     int num_sms = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    std::mutex mu;
-    // device buffers
-    DevBuf designs, jobs, lam_u, z64, z32, lp, lx, hist, S1, S2, acc, tiles, out, ctl, queue, pout;
+    std::mutex mu;        // serialises the synchronous entry points (main slot)
+    std::mutex cache_mu;  // ray-table cache
+    PassSlot main;
     DevBuf pair_lam, pair_z, pair_bins, pair_ts, pair_flags, peak, logtab;
-    // pinned staging
-    HostBuf h_designs, h_jobs, h_lam, h_z64, h_z32, h_out, h_ctl, h_pout, h_pairs;
-    bool hist_dirty = true;
     uint32_t ray_tile = 32;
     uint32_t warps_per_cta = 8;
-    uint32_t qcap = 1u << 18;
-    double last_ms = 0.0;
-    uint32_t last_launches = 0;
-    uint64_t last_h2d = 0, last_d2h = 0;
     bool profiling = false;
-    cudaEvent_t kev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    double kernel_ms[4] = {0, 0, 0, 0};
-    // ray-table cache (host side), keyed by (seed, R)
-    std::map<RayKey, RayTable> ray_cache;
-    // graph cache: one executable graph per pass signature
-    std::vector<uint8_t> graph_key;
-    cudaGraphExec_t graph_exec = nullptr;
-    int graph_launches = 0;
     bool use_graphs = true;
+    std::map<RayKey, RayTablePtr> ray_cache;
 };
 
 namespace {
 
-#define CPD_TRY(expr)                         \
-    do {                                      \
-        cudaError_t _e = (expr);              \
+#define CPD_TRY(expr)                                 \
+    do {                                              \
+        cudaError_t _e = (expr);                      \
         if (_e != cudaSuccess) return CPD_CUDA_ERROR; \
     } while (0)
 
-const RayTable &ray_table_cached(cpd_context *ctx, double seed, uint32_t R)
+RayTablePtr ray_table_cached(cpd_context *ctx, double seed, uint32_t R)
 {
     uint64_t bits;
     std::memcpy(&bits, &seed, 8);
     RayKey key{bits, R};
-    auto it = ctx->ray_cache.find(key);
-    if (it != ctx->ray_cache.end()) return it->second;
-    if (ctx->ray_cache.size() > 64) ctx->ray_cache.clear();
+    {
+        std::lock_guard<std::mutex> lk(ctx->cache_mu);
+        auto it = ctx->ray_cache.find(key);
+        if (it != ctx->ray_cache.end()) return it->second;
+    }
     std::vector<double> u(R);
     seed_points(seed, 1, R, u.data());
-    RayTable t;
-    ray_table(u.data(), R, t.z64, t.z32);
-    return ctx->ray_cache.emplace(key, std::move(t)).first->second;
+    auto t = std::make_shared<RayTable>();
+    ray_table(u.data(), R, t->z64, t->z32);
+    std::lock_guard<std::mutex> lk(ctx->cache_mu);
+    if (ctx->ray_cache.size() > 256) ctx->ray_cache.clear();
+    return ctx->ray_cache.emplace(key, t).first->second;
 }
 
 // One design's sampling inputs for a pass.
@@ -155,13 +199,24 @@ struct PassResult {
 
 uint32_t tile_rows_for(uint32_t B) { return std::max<uint32_t>(1u, 1024u / B); }
 
-// Plans and runs one pass over `ds`. Accumulators (S1, S2, acc) are zeroed when
-// `fresh`; they persist otherwise (the seeds of one call).
-int run_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode, bool fresh, double *p_out_host,
-             PassResult &res)
+// Device bytes one design occupies in a pass (histogram, per-row tables, ray tables):
+// the admission unit of the server.
+uint64_t design_bytes(uint32_t W, uint32_t R, uint32_t B)
+{
+    return (uint64_t)W * (8ull * B + sizeof(LamParams) + sizeof(ExactLam) + 8) + 16ull * R + 16ull * B +
+           sizeof(DevDesign) + sizeof(DesignJob) + sizeof(DesignAcc) + sizeof(DesignOut);
+}
+
+// Plans, stages and issues one pass on slot `s` (asynchronously; `s.done` is recorded
+// at the end). Accumulators are zeroed when `fresh`; they persist otherwise (the seeds
+// of one call).
+int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds, uint32_t mode, bool fresh,
+               double *p_out_host, bool use_graph, bool profile)
 {
     const uint32_t n = (uint32_t)ds.size();
     std::vector<DesignJob> jobs(n);
+    std::vector<uint8_t> owns_rays(n, 1);  // designs that share a ray table share its copy
+    std::map<const RayTable *, uint64_t> ray_offs;
     uint64_t rows = 0, hist = 0, lam = 0, ray = 0, accc = 0, items = 0, tiles = 0;
     for (uint32_t i = 0; i < n; i++) {
         const PassDesign &p = ds[i];
@@ -174,7 +229,9 @@ int run_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode,
         J.row_off = rows;
         J.hist_off = hist;
         J.lam_off = lam;
-        J.ray_off = ray;
+        auto ro = ray_offs.emplace(p.rays, ray);
+        J.ray_off = ro.first->second;
+        owns_rays[i] = ro.second;
         J.acc_off = accc;
         J.item_off = items;
         J.tile_off = tiles;
@@ -186,89 +243,88 @@ int run_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode,
         rows += J.W;
         hist += (uint64_t)J.W * J.B;
         lam += J.W;
-        ray += J.Rz;
+        if (owns_rays[i]) ray += J.Rz;
         accc += J.B;
         items += (uint64_t)((J.W + 31) / 32) * J.nchunk;
         tiles += J.ntiles;
     }
     // staging
-    CPD_TRY(ctx->h_designs.ensure(sizeof(DevDesign) * n));
-    CPD_TRY(ctx->h_jobs.ensure(sizeof(DesignJob) * n));
-    CPD_TRY(ctx->h_lam.ensure(sizeof(double) * std::max<uint64_t>(lam, 1)));
-    CPD_TRY(ctx->h_z64.ensure(sizeof(double) * std::max<uint64_t>(ray, 1)));
-    CPD_TRY(ctx->h_z32.ensure(2 * sizeof(float) * std::max<uint64_t>(ray, 1)));
-    CPD_TRY(ctx->h_out.ensure(sizeof(DesignOut) * n));
-    CPD_TRY(ctx->h_ctl.ensure(sizeof(Control)));
+    CPD_TRY(S.h_designs.ensure(sizeof(DevDesign) * n));
+    CPD_TRY(S.h_jobs.ensure(sizeof(DesignJob) * n));
+    CPD_TRY(S.h_lam.ensure(sizeof(double) * std::max<uint64_t>(lam, 1)));
+    CPD_TRY(S.h_z64.ensure(sizeof(double) * std::max<uint64_t>(ray, 1)));
+    CPD_TRY(S.h_z32.ensure(2 * sizeof(float) * std::max<uint64_t>(ray, 1)));
+    CPD_TRY(S.h_out.ensure(sizeof(DesignOut) * n));
+    CPD_TRY(S.h_ctl.ensure(sizeof(Control)));
     for (uint32_t i = 0; i < n; i++) {
-        ctx->h_designs.as<DevDesign>()[i] = *ds[i].dev;
-        ctx->h_jobs.as<DesignJob>()[i] = jobs[i];
-        std::memcpy(ctx->h_lam.as<double>() + jobs[i].lam_off, ds[i].lam_u, sizeof(double) * ds[i].W);
-        std::memcpy(ctx->h_z64.as<double>() + jobs[i].ray_off, ds[i].rays->z64.data(), sizeof(double) * jobs[i].Rz);
-        std::memcpy(ctx->h_z32.as<float>() + 2 * jobs[i].ray_off, ds[i].rays->z32.data(),
-                    2 * sizeof(float) * jobs[i].Rz);
+        S.h_designs.as<DevDesign>()[i] = *ds[i].dev;
+        S.h_jobs.as<DesignJob>()[i] = jobs[i];
+        std::memcpy(S.h_lam.as<double>() + jobs[i].lam_off, ds[i].lam_u, sizeof(double) * ds[i].W);
+        if (!owns_rays[i]) continue;
+        std::memcpy(S.h_z64.as<double>() + jobs[i].ray_off, ds[i].rays->z64.data(), sizeof(double) * jobs[i].Rz);
+        std::memcpy(S.h_z32.as<float>() + 2 * jobs[i].ray_off, ds[i].rays->z32.data(), 2 * sizeof(float) * jobs[i].Rz);
     }
     // device buffers
     const size_t hist_bytes = sizeof(unsigned long long) * std::max<uint64_t>(hist, 1);
-    size_t old_hist = ctx->hist.cap;
-    CPD_TRY(ctx->designs.ensure(sizeof(DevDesign) * n));
-    CPD_TRY(ctx->jobs.ensure(sizeof(DesignJob) * n));
-    CPD_TRY(ctx->lam_u.ensure(sizeof(double) * std::max<uint64_t>(lam, 1)));
-    CPD_TRY(ctx->z64.ensure(sizeof(double) * std::max<uint64_t>(ray, 1)));
-    CPD_TRY(ctx->z32.ensure(2 * sizeof(float) * std::max<uint64_t>(ray, 1)));
-    CPD_TRY(ctx->lp.ensure(sizeof(LamParams) * std::max<uint64_t>(rows, 1)));
-    CPD_TRY(ctx->lx.ensure(sizeof(ExactLam) * std::max<uint64_t>(rows, 1)));
-    CPD_TRY(ctx->hist.ensure(hist_bytes));
-    if (ctx->hist.cap != old_hist) ctx->hist_dirty = true;
-    CPD_TRY(ctx->S1.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
-    CPD_TRY(ctx->S2.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
-    CPD_TRY(ctx->acc.ensure(sizeof(DesignAcc) * n));
-    CPD_TRY(ctx->tiles.ensure(sizeof(unsigned int) * n));
-    CPD_TRY(ctx->out.ensure(sizeof(DesignOut) * n));
-    CPD_TRY(ctx->ctl.ensure(sizeof(Control)));
-    CPD_TRY(ctx->queue.ensure(sizeof(QEntry) * ctx->qcap));
-    if (p_out_host) CPD_TRY(ctx->pout.ensure(hist_bytes));
+    const size_t old_hist = S.hist.cap;
+    CPD_TRY(S.designs.ensure(sizeof(DevDesign) * n));
+    CPD_TRY(S.jobs.ensure(sizeof(DesignJob) * n));
+    CPD_TRY(S.lam_u.ensure(sizeof(double) * std::max<uint64_t>(lam, 1)));
+    CPD_TRY(S.z64.ensure(sizeof(double) * std::max<uint64_t>(ray, 1)));
+    CPD_TRY(S.z32.ensure(2 * sizeof(float) * std::max<uint64_t>(ray, 1)));
+    CPD_TRY(S.lp.ensure(sizeof(LamParams) * std::max<uint64_t>(rows, 1)));
+    CPD_TRY(S.lx.ensure(sizeof(ExactLam) * std::max<uint64_t>(rows, 1)));
+    CPD_TRY(S.hist.ensure(hist_bytes));
+    if (S.hist.cap != old_hist) S.hist_dirty = true;
+    CPD_TRY(S.S1.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
+    CPD_TRY(S.S2.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
+    CPD_TRY(S.acc.ensure(sizeof(DesignAcc) * n));
+    CPD_TRY(S.tiles.ensure(sizeof(unsigned int) * n));
+    CPD_TRY(S.out.ensure(sizeof(DesignOut) * n));
+    CPD_TRY(S.ctl.ensure(sizeof(Control)));
+    CPD_TRY(S.queue.ensure(sizeof(QEntry) * S.qcap));
+    if (p_out_host) CPD_TRY(S.pout.ensure(hist_bytes));
 
-    cudaStream_t s = ctx->stream;
-    if (ctx->hist_dirty) {
-        CPD_TRY(cudaMemsetAsync(ctx->hist.p, 0, ctx->hist.cap, s));
-        ctx->hist_dirty = false;
+    cudaStream_t s = S.stream;
+    if (S.hist_dirty) {
+        CPD_TRY(cudaMemsetAsync(S.hist.p, 0, S.hist.cap, s));
+        S.hist_dirty = false;
     }
-    CPD_TRY(cudaMemcpyAsync(ctx->designs.p, ctx->h_designs.p, sizeof(DevDesign) * n, cudaMemcpyHostToDevice, s));
-    CPD_TRY(cudaMemcpyAsync(ctx->jobs.p, ctx->h_jobs.p, sizeof(DesignJob) * n, cudaMemcpyHostToDevice, s));
-    CPD_TRY(cudaMemcpyAsync(ctx->lam_u.p, ctx->h_lam.p, sizeof(double) * lam, cudaMemcpyHostToDevice, s));
-    CPD_TRY(cudaMemcpyAsync(ctx->z64.p, ctx->h_z64.p, sizeof(double) * ray, cudaMemcpyHostToDevice, s));
-    CPD_TRY(cudaMemcpyAsync(ctx->z32.p, ctx->h_z32.p, 2 * sizeof(float) * ray, cudaMemcpyHostToDevice, s));
-    ctx->last_h2d += sizeof(DevDesign) * n + sizeof(DesignJob) * n + sizeof(double) * lam +
-                     (sizeof(double) + 2 * sizeof(float)) * ray;
-    ctx->last_d2h += sizeof(DesignOut) * n + sizeof(Control) + (p_out_host ? sizeof(double) * hist : 0);
+    CPD_TRY(cudaMemcpyAsync(S.designs.p, S.h_designs.p, sizeof(DevDesign) * n, cudaMemcpyHostToDevice, s));
+    CPD_TRY(cudaMemcpyAsync(S.jobs.p, S.h_jobs.p, sizeof(DesignJob) * n, cudaMemcpyHostToDevice, s));
+    CPD_TRY(cudaMemcpyAsync(S.lam_u.p, S.h_lam.p, sizeof(double) * lam, cudaMemcpyHostToDevice, s));
+    CPD_TRY(cudaMemcpyAsync(S.z64.p, S.h_z64.p, sizeof(double) * ray, cudaMemcpyHostToDevice, s));
+    CPD_TRY(cudaMemcpyAsync(S.z32.p, S.h_z32.p, 2 * sizeof(float) * ray, cudaMemcpyHostToDevice, s));
+    S.h2d += sizeof(DevDesign) * n + sizeof(DesignJob) * n + sizeof(double) * lam + (sizeof(double) + 2 * sizeof(float)) * ray;
+    S.d2h += sizeof(DesignOut) * n + sizeof(Control) + (p_out_host ? sizeof(double) * hist : 0);
     if (fresh) {
-        CPD_TRY(cudaMemsetAsync(ctx->S1.p, 0, sizeof(unsigned long long) * accc, s));
-        CPD_TRY(cudaMemsetAsync(ctx->S2.p, 0, sizeof(unsigned long long) * accc, s));
-        CPD_TRY(cudaMemsetAsync(ctx->acc.p, 0, sizeof(DesignAcc) * n, s));
+        CPD_TRY(cudaMemsetAsync(S.S1.p, 0, sizeof(unsigned long long) * accc, s));
+        CPD_TRY(cudaMemsetAsync(S.S2.p, 0, sizeof(unsigned long long) * accc, s));
+        CPD_TRY(cudaMemsetAsync(S.acc.p, 0, sizeof(DesignAcc) * n, s));
     }
 
     LaunchArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.designs = ctx->designs.as<DevDesign>();
-    a.jobs = ctx->jobs.as<DesignJob>();
+    a.designs = S.designs.as<DevDesign>();
+    a.jobs = S.jobs.as<DesignJob>();
     a.njobs = n;
     a.total_rows = rows;
     a.total_items = items;
     a.total_tiles = tiles;
-    a.lam_u = ctx->lam_u.as<double>();
-    a.z64 = ctx->z64.as<double>();
-    a.z32 = ctx->z32.as<float>();
-    a.lp = ctx->lp.as<LamParams>();
-    a.lx = ctx->lx.as<ExactLam>();
-    a.hist = ctx->hist.as<unsigned long long>();
-    a.S1 = ctx->S1.as<unsigned long long>();
-    a.S2 = ctx->S2.as<unsigned long long>();
-    a.acc = ctx->acc.as<DesignAcc>();
-    a.tiles_done = ctx->tiles.as<unsigned int>();
-    a.out = ctx->out.as<DesignOut>();
-    a.ctl = ctx->ctl.as<Control>();
-    a.queue = ctx->queue.as<QEntry>();
-    a.qcap = ctx->qcap;
+    a.lam_u = S.lam_u.as<double>();
+    a.z64 = S.z64.as<double>();
+    a.z32 = S.z32.as<float>();
+    a.lp = S.lp.as<LamParams>();
+    a.lx = S.lx.as<ExactLam>();
+    a.hist = S.hist.as<unsigned long long>();
+    a.S1 = S.S1.as<unsigned long long>();
+    a.S2 = S.S2.as<unsigned long long>();
+    a.acc = S.acc.as<DesignAcc>();
+    a.tiles_done = S.tiles.as<unsigned int>();
+    a.out = S.out.as<DesignOut>();
+    a.ctl = S.ctl.as<Control>();
+    a.queue = S.queue.as<QEntry>();
+    a.qcap = S.qcap;
     a.ray_tile = ctx->ray_tile;
     a.mode = mode;
     if (mode == CPD_TRACE_FP32) {
@@ -278,62 +334,70 @@ int run_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode,
         a.guards = default_guards();
         a.yguard_rel = kYGuardRel;
     }
-    a.p_out = p_out_host ? ctx->pout.as<double>() : nullptr;
+    a.p_out = p_out_host ? S.pout.as<double>() : nullptr;
     a.logtab = ctx->logtab.as<float>();
 
     // The device work of a pass, captured once per signature and replayed.
     std::vector<uint8_t> key(sizeof(a) + 3 * sizeof(uint32_t));
     std::memcpy(key.data(), &a, sizeof(a));
-    uint32_t extra[3] = {n, ctx->warps_per_cta, (uint32_t)ctx->num_sms};
+    const uint32_t extra[3] = {n, ctx->warps_per_cta, (uint32_t)ctx->num_sms};
     std::memcpy(key.data() + sizeof(a), extra, sizeof(extra));
     auto record = [&](cudaStream_t st) -> int {
-        int l = 0;
-        cudaMemsetAsync(ctx->ctl.p, 0, sizeof(Control), st);
-        cudaMemsetAsync(ctx->tiles.p, 0, sizeof(unsigned int) * n, st);
-        l = launch_pass(a, ctx->num_sms, ctx->warps_per_cta, st, ctx->profiling ? ctx->kev : nullptr);
-        cudaMemcpyAsync(ctx->h_out.p, ctx->out.p, sizeof(DesignOut) * n, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(ctx->h_ctl.p, ctx->ctl.p, sizeof(Control), cudaMemcpyDeviceToHost, st);
+        cudaMemsetAsync(S.ctl.p, 0, sizeof(Control), st);
+        cudaMemsetAsync(S.tiles.p, 0, sizeof(unsigned int) * n, st);
+        const int l = launch_pass(a, ctx->num_sms, ctx->warps_per_cta, st, profile ? S.kev : nullptr);
+        cudaMemcpyAsync(S.h_out.p, S.out.p, sizeof(DesignOut) * n, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(S.h_ctl.p, S.ctl.p, sizeof(Control), cudaMemcpyDeviceToHost, st);
         return l;
     };
-    CPD_TRY(cudaEventRecord(ctx->ev0, s));
-    int launches = 0;
-    if (ctx->use_graphs && !ctx->profiling) {
-        if (!ctx->graph_exec || key != ctx->graph_key) {
-            if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
-            ctx->graph_exec = nullptr;
+    CPD_TRY(cudaEventRecord(S.ev0, s));
+    if (use_graph && !profile) {
+        if (!S.graph_exec || key != S.graph_key) {
+            if (S.graph_exec) cudaGraphExecDestroy(S.graph_exec);
+            S.graph_exec = nullptr;
             cudaGraph_t g = nullptr;
             CPD_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            ctx->graph_launches = record(s);
+            S.graph_launches = record(s);
             CPD_TRY(cudaStreamEndCapture(s, &g));
-            cudaError_t e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+            const cudaError_t e = cudaGraphInstantiate(&S.graph_exec, g, 0);
             cudaGraphDestroy(g);
             CPD_TRY(e);
-            ctx->graph_key = key;
+            S.graph_key = key;
         }
-        CPD_TRY(cudaGraphLaunch(ctx->graph_exec, s));
-        launches = ctx->graph_launches;
+        CPD_TRY(cudaGraphLaunch(S.graph_exec, s));
+        S.launches = S.graph_launches;
     } else {
-        launches = record(s);
+        S.launches = record(s);
         CPD_TRY(cudaGetLastError());
     }
-    CPD_TRY(cudaEventRecord(ctx->ev1, s));
+    CPD_TRY(cudaEventRecord(S.ev1, s));
     if (p_out_host)
-        CPD_TRY(cudaMemcpyAsync(p_out_host, ctx->pout.p, sizeof(double) * hist, cudaMemcpyDeviceToHost, s));
-    CPD_TRY(cudaStreamSynchronize(s));
+        CPD_TRY(cudaMemcpyAsync(p_out_host, S.pout.p, sizeof(double) * hist, cudaMemcpyDeviceToHost, s));
+    CPD_TRY(cudaEventRecord(S.done, s));
+    S.n = n;
+    S.hist_cells = hist;
+    S.p_out_host = p_out_host;
+    S.profiled = profile;
+    return CPD_OK;
+}
+
+// Collects the results of the pass issued on `S` (its `done` event has completed).
+int pass_finish(PassSlot &S, PassResult &res)
+{
+    CPD_TRY(cudaEventSynchronize(S.done));
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    ctx->last_ms = ms;
-    ctx->last_launches = (uint32_t)launches;
-    if (ctx->profiling)
+    cudaEventElapsedTime(&ms, S.ev0, S.ev1);
+    S.last_ms = ms;
+    if (S.profiled)
         for (int i = 0; i < 4; i++) {
             float km = 0.f;
-            cudaEventElapsedTime(&km, ctx->kev[i], ctx->kev[i + 1]);
-            ctx->kernel_ms[i] = km;
+            cudaEventElapsedTime(&km, S.kev[i], S.kev[i + 1]);
+            S.kernel_ms[i] = km;
         }
-    const Control *c = ctx->h_ctl.as<Control>();
-    res.overflow = c->overflow != 0 || c->queue_count > ctx->qcap;
-    if (res.overflow) ctx->hist_dirty = true;
-    res.outs.assign(ctx->h_out.as<DesignOut>(), ctx->h_out.as<DesignOut>() + n);
+    const Control *c = S.h_ctl.as<Control>();
+    res.overflow = c->overflow != 0 || c->queue_count > S.qcap;
+    if (res.overflow) S.hist_dirty = true;
+    res.outs.assign(S.h_out.as<DesignOut>(), S.h_out.as<DesignOut>() + S.n);
     return CPD_OK;
 }
 
@@ -359,25 +423,215 @@ bool valid_design(const cpd_design *d)
     return d && d->nglass >= 1 && d->nglass <= CPD_MAX_GLASS && d->bin_count >= 1 && d->bin_count <= CPD_MAX_BINS;
 }
 
-// Runs one pass, growing the re-trace queue and re-running the pass if it overflowed.
-// A pass that overflowed leaves the persistent accumulators untouched (the entropy
-// kernel skips such a pass), so the re-run is exact.
-int run_pass_checked(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode, bool fresh,
-                     double *p_out, PassResult &res)
+bool valid_item(const cpd_batch_item &it)
+{
+    return it.max_n >= 1 && it.max_n <= CPD_MAX_WAVELENGTHS && it.max_eval >= 1 && it.max_eval <= CPD_MAX_RAYS;
+}
+
+// Runs one pass on `S` to completion, growing the re-trace queue and re-running the
+// pass if it overflowed. A pass that overflowed leaves the persistent accumulators
+// untouched (the entropy kernel skips such a pass), so the re-run is exact.
+int run_pass_checked(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds, uint32_t mode, bool fresh,
+                     double *p_out, PassResult &res, bool use_graph)
 {
     for (int attempt = 0; attempt < 6; attempt++) {
-        int e = run_pass(ctx, ds, mode, fresh, p_out, res);
+        int e = pass_issue(ctx, S, ds, mode, fresh, p_out, use_graph, ctx->profiling);
+        if (!e) e = pass_finish(S, res);
         if (e) {
-            ctx->hist_dirty = true;
+            S.hist_dirty = true;
             return e;
         }
         if (!res.overflow) return CPD_OK;
-        ctx->qcap *= 4;
+        S.qcap *= 4;
     }
     return CPD_NO_CAPACITY;
 }
 
 }  // namespace
+
+// ------------------------------------------------------------------ the server
+
+namespace {
+struct SrvRequest {
+    std::vector<cpd_design> designs;
+    std::vector<cpd_batch_item> items;
+    std::vector<cpd_fitness> outs;
+    uint32_t remaining = 0;
+    uint32_t mode = 0;
+    int status = CPD_OK;
+    bool done = false;
+    std::chrono::steady_clock::time_point t_submit, t_done;
+};
+struct SrvWork {
+    uint64_t req;
+    uint32_t idx;
+    uint64_t bytes;
+};
+}  // namespace
+
+struct cpd_server {
+    cpd_context *ctx = nullptr;
+    std::vector<std::unique_ptr<PassSlot>> slots;
+    std::vector<std::vector<SrvWork>> slot_work;
+    std::vector<bool> busy;
+    uint64_t budget = 0, in_use = 0;
+    uint32_t max_designs_per_pass = 256;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<SrvWork> pending;
+    std::map<uint64_t, SrvRequest> reqs;
+    uint64_t next_id = 1;
+    std::thread worker;
+    bool stop = false;
+    uint64_t designs_done = 0, passes = 0, max_in_flight = 0;
+};
+
+namespace {
+
+// Completes the pass on slot i (called by the worker without the lock held for the
+// device wait; the lock is taken to publish results).
+void srv_complete(cpd_server *sv, size_t i)
+{
+    PassSlot &S = *sv->slots[i];
+    PassResult res;
+    int e = pass_finish(S, res);
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto &work = sv->slot_work[i];
+    if (!e && res.overflow) e = CPD_NO_CAPACITY;  // re-queued below with a larger queue
+    if (e == CPD_NO_CAPACITY && S.qcap < (1u << 26)) {
+        // grow the re-trace queue and run the same designs again
+        S.qcap *= 4;
+        for (auto it = work.rbegin(); it != work.rend(); ++it) {
+            sv->in_use -= it->bytes;
+            sv->pending.push_front(*it);
+        }
+        e = CPD_OK;
+        work.clear();
+    }
+    for (size_t k = 0; k < work.size(); k++) {
+        auto rit = sv->reqs.find(work[k].req);
+        if (rit == sv->reqs.end()) continue;
+        SrvRequest &r = rit->second;
+        if (e) r.status = e;
+        else fill_fitness(r.designs[work[k].idx], res.outs[k],
+                          (uint64_t)r.items[work[k].idx].max_n * r.items[work[k].idx].max_eval, r.outs[work[k].idx],
+                          true);
+        if (--r.remaining == 0) {
+            r.done = true;
+            r.t_done = std::chrono::steady_clock::now();
+        }
+        sv->designs_done++;
+    }
+    for (auto &w : work) sv->in_use -= w.bytes;
+    work.clear();
+    sv->busy[i] = false;
+    sv->passes++;
+    sv->cv_done.notify_all();
+}
+
+void srv_loop(cpd_server *sv)
+{
+    cudaSetDevice(sv->ctx->device);
+    for (;;) {
+        bool progressed = false;
+        // completions
+        for (size_t i = 0; i < sv->slots.size(); i++) {
+            bool b;
+            {
+                std::lock_guard<std::mutex> lk(sv->mu);
+                b = sv->busy[i];
+            }
+            if (b && cudaEventQuery(sv->slots[i]->done) != cudaErrorNotReady) {
+                srv_complete(sv, i);
+                progressed = true;
+            }
+        }
+        // admissions: each free slot takes the oldest pending designs of one trace mode
+        // while they fit the device-memory budget
+        for (size_t i = 0; i < sv->slots.size(); i++) {
+            std::vector<SrvWork> take;
+            std::vector<DevDesign> devs;
+            std::vector<std::vector<double>> lams;
+            std::vector<RayTablePtr> rays;
+            uint32_t mode = 0;
+            {
+                std::lock_guard<std::mutex> lk(sv->mu);
+                if (sv->busy[i] || sv->pending.empty()) continue;
+                bool others = false;
+                for (size_t j = 0; j < sv->slots.size(); j++) others |= sv->busy[j];
+                mode = sv->reqs[sv->pending.front().req].mode;
+                while (!sv->pending.empty() && take.size() < sv->max_designs_per_pass) {
+                    const SrvWork &w = sv->pending.front();
+                    if (sv->reqs[w.req].mode != mode) break;
+                    if (sv->in_use + w.bytes > sv->budget && (others || !take.empty())) break;
+                    sv->in_use += w.bytes;
+                    take.push_back(w);
+                    sv->pending.pop_front();
+                }
+                if (take.empty()) continue;
+                sv->busy[i] = true;
+                sv->slot_work[i] = take;
+                uint64_t nb = 0;
+                for (size_t j = 0; j < sv->slots.size(); j++) nb += sv->busy[j];
+                sv->max_in_flight = std::max<uint64_t>(sv->max_in_flight, nb);
+            }
+            // host preparation and issue without the lock (the slot belongs to the worker)
+            std::vector<PassDesign> ds(take.size());
+            devs.resize(take.size());
+            lams.resize(take.size());
+            rays.resize(take.size());
+            for (size_t k = 0; k < take.size(); k++) {
+                const SrvRequest *r;
+                {
+                    std::lock_guard<std::mutex> lk(sv->mu);
+                    r = &sv->reqs[take[k].req];
+                }
+                const cpd_batch_item &it = r->items[take[k].idx];
+                design_to_dev(r->designs[take[k].idx], devs[k]);
+                lams[k].resize(it.max_n);
+                seed_points(it.seed, 0, it.max_n, lams[k].data());
+                rays[k] = ray_table_cached(sv->ctx, it.seed, it.max_eval);
+                ds[k] = PassDesign{&devs[k], it.max_n, it.max_eval, lams[k].data(), rays[k].get()};
+            }
+            int e = pass_issue(sv->ctx, *sv->slots[i], ds, mode, true, nullptr, false, false);
+            if (e) {
+                std::lock_guard<std::mutex> lk(sv->mu);
+                sv->slots[i]->hist_dirty = true;
+                for (auto &w : take) {
+                    SrvRequest &r = sv->reqs[w.req];
+                    r.status = e;
+                    if (--r.remaining == 0) {
+                        r.done = true;
+                        r.t_done = std::chrono::steady_clock::now();
+                    }
+                    sv->in_use -= w.bytes;
+                }
+                sv->busy[i] = false;
+                sv->slot_work[i].clear();
+                sv->cv_done.notify_all();
+            }
+            progressed = true;
+        }
+        {
+            std::unique_lock<std::mutex> lk(sv->mu);
+            bool any_busy = false;
+            for (bool b : sv->busy) any_busy |= b;
+            if (sv->stop && !any_busy && sv->pending.empty()) return;
+            if (!progressed) {
+                if (any_busy) {
+                    lk.unlock();
+                    std::this_thread::sleep_for(std::chrono::microseconds(20));
+                } else {
+                    sv->cv_work.wait_for(lk, std::chrono::milliseconds(50));
+                }
+            }
+        }
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
 
 extern "C" {
 
@@ -387,32 +641,18 @@ int cpd_context_create(int device, cpd_context **out)
     *out = nullptr;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CPD_CUDA_ERROR;
+    if (cudaSetDevice(device) != cudaSuccess) return CPD_CUDA_ERROR;
     cpd_context *ctx = new cpd_context();
     ctx->device = device;
-    if (cudaSetDevice(device) != cudaSuccess) {
-        delete ctx;
-        return CPD_CUDA_ERROR;
-    }
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+    std::vector<float> tab(4 * ff::kLogTable);
+    ff::make_log_table(tab.data());
+    if (ctx->main.create() != cudaSuccess || ctx->logtab.ensure(sizeof(float) * tab.size()) != cudaSuccess ||
+        cudaMemcpy(ctx->logtab.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        ctx->main.destroy();
+        ctx->logtab.release();
         delete ctx;
         return CPD_CUDA_ERROR;
-    }
-    for (int i = 0; i < 5; i++)
-        if (cudaEventCreate(&ctx->kev[i]) != cudaSuccess) {
-            delete ctx;
-            return CPD_CUDA_ERROR;
-        }
-    {
-        std::vector<float> tab(4 * ff::kLogTable);
-        ff::make_log_table(tab.data());
-        if (ctx->logtab.ensure(sizeof(float) * tab.size()) != cudaSuccess ||
-            cudaMemcpy(ctx->logtab.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice) !=
-                cudaSuccess) {
-            delete ctx;
-            return CPD_CUDA_ERROR;
-        }
     }
     *out = ctx;
     return CPD_OK;
@@ -422,20 +662,10 @@ void cpd_context_destroy(cpd_context *ctx)
 {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
-    for (DevBuf *b : {&ctx->designs, &ctx->jobs, &ctx->lam_u, &ctx->z64, &ctx->z32, &ctx->lp, &ctx->lx, &ctx->hist, &ctx->S1,
-                      &ctx->S2, &ctx->acc, &ctx->tiles, &ctx->out, &ctx->ctl, &ctx->queue, &ctx->pout,
-                      &ctx->pair_lam, &ctx->pair_z, &ctx->pair_bins, &ctx->pair_ts, &ctx->pair_flags, &ctx->peak,
+    ctx->main.destroy();
+    for (DevBuf *b : {&ctx->pair_lam, &ctx->pair_z, &ctx->pair_bins, &ctx->pair_ts, &ctx->pair_flags, &ctx->peak,
                       &ctx->logtab})
         b->release();
-    for (HostBuf *b : {&ctx->h_designs, &ctx->h_jobs, &ctx->h_lam, &ctx->h_z64, &ctx->h_z32, &ctx->h_out, &ctx->h_ctl,
-                       &ctx->h_pout, &ctx->h_pairs})
-        b->release();
-    cudaEventDestroy(ctx->ev0);
-    cudaEventDestroy(ctx->ev1);
-    for (int i = 0; i < 5; i++) cudaEventDestroy(ctx->kev[i]);
-    cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
 
@@ -462,8 +692,8 @@ int cpd_get_launch_shape(cpd_context *ctx, uint32_t *ray_tile, uint32_t *warps_p
 int cpd_last_timing(cpd_context *ctx, double *kernel_ms, uint32_t *launches)
 {
     if (!ctx) return CPD_INVALID_ARGUMENT;
-    if (kernel_ms) *kernel_ms = ctx->last_ms;
-    if (launches) *launches = ctx->last_launches;
+    if (kernel_ms) *kernel_ms = ctx->main.last_ms;
+    if (launches) *launches = (uint32_t)ctx->main.launches;
     return CPD_OK;
 }
 
@@ -475,20 +705,25 @@ int cpd_set_profiling(cpd_context *ctx, int on)
     return CPD_OK;
 }
 
-int cpd_last_transfer_bytes(cpd_context *ctx, uint64_t *h2d, uint64_t *d2h)
-{
-    if (!ctx) return CPD_INVALID_ARGUMENT;
-    if (h2d) *h2d = ctx->last_h2d;
-    if (d2h) *d2h = ctx->last_d2h;
-    return CPD_OK;
-}
-
 int cpd_last_kernel_times(cpd_context *ctx, double ms[4])
 {
     if (!ctx || !ms) return CPD_INVALID_ARGUMENT;
-    for (int i = 0; i < 4; i++) ms[i] = ctx->kernel_ms[i];
+    for (int i = 0; i < 4; i++) ms[i] = ctx->main.kernel_ms[i];
     return CPD_OK;
 }
+
+int cpd_last_transfer_bytes(cpd_context *ctx, uint64_t *h2d, uint64_t *d2h)
+{
+    if (!ctx) return CPD_INVALID_ARGUMENT;
+    if (h2d) *h2d = ctx->main.h2d;
+    if (d2h) *d2h = ctx->main.d2h;
+    return CPD_OK;
+}
+
+#define CPD_SYNC_ENTRY(ctx)                                                 \
+    std::lock_guard<std::mutex> lk((ctx)->mu);                              \
+    if (cudaSetDevice((ctx)->device) != cudaSuccess) return CPD_CUDA_ERROR; \
+    (ctx)->main.h2d = (ctx)->main.d2h = 0
 
 int cpd_fitness_gpu_points(cpd_context *ctx, const cpd_design *d, const double *lam_u, uint32_t W,
                            const double *ray_u, uint32_t R, uint32_t trace_mode, cpd_fitness *out, double *p_out)
@@ -496,16 +731,14 @@ int cpd_fitness_gpu_points(cpd_context *ctx, const cpd_design *d, const double *
     if (!ctx || !valid_design(d) || !lam_u || !ray_u || !out) return CPD_INVALID_ARGUMENT;
     if (W == 0 || W > CPD_MAX_WAVELENGTHS || R == 0 || R > CPD_MAX_RAYS || trace_mode > CPD_TRACE_FP64)
         return CPD_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return CPD_CUDA_ERROR;
-    ctx->last_h2d = ctx->last_d2h = 0;
+    CPD_SYNC_ENTRY(ctx);
     DevDesign D;
     design_to_dev(*d, D);
     RayTable rt;
     ray_table(ray_u, R, rt.z64, rt.z32);
     std::vector<PassDesign> ds{PassDesign{&D, W, R, lam_u, &rt}};
     PassResult res;
-    int e = run_pass_checked(ctx, ds, trace_mode, true, p_out, res);
+    int e = run_pass_checked(ctx, ctx->main, ds, trace_mode, true, p_out, res, ctx->use_graphs);
     if (e) return e;
     fill_fitness(*d, res.outs[0], (uint64_t)W * R, *out, false);
     return CPD_OK;
@@ -517,9 +750,7 @@ int cpd_fitness_gpu(cpd_context *ctx, const cpd_design *d, const double *seeds, 
     if (!ctx || !valid_design(d) || !seeds || !out || nseeds == 0) return CPD_INVALID_ARGUMENT;
     if (max_n == 0 || max_eval == 0 || max_eval > CPD_MAX_RAYS) return CPD_INVALID_ARGUMENT;
     if ((uint64_t)max_n * nseeds > CPD_MAX_WAVELENGTHS) return CPD_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return CPD_CUDA_ERROR;
-    ctx->last_h2d = ctx->last_d2h = 0;
+    CPD_SYNC_ENTRY(ctx);
     if (nwarp >= 1 && nwarp <= 8) ctx->warps_per_cta = nwarp;
     DevDesign D;
     design_to_dev(*d, D);
@@ -528,9 +759,9 @@ int cpd_fitness_gpu(cpd_context *ctx, const cpd_design *d, const double *seeds, 
     uint64_t rays = 0;
     for (uint32_t s = 0; s < nseeds; s++) {
         seed_points(seeds[s], 0, max_n, lam.data());
-        const RayTable &rt = ray_table_cached(ctx, seeds[s], max_eval);
-        std::vector<PassDesign> ds{PassDesign{&D, max_n, max_eval, lam.data(), &rt}};
-        int e = run_pass_checked(ctx, ds, CPD_TRACE_HYBRID, s == 0, nullptr, res);
+        RayTablePtr rt = ray_table_cached(ctx, seeds[s], max_eval);
+        std::vector<PassDesign> ds{PassDesign{&D, max_n, max_eval, lam.data(), rt.get()}};
+        int e = run_pass_checked(ctx, ctx->main, ds, CPD_TRACE_HYBRID, s == 0, nullptr, res, ctx->use_graphs);
         if (e) return e;
         rays += (uint64_t)max_n * max_eval;
         if (res.outs[0].converged) break;
@@ -543,29 +774,22 @@ int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd
                           uint32_t trace_mode, cpd_fitness *outs)
 {
     if (!ctx || !designs || !items || !outs || n == 0 || trace_mode > CPD_TRACE_FP64) return CPD_INVALID_ARGUMENT;
-    for (uint32_t i = 0; i < n; i++) {
-        if (!valid_design(&designs[i])) return CPD_INVALID_ARGUMENT;
-        if (items[i].max_n == 0 || items[i].max_n > CPD_MAX_WAVELENGTHS || items[i].max_eval == 0 ||
-            items[i].max_eval > CPD_MAX_RAYS)
-            return CPD_INVALID_ARGUMENT;
-    }
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return CPD_CUDA_ERROR;
-    ctx->last_h2d = ctx->last_d2h = 0;
+    for (uint32_t i = 0; i < n; i++)
+        if (!valid_design(&designs[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
+    CPD_SYNC_ENTRY(ctx);
     std::vector<DevDesign> devs(n);
     std::vector<std::vector<double>> lams(n);
+    std::vector<RayTablePtr> rts(n);
     std::vector<PassDesign> ds(n);
     for (uint32_t i = 0; i < n; i++) {
         design_to_dev(designs[i], devs[i]);
         lams[i].resize(items[i].max_n);
         seed_points(items[i].seed, 0, items[i].max_n, lams[i].data());
-    }
-    for (uint32_t i = 0; i < n; i++) {
-        const RayTable &rt = ray_table_cached(ctx, items[i].seed, items[i].max_eval);
-        ds[i] = PassDesign{&devs[i], items[i].max_n, items[i].max_eval, lams[i].data(), &rt};
+        rts[i] = ray_table_cached(ctx, items[i].seed, items[i].max_eval);
+        ds[i] = PassDesign{&devs[i], items[i].max_n, items[i].max_eval, lams[i].data(), rts[i].get()};
     }
     PassResult res;
-    int e = run_pass_checked(ctx, ds, trace_mode, true, nullptr, res);
+    int e = run_pass_checked(ctx, ctx->main, ds, trace_mode, true, nullptr, res, ctx->use_graphs);
     if (e) return e;
     for (uint32_t i = 0; i < n; i++)
         fill_fitness(designs[i], res.outs[i], (uint64_t)items[i].max_n * items[i].max_eval, outs[i], true);
@@ -599,62 +823,158 @@ int cpd_trace_rays(cpd_context *ctx, const cpd_design *d, const double *lam_u, c
     if (!ctx || !valid_design(d) || !lam_u || !ray_u || !bins || !ts || trace_mode > CPD_TRACE_FP64)
         return CPD_INVALID_ARGUMENT;
     if (n == 0) return CPD_OK;
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return CPD_CUDA_ERROR;
-    ctx->last_h2d = ctx->last_d2h = 0;
+    CPD_SYNC_ENTRY(ctx);
+    PassSlot &S = ctx->main;
     DevDesign D;
     design_to_dev(*d, D);
     std::vector<double> z(n);
     for (uint32_t i = 0; i < n; i++) z[i] = norminv(ray_u[i]);
-    cudaStream_t s = ctx->stream;
-    CPD_TRY(ctx->designs.ensure(sizeof(DevDesign)));
+    cudaStream_t s = S.stream;
+    CPD_TRY(S.designs.ensure(sizeof(DevDesign)));
     CPD_TRY(ctx->pair_lam.ensure(sizeof(double) * n));
     CPD_TRY(ctx->pair_z.ensure(sizeof(double) * n));
     CPD_TRY(ctx->pair_bins.ensure(sizeof(uint32_t) * n));
     CPD_TRY(ctx->pair_ts.ensure(sizeof(double) * n));
     CPD_TRY(ctx->pair_flags.ensure(n));
-    CPD_TRY(cudaMemcpyAsync(ctx->designs.p, &D, sizeof(DevDesign), cudaMemcpyHostToDevice, s));
+    CPD_TRY(cudaMemcpyAsync(S.designs.p, &D, sizeof(DevDesign), cudaMemcpyHostToDevice, s));
     CPD_TRY(cudaMemcpyAsync(ctx->pair_lam.p, lam_u, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     CPD_TRY(cudaMemcpyAsync(ctx->pair_z.p, z.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    CPD_TRY(cudaEventRecord(ctx->ev0, s));
-    launch_trace_pairs(ctx->designs.as<DevDesign>(), ctx->pair_lam.as<double>(), ctx->pair_z.as<double>(), n,
+    CPD_TRY(cudaEventRecord(S.ev0, s));
+    launch_trace_pairs(S.designs.as<DevDesign>(), ctx->pair_lam.as<double>(), ctx->pair_z.as<double>(), n,
                        trace_mode, ctx->pair_bins.as<uint32_t>(), ctx->pair_ts.as<double>(),
                        ctx->pair_flags.as<uint8_t>(), s);
     CPD_TRY(cudaGetLastError());
-    CPD_TRY(cudaEventRecord(ctx->ev1, s));
+    CPD_TRY(cudaEventRecord(S.ev1, s));
     CPD_TRY(cudaMemcpyAsync(bins, ctx->pair_bins.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
     CPD_TRY(cudaMemcpyAsync(ts, ctx->pair_ts.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     if (flags) CPD_TRY(cudaMemcpyAsync(flags, ctx->pair_flags.p, n, cudaMemcpyDeviceToHost, s));
     CPD_TRY(cudaStreamSynchronize(s));
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    ctx->last_ms = ms;
-    ctx->last_launches = 1;
+    cudaEventElapsedTime(&ms, S.ev0, S.ev1);
+    S.last_ms = ms;
+    S.launches = 1;
     return CPD_OK;
 }
 
 int cpd_measure_fp32_peak(cpd_context *ctx, uint32_t iters, double *tflops)
 {
     if (!ctx || !tflops || iters == 0) return CPD_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return CPD_CUDA_ERROR;
-    ctx->last_h2d = ctx->last_d2h = 0;
+    CPD_SYNC_ENTRY(ctx);
+    PassSlot &S = ctx->main;
     const int threads = 256;
     const int blocks = ctx->num_sms * 8;
     CPD_TRY(ctx->peak.ensure(sizeof(float) * blocks));
-    cudaStream_t s = ctx->stream;
+    cudaStream_t s = S.stream;
     launch_fma_peak(ctx->peak.as<float>(), 16, blocks, threads, s);  // warm-up
-    CPD_TRY(cudaEventRecord(ctx->ev0, s));
+    CPD_TRY(cudaEventRecord(S.ev0, s));
     launch_fma_peak(ctx->peak.as<float>(), iters, blocks, threads, s);
-    CPD_TRY(cudaEventRecord(ctx->ev1, s));
+    CPD_TRY(cudaEventRecord(S.ev1, s));
     CPD_TRY(cudaStreamSynchronize(s));
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    cudaEventElapsedTime(&ms, S.ev0, S.ev1);
     const double flops = 2.0 * 8.0 * 16.0 * (double)iters * threads * (double)blocks;
     *tflops = flops / (ms * 1e-3) / 1e12;
-    ctx->last_ms = ms;
-    ctx->last_launches = 2;
+    S.last_ms = ms;
+    S.launches = 2;
     return CPD_OK;
+}
+
+// ------------------------------------------------------------------ server ABI
+
+int cpd_server_create(cpd_context *ctx, uint64_t mem_budget_bytes, uint32_t slots, uint32_t max_designs_per_pass,
+                      cpd_server **out)
+{
+    if (!ctx || !out || slots == 0 || slots > 8 || mem_budget_bytes == 0) return CPD_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return CPD_CUDA_ERROR;
+    cpd_server *sv = new cpd_server();
+    sv->ctx = ctx;
+    sv->budget = mem_budget_bytes;
+    if (max_designs_per_pass) sv->max_designs_per_pass = max_designs_per_pass;
+    for (uint32_t i = 0; i < slots; i++) {
+        sv->slots.emplace_back(new PassSlot());
+        if (sv->slots.back()->create() != cudaSuccess) {
+            for (auto &s : sv->slots) s->destroy();
+            delete sv;
+            return CPD_CUDA_ERROR;
+        }
+    }
+    sv->slot_work.resize(slots);
+    sv->busy.assign(slots, false);
+    sv->worker = std::thread(srv_loop, sv);
+    *out = sv;
+    return CPD_OK;
+}
+
+int cpd_server_submit(cpd_server *sv, const cpd_design *designs, const cpd_batch_item *items, uint32_t n,
+                      uint32_t trace_mode, uint64_t *request_id)
+{
+    if (!sv || !designs || !items || !request_id || n == 0 || trace_mode > CPD_TRACE_FP64) return CPD_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < n; i++)
+        if (!valid_design(&designs[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->stop) return CPD_INVALID_ARGUMENT;
+    const uint64_t id = sv->next_id++;
+    SrvRequest &r = sv->reqs[id];
+    r.designs.assign(designs, designs + n);
+    r.items.assign(items, items + n);
+    r.outs.resize(n);
+    r.remaining = n;
+    r.mode = trace_mode;
+    r.t_submit = std::chrono::steady_clock::now();
+    for (uint32_t i = 0; i < n; i++)
+        sv->pending.push_back(
+            SrvWork{id, i, design_bytes(items[i].max_n, items[i].max_eval, designs[i].bin_count)});
+    *request_id = id;
+    sv->cv_work.notify_one();
+    return CPD_OK;
+}
+
+int cpd_server_wait(cpd_server *sv, uint64_t request_id, cpd_fitness *outs, double timeout_ms, double *latency_ms)
+{
+    if (!sv || !outs) return CPD_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(request_id);
+    if (it == sv->reqs.end()) return CPD_INVALID_ARGUMENT;
+    const auto deadline = std::chrono::steady_clock::now() +
+                          std::chrono::microseconds((int64_t)(std::max(0.0, timeout_ms) * 1000.0));
+    while (!it->second.done) {
+        if (sv->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && !it->second.done) return CPD_TIMEOUT;
+        it = sv->reqs.find(request_id);
+        if (it == sv->reqs.end()) return CPD_INVALID_ARGUMENT;
+    }
+    SrvRequest &r = it->second;
+    std::memcpy(outs, r.outs.data(), sizeof(cpd_fitness) * r.outs.size());
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r.t_done - r.t_submit).count();
+    const int status = r.status;
+    sv->reqs.erase(it);
+    return status;
+}
+
+int cpd_server_stats(cpd_server *sv, uint64_t *designs_done, uint64_t *passes, uint64_t *max_in_flight,
+                     uint64_t *pending)
+{
+    if (!sv) return CPD_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (designs_done) *designs_done = sv->designs_done;
+    if (passes) *passes = sv->passes;
+    if (max_in_flight) *max_in_flight = sv->max_in_flight;
+    if (pending) *pending = sv->pending.size();
+    return CPD_OK;
+}
+
+void cpd_server_destroy(cpd_server *sv)
+{
+    if (!sv) return;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+        sv->cv_work.notify_all();
+    }
+    if (sv->worker.joinable()) sv->worker.join();
+    cudaSetDevice(sv->ctx->device);
+    for (auto &s : sv->slots) s->destroy();
+    delete sv;
 }
 
 }  // extern "C"

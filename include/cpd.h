@@ -125,6 +125,16 @@ int cpd_position_detector_array(const cpd_spectrometer_params *p, double accepta
  * argument checks of SizedCompoundPrism::new (src/pylib.rs:514-561). */
 int cpd_design_build(const cpd_spectrometer_params *p, cpd_design *out);
 
+/* No reference counterpart: cpd_design_build over n parameter records, for an
+ * optimizer that builds a whole generation at once (designer.py:203-265 builds one
+ * Spectrometer per call). With acceptance in (0, 1] each detector is first placed by
+ * cpd_position_detector_array (its det_position/det_flipped inputs are ignored); with
+ * acceptance 0 they are used as given. status[i] is design i's cpd_design_build or
+ * positioning status; a failed design is zero-filled. Returns CPD_OK unless the
+ * arguments are invalid. */
+int cpd_design_build_batch(const cpd_spectrometer_params *p, uint32_t n, double acceptance,
+                           cpd_design *out, int32_t *status);
+
 /* CompoundPrism.exit_ray (src/pylib.rs:563-573): out = {x, y, dir x, dir y}. */
 int cpd_exit_ray(const cpd_design *d, double y, double wavelength, double out[4]);
 
@@ -242,6 +252,35 @@ int cpd_last_transfer_bytes(cpd_context *ctx, uint64_t *h2d, uint64_t *d2h);
 /* FP32 FMA throughput probe: runs a dependent-chain-free FMA kernel for `iters`
  * iterations on every SM and returns the achieved TFLOP/s (roofline peak). */
 int cpd_measure_fp32_peak(cpd_context *ctx, uint32_t iters, double *tflops);
+
+/* ---------------------------------------------------------------- serving */
+
+/* Continuous-batching fitness server (no reference counterpart: the reference's
+ * optimizer, designer.py:267-300, calls gpu_fitness once per design and waits).
+ * Requests of any size arrive from any thread; a worker thread admits their designs
+ * first-come first-served into passes while the device bytes of the designs in flight
+ * (histogram, per-wavelength tables and ray tables; about W*(8B+400) + 16R bytes each)
+ * stay within mem_budget_bytes, and keeps up to `slots` passes in flight on separate
+ * streams. A design larger than the budget runs alone. max_designs_per_pass caps one
+ * pass (0 = 256). Each design's result is bitwise the one it gets alone
+ * (cpd_fitness_gpu_batch with n = 1): the accumulation is integer and
+ * order-independent. */
+typedef struct cpd_server cpd_server;
+int cpd_server_create(cpd_context *ctx, uint64_t mem_budget_bytes, uint32_t slots,
+                      uint32_t max_designs_per_pass, cpd_server **out);
+/* Queues n designs (one trace mode per request); returns a request id at once. */
+int cpd_server_submit(cpd_server *sv, const cpd_design *designs, const cpd_batch_item *items,
+                      uint32_t n, uint32_t trace_mode, uint64_t *request_id);
+/* Waits up to timeout_ms for a request. On completion writes its n results, the time
+ * from submit to completion (latency_ms, optional), forgets the request and returns
+ * CPD_OK (or the error a pass met); on timeout returns CPD_TIMEOUT and the request
+ * stays queued. */
+int cpd_server_wait(cpd_server *sv, uint64_t request_id, cpd_fitness *outs, double timeout_ms,
+                    double *latency_ms);
+int cpd_server_stats(cpd_server *sv, uint64_t *designs_done, uint64_t *passes,
+                     uint64_t *max_passes_in_flight, uint64_t *pending_designs);
+/* Finishes every queued design, then stops the worker and frees the slots. */
+void cpd_server_destroy(cpd_server *sv);
 
 #ifdef __cplusplus
 }
