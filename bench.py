@@ -369,6 +369,9 @@ def main():
             extras["roofline"] = {"error": repr(e)}
         try:
             pop, Ws, rej = batched_population()
+            t_tune = time.perf_counter()
+            tuned = cpd.autotune_batch(pop, seeds=0.5, max_n=Ws, max_eval=R_PLAIN, context=ctx)
+            t_tune = time.perf_counter() - t_tune
             for _ in range(2):
                 cpd.fitness_batch(pop, seeds=0.5, max_n=Ws, max_eval=R_PLAIN, context=ctx)
             bt = []
@@ -384,7 +387,9 @@ def main():
                 "workload": f"{nb} designs, G in 2..6, B in 16..128, W in 512..4096, R={R_PLAIN}",
                 "designs_per_s_device": nb / (min(bdev) / 1e3), "designs_per_s_e2e": nb / min(bt),
                 "ms_device": min(bdev), "ms_e2e": min(bt), "rays": int(sum(int(w) for w in Ws) * R_PLAIN),
-                "speedup_vs_plain_e2e": (nb / min(bt)) / e2e}}
+                "speedup_vs_plain_e2e": (nb / min(bt)) / e2e,
+                "autotuned_shape": {"ray_tile": tuned[0], "warps_per_cta": tuned[1], "best_ms": tuned[2],
+                                    "tuning_s": t_tune}}}
         except Exception as e:  # noqa: BLE001
             extras["forms"] = {"error": repr(e)}
         try:

@@ -25,7 +25,7 @@ __all__ = [
     "RayTraceError", "CudaError", "Glass", "DesignFitness", "Vector2D", "UnitVector2D",
     "UniformWavelengthDistribution", "GaussianBeam", "FiberBeam", "CompoundPrism",
     "position_detector_array", "DetectorArray", "Spectrometer", "Context", "default_context",
-    "fitness_batch", "build_designs", "Server", "TRACE_HYBRID", "TRACE_FP32", "TRACE_FP64",
+    "fitness_batch", "autotune_batch", "build_designs", "Server", "TRACE_HYBRID", "TRACE_FP32", "TRACE_FP64",
 ]
 
 TRACE_HYBRID = N.TRACE_HYBRID
@@ -357,6 +357,10 @@ class Context:
         _check(N.lib.cpd_last_timing(self._h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
+    def set_autotune(self, on: bool = True):
+        """Batched calls pick their launch shape with the autotuner (per batch class)."""
+        _check(N.lib.cpd_set_autotune(self._h, int(bool(on))))
+
     def set_profiling(self, on: bool = True):
         _check(N.lib.cpd_set_profiling(self._h, int(bool(on))))
 
@@ -514,11 +518,7 @@ class Spectrometer:
                 f"wavelengths={self.wavelengths.bounds}, beam={self.beam!r})")
 
 
-def fitness_batch(spectrometers: Sequence[Spectrometer], *, seeds=None, max_n=256, max_eval=16_384,
-                  mode: int = TRACE_HYBRID, context: Optional[Context] = None):
-    """Batched GPU fitness of many designs in one launch sequence (no reference
-    counterpart). max_n, max_eval and seeds may be scalars or per-design sequences.
-    Returns a list of cpd_fitness records (status OK or NOT_CONVERGED per design)."""
+def _batch_records(spectrometers, seeds, max_n, max_eval):
     n = len(spectrometers)
     designs = (N.Design * n)()
     items = (N.BatchItem * n)()
@@ -530,10 +530,31 @@ def fitness_batch(spectrometers: Sequence[Spectrometer], *, seeds=None, max_n=25
         items[i].seed = float(sd[i])
         items[i].max_n = int(mn[i])
         items[i].max_eval = int(me[i])
+    return n, designs, items
+
+
+def fitness_batch(spectrometers: Sequence[Spectrometer], *, seeds=None, max_n=256, max_eval=16_384,
+                  mode: int = TRACE_HYBRID, context: Optional[Context] = None):
+    """Batched GPU fitness of many designs in one launch sequence (no reference
+    counterpart). max_n, max_eval and seeds may be scalars or per-design sequences.
+    Returns a list of cpd_fitness records (status OK or NOT_CONVERGED per design)."""
+    n, designs, items = _batch_records(spectrometers, seeds, max_n, max_eval)
     outs = (N.Fitness * n)()
     ctx = context or default_context()
     _check(N.lib.cpd_fitness_gpu_batch(ctx.handle, designs, items, n, int(mode), outs), "fitness_batch")
     return list(outs)
+
+
+def autotune_batch(spectrometers: Sequence[Spectrometer], *, seeds=None, max_n=256, max_eval=16_384,
+                   mode: int = TRACE_HYBRID, context: Optional[Context] = None):
+    """Runs the launch-shape autotuner on a batch (cpd_autotune_batch) and leaves the
+    fastest shape set on the context. Returns (ray_tile, warps_per_cta, best_ms)."""
+    n, designs, items = _batch_records(spectrometers, seeds, max_n, max_eval)
+    ctx = context or default_context()
+    rt, w, ms = C.c_uint32(0), C.c_uint32(0), C.c_double(0.0)
+    _check(N.lib.cpd_autotune_batch(ctx.handle, designs, items, n, int(mode), C.byref(rt), C.byref(w),
+                                    C.byref(ms)), "autotune_batch")
+    return rt.value, w.value, ms.value
 
 
 def build_designs(params: np.ndarray, acceptance: float = 0.0):

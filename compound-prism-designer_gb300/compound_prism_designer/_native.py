@@ -146,6 +146,9 @@ SIGNATURES = [
                                  C.POINTER(C.c_uint8)]),
     ("cpd_fitness_gpu_batch", C.c_int, [_ctxp, C.POINTER(Design), C.POINTER(BatchItem), C.c_uint32, C.c_uint32,
                                         C.POINTER(Fitness)]),
+    ("cpd_autotune_batch", C.c_int, [_ctxp, C.POINTER(Design), C.POINTER(BatchItem), C.c_uint32, C.c_uint32, _up,
+                                     _up, _dp]),
+    ("cpd_set_autotune", C.c_int, [_ctxp, C.c_int]),
     ("cpd_set_launch_shape", C.c_int, [_ctxp, C.c_uint32, C.c_uint32]),
     ("cpd_get_launch_shape", C.c_int, [_ctxp, _up, _up]),
     ("cpd_last_timing", C.c_int, [_ctxp, _dp, _up]),

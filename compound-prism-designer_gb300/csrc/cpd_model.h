@@ -447,6 +447,9 @@ struct Guards {
 // the exact trace): no wrong decision at 0.1x these widths, the first at 0.03x.
 CPD_HD Guards default_guards() { return Guards{1.0e-4f, 1.0e-5f, 1.0e-4f, 1.0e-5f}; }
 
+// Relative part of the detector-position guard (2^-20, 16 FP32 ulps of the largest term).
+constexpr float kPosRel = 9.5367431640625e-07f;
+
 // Relative guard of the y-interval ends: both sides are f64, so a few ulps suffice.
 constexpr double kYGuardRel = 1e-11;
 
@@ -794,10 +797,14 @@ CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, flo
     const float dgu = fmaf(dpx, D.dufx, dpy * D.dufy);
     const float ddu = fmaf(dex, D.dufx, dey * D.dufy);
     const float dT = div_fast(fmaf(dgn, P.cid, -P.gn * dcid), cid * P.cid);
-    const float dpos = fmaf(ddu, P.T + dT, fmaf(P.du, dT, dgu));
+    const float tu = ddu * (P.T + dT), tt = P.du * dT;
+    const float dpos = tu + (tt + dgu);
     const float pos = P.pos + dpos;
-    if (pos < -g.pos || pos > D.L + g.pos) return RAY_LOST;
-    flag |= pos < g.pos || pos > D.L - g.pos;
+    // The position is the one unbounded quantity (a reference ray can land metres from
+    // the detector): its guard grows with the magnitudes it was summed from, 16 FP32 ulps.
+    const float gp = fmaf(kPosRel, fabs_f(P.pos) + fabs_f(tu) + fabs_f(tt) + fabs_f(dgu), g.pos);
+    if (pos < -gp || pos > D.L + gp) return RAY_LOST;
+    flag |= pos < gp || pos > D.L - gp;
     const float xx = pos - D.c0;
     float qf = floorf(xx * D.inv_slope);
     float rem = fmaf(-qf, D.slope, xx);
@@ -808,7 +815,7 @@ CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, flo
         qf += 1.f;
         rem -= D.slope;
     }
-    flag |= rem < g.pos || rem > D.slope - g.pos || fabs_f(rem - D.bin_size) < g.pos;
+    flag |= rem < gp || rem > D.slope - gp || fabs_f(rem - D.bin_size) < gp;
     if (flag) return RAY_FLAG;
     const uint32_t b = qf <= 0.f ? 0u : (uint32_t)qf;
     if (b < D.B && rem < D.bin_size) {

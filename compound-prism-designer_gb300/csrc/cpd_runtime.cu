@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -154,7 +155,10 @@ struct cpd_context {
     uint32_t warps_per_cta = 8;
     bool profiling = false;
     bool use_graphs = true;
+    bool autotune = false;
     std::map<RayKey, RayTablePtr> ray_cache;
+    // launch shape picked by the autotuner per class of batch
+    std::map<std::array<uint64_t, 5>, std::pair<uint32_t, uint32_t>> tune_cache;
 };
 
 namespace {
@@ -445,6 +449,81 @@ int run_pass_checked(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign
         S.qcap *= 4;
     }
     return CPD_NO_CAPACITY;
+}
+
+// The class of a batch for the launch-shape cache: trace mode and the binary orders of
+// magnitude of its design count, wavelength rows, rays and widest detector.
+std::array<uint64_t, 5> tune_class(const std::vector<PassDesign> &ds, uint32_t mode)
+{
+    uint64_t rows = 0, rays = 0, maxB = 0;
+    for (const PassDesign &p : ds) {
+        rows += p.W;
+        rays += (uint64_t)p.W * p.R;
+        maxB = std::max<uint64_t>(maxB, p.dev->B);
+    }
+    auto lg = [](uint64_t v) {
+        uint64_t b = 0;
+        while ((1ull << b) < v && b < 63) b++;
+        return b;
+    };
+    return {mode, lg(ds.size()), lg(rows), lg(rays), lg(maxB)};
+}
+
+// The autotuner: times every (ray tile, warps per CTA) candidate on the batch itself
+// (captured graph, two timed passes after one warm-up each, minimum device time) and
+// keeps the fastest. Results do not depend on the launch shape (integer accumulation),
+// so any candidate is safe to pick.
+int tune_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode, double *best_ms)
+{
+    static const uint32_t kTiles[] = {16, 32, 64, 128, 256};
+    static const uint32_t kWarps[] = {2, 4, 8};
+    const uint32_t rt0 = ctx->ray_tile, w0 = ctx->warps_per_cta;
+    double best = 1e300;
+    uint32_t brt = rt0, bw = w0;
+    PassResult res;
+    for (uint32_t rt : kTiles)
+        for (uint32_t w : kWarps) {
+            ctx->ray_tile = rt;
+            ctx->warps_per_cta = w;
+            double m = 1e300;
+            for (int k = 0; k < 3; k++) {
+                const int e = run_pass_checked(ctx, ctx->main, ds, mode, true, nullptr, res, ctx->use_graphs);
+                if (e) {
+                    ctx->ray_tile = rt0;
+                    ctx->warps_per_cta = w0;
+                    return e;
+                }
+                if (k) m = std::min(m, ctx->main.last_ms);
+            }
+            if (m < best) {
+                best = m;
+                brt = rt;
+                bw = w;
+            }
+        }
+    ctx->ray_tile = brt;
+    ctx->warps_per_cta = bw;
+    ctx->tune_cache[tune_class(ds, mode)] = {brt, bw};
+    if (best_ms) *best_ms = best;
+    return CPD_OK;
+}
+
+// Builds the pass inputs of a batch (host copies kept alive by the caller's vectors).
+void batch_inputs(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items, uint32_t n,
+                  std::vector<DevDesign> &devs, std::vector<std::vector<double>> &lams, std::vector<RayTablePtr> &rts,
+                  std::vector<PassDesign> &ds)
+{
+    devs.resize(n);
+    lams.resize(n);
+    rts.resize(n);
+    ds.resize(n);
+    for (uint32_t i = 0; i < n; i++) {
+        design_to_dev(designs[i], devs[i]);
+        lams[i].resize(items[i].max_n);
+        seed_points(items[i].seed, 0, items[i].max_n, lams[i].data());
+        rts[i] = ray_table_cached(ctx, items[i].seed, items[i].max_eval);
+        ds[i] = PassDesign{&devs[i], items[i].max_n, items[i].max_eval, lams[i].data(), rts[i].get()};
+    }
 }
 
 }  // namespace
@@ -777,22 +856,53 @@ int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd
     for (uint32_t i = 0; i < n; i++)
         if (!valid_design(&designs[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
     CPD_SYNC_ENTRY(ctx);
-    std::vector<DevDesign> devs(n);
-    std::vector<std::vector<double>> lams(n);
-    std::vector<RayTablePtr> rts(n);
-    std::vector<PassDesign> ds(n);
-    for (uint32_t i = 0; i < n; i++) {
-        design_to_dev(designs[i], devs[i]);
-        lams[i].resize(items[i].max_n);
-        seed_points(items[i].seed, 0, items[i].max_n, lams[i].data());
-        rts[i] = ray_table_cached(ctx, items[i].seed, items[i].max_eval);
-        ds[i] = PassDesign{&devs[i], items[i].max_n, items[i].max_eval, lams[i].data(), rts[i].get()};
+    std::vector<DevDesign> devs;
+    std::vector<std::vector<double>> lams;
+    std::vector<RayTablePtr> rts;
+    std::vector<PassDesign> ds;
+    batch_inputs(ctx, designs, items, n, devs, lams, rts, ds);
+    if (ctx->autotune && !ctx->profiling) {
+        auto it = ctx->tune_cache.find(tune_class(ds, trace_mode));
+        if (it != ctx->tune_cache.end()) {
+            ctx->ray_tile = it->second.first;
+            ctx->warps_per_cta = it->second.second;
+        } else {
+            const int te = tune_pass(ctx, ds, trace_mode, nullptr);
+            if (te) return te;
+        }
     }
     PassResult res;
     int e = run_pass_checked(ctx, ctx->main, ds, trace_mode, true, nullptr, res, ctx->use_graphs);
     if (e) return e;
     for (uint32_t i = 0; i < n; i++)
         fill_fitness(designs[i], res.outs[i], (uint64_t)items[i].max_n * items[i].max_eval, outs[i], true);
+    return CPD_OK;
+}
+
+int cpd_autotune_batch(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items, uint32_t n,
+                       uint32_t trace_mode, uint32_t *ray_tile, uint32_t *warps_per_cta, double *best_ms)
+{
+    if (!ctx || !designs || !items || n == 0 || trace_mode > CPD_TRACE_FP64) return CPD_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < n; i++)
+        if (!valid_design(&designs[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
+    CPD_SYNC_ENTRY(ctx);
+    std::vector<DevDesign> devs;
+    std::vector<std::vector<double>> lams;
+    std::vector<RayTablePtr> rts;
+    std::vector<PassDesign> ds;
+    batch_inputs(ctx, designs, items, n, devs, lams, rts, ds);
+    const int e = tune_pass(ctx, ds, trace_mode, best_ms);
+    if (e) return e;
+    if (ray_tile) *ray_tile = ctx->ray_tile;
+    if (warps_per_cta) *warps_per_cta = ctx->warps_per_cta;
+    return CPD_OK;
+}
+
+int cpd_set_autotune(cpd_context *ctx, int on)
+{
+    if (!ctx) return CPD_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->autotune = on != 0;
     return CPD_OK;
 }
 

@@ -77,3 +77,15 @@ def test_survival_keeps_the_best():
     info = np.arange(10, dtype=float)
     keep = gen.survive(pop, info, 3)
     assert np.array_equal(keep.height, pop.height[[9, 8, 7]])
+
+
+def test_near_critical_designs_sit_within_two_degrees_of_tir():
+    from compound_prism_designer import precision as P
+
+    pop = P.study_population(99, n=4, B=128)
+    for spec, near, margin in pop[:2]:
+        assert near and 0.0 < margin <= 2.0
+        # the margin is the smallest over three wavelengths: the middle one leaves too
+        assert P.exit_margin_deg(spec, spec.beam.y_mean, 0.66) >= margin
+    for spec, near, margin in pop[2:]:
+        assert not near

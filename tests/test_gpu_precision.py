@@ -1,0 +1,96 @@
+"""Precision study on a small population: FP32-only and hybrid traces against the
+all-FP64 trace, and the FP64 trace against the CPU oracle, on near-critical designs
+(exit-face incidence within 2 degrees of total internal reflection) and ordinary ones.
+
+Bounds (the benchmark spec): the hybrid trace must agree with FP64 exactly on hit
+bins, within 1e-6 absolute on p(d|lambda) and within 1e-4 relative on MI. The
+FP64 trace must agree with the oracle within the 2^-32 fixed-point quantum on p and
+1e-8 relative on MI. FP32-only has no bound; its errors are the study's output and
+are only checked to be finite.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import compound_prism_designer as cpd
+from compound_prism_designer import precision as P
+from compound_prism_designer import synth
+
+pytestmark = pytest.mark.gpu
+NTHREADS = max(1, min(16, os.cpu_count() or 1))
+
+
+@pytest.fixture(scope="module")
+def population():
+    return P.study_population(314, n=8, B=128)
+
+
+def test_hybrid_meets_the_bounds_near_and_far_from_tir(population):
+    rng = np.random.default_rng(1)
+    lam_u = P.synth_points(0.5, 512)
+    ray_u = P.synth_points(0.5, 1024, first=1)
+    pl, pr = rng.uniform(size=16384), rng.uniform(1e-9, 1 - 1e-9, size=16384)
+    for spec, near, margin in population:
+        if near:
+            assert 0.0 < margin <= 2.0
+        r = P.evaluate(spec, lam_u, ray_u, pl, pr)
+        h = r["hybrid"]
+        assert h["hit_index_mismatches"] == 0, (near, margin, h)
+        assert h["p_max_abs_err"] <= 1e-6, (near, margin, h)
+        assert h["mi_rel_err"] <= 1e-4, (near, margin, h)
+        f = r["fp32"]
+        assert np.isfinite(f["mi_rel_err"]) and np.isfinite(f["p_max_abs_err"])
+
+
+def test_fp64_trace_equals_oracle_on_near_critical_designs(population):
+    lam_u = O.qrng_points(0.5, 256)
+    ray_u = O.qrng_points(0.5, 1024)
+    for spec, near, margin in population[:4]:
+        assert near
+        d = synth.spec_dict(spec)
+        f, p = spec.gpu_fitness_points(lam_u, ray_u, mode=cpd.TRACE_FP64, want_p=True)
+        po, st = O.fitness_points(d, lam_u, ray_u, nthreads=NTHREADS)
+        assert np.abs(p - po).max() <= 2.0 ** -32, margin
+        assert abs(f.info - st["info"]) <= 1e-8 * abs(st["info"]) + 1e-9, margin
+        assert f.hits == st["hits"]
+
+
+def test_summary_counts_classes(population):
+    rows = []
+    lam_u = P.synth_points(0.5, 64)
+    ray_u = P.synth_points(0.5, 256, first=1)
+    for i, (spec, near, margin) in enumerate(population):
+        r = P.evaluate(spec, lam_u, ray_u, lam_u[:16], ray_u[:16])
+        r.update(design=i, near_critical=near, margin_deg=margin)
+        rows.append(r)
+    s = P.summarize(rows)
+    assert s["near_critical"]["designs"] == 4 and s["ordinary"]["designs"] == 4
+    assert s["near_critical"]["hybrid"]["designs_over_1e-4_mi"] == 0
+
+
+def test_far_reference_ray_design_on_the_gpu():
+    """The design whose reference rays land ~1.9 m from the detector: the hybrid trace
+    equals the oracle on the rows that once went wrong and stays within the bounds of
+    the FP64 trace over all 8192 x 2048 points."""
+    import json
+
+    from conftest import GOLDEN
+
+    case = json.load(open(os.path.join(GOLDEN, "regression_designs.json")))["far_reference_detector"]
+    d = case["design"]
+    spec = synth.spectrometer_from_dict(d)
+    pts = case["points"]
+    lam_all = P.synth_points(pts["lam_seed"], pts["wavelengths"])
+    ray_u = P.synth_points(pts["ray_seed"], pts["rays"], first=pts["ray_first"])
+    lam_bad = lam_all[case["bad_rows"]]
+    f, p = spec.gpu_fitness_points(lam_bad, ray_u, mode=cpd.TRACE_HYBRID, want_p=True)
+    po, st = O.fitness_points(d, lam_bad, ray_u, nthreads=NTHREADS)
+    assert np.abs(p - po).max() <= 1e-6
+    assert f.hits == st["hits"]
+    f64, p64 = spec.gpu_fitness_points(lam_all, ray_u, mode=cpd.TRACE_FP64, want_p=True)
+    fh, ph = spec.gpu_fitness_points(lam_all, ray_u, mode=cpd.TRACE_HYBRID, want_p=True)
+    assert np.abs(ph - p64).max() <= 1e-6
+    assert abs(fh.info - f64.info) <= 1e-4 * abs(f64.info)
+    assert fh.hits == f64.hits
