@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(128) trace_pairs_kernel(const DevDesign *__res
                 // the ray is its own reference and it has no usable exit/detector geometry
                 exact = mode == CPD_TRACE_HYBRID;
             } else if (P.core_lo == 0 && P.core_hi == 1) {
-                const Guards g = mode == CPD_TRACE_FP32 ? Guards{0.f, 0.f, 0.f, 0.f} : default_guards();
+                const Guards g = mode == CPD_TRACE_FP32 ? no_guards() : default_guards();
                 float zh, zl;
                 split_f32(z, zh, zl);
                 uint32_t b = 0;

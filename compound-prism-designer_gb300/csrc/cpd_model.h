@@ -438,17 +438,20 @@ CPD_HD int trace_lam(const DevDesign &D, const ExactLam &E, double y, uint32_t &
 // upper bounds on the FP32 error of each margin measured over random designs,
 // times a safety factor ("guard bands").
 struct Guards {
-    float pos;     // mm, detector coordinate vs 0, L and every bin edge
-    float cosine;  // exit-face cr^2, AR threshold 0.5, detector min_ci
-    float dist;    // mm, exit-face root sign
-    float rel;     // relative: discriminant, radial bound
+    float pos;      // mm, detector coordinate vs 0, L and every bin edge
+    float cosine;   // exit-face cr^2, AR threshold 0.5, detector min_ci
+    float dist;     // mm, exit-face root sign
+    float rel;      // relative: discriminant, radial bound
+    float pos_rel;  // detector coordinate, relative to the terms it is summed from
 };
 // Measured over 40 random designs x 131k rays (host emulation of this code against
 // the exact trace): no wrong decision at 0.1x these widths, the first at 0.03x.
-CPD_HD Guards default_guards() { return Guards{1.0e-4f, 1.0e-5f, 1.0e-4f, 1.0e-5f}; }
-
-// Relative part of the detector-position guard (2^-20, 16 FP32 ulps of the largest term).
-constexpr float kPosRel = 9.5367431640625e-07f;
+// pos_rel (2^-20, 16 FP32 ulps of the largest term) covers designs whose reference
+// ray lands far (metres) from the detector, where the absolute 1e-4 mm is below one
+// ulp of the summed terms.
+CPD_HD Guards default_guards() { return Guards{1.0e-4f, 1.0e-5f, 1.0e-4f, 1.0e-5f, 9.5367431640625e-07f}; }
+// The FP32-only study mode: no guard band, nothing flagged.
+CPD_HD Guards no_guards() { return Guards{0.f, 0.f, 0.f, 0.f, 0.f}; }
 
 // Relative guard of the y-interval ends: both sides are f64, so a few ulps suffice.
 constexpr double kYGuardRel = 1e-11;
@@ -801,8 +804,8 @@ CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, flo
     const float dpos = tu + (tt + dgu);
     const float pos = P.pos + dpos;
     // The position is the one unbounded quantity (a reference ray can land metres from
-    // the detector): its guard grows with the magnitudes it was summed from, 16 FP32 ulps.
-    const float gp = fmaf(kPosRel, fabs_f(P.pos) + fabs_f(tu) + fabs_f(tt) + fabs_f(dgu), g.pos);
+    // the detector): its guard grows with the magnitudes it was summed from.
+    const float gp = fmaf(g.pos_rel, fabs_f(P.pos) + fabs_f(tu) + fabs_f(tt) + fabs_f(dgu), g.pos);
     if (pos < -gp || pos > D.L + gp) return RAY_LOST;
     flag |= pos < gp || pos > D.L - gp;
     const float xx = pos - D.c0;

@@ -332,7 +332,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     a.ray_tile = ctx->ray_tile;
     a.mode = mode;
     if (mode == CPD_TRACE_FP32) {
-        a.guards = Guards{0.f, 0.f, 0.f, 0.f};
+        a.guards = no_guards();
         a.yguard_rel = 0.0;
     } else {
         a.guards = default_guards();

@@ -177,7 +177,7 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     a.ray_tile = ray_tile;
     a.mode = trace_mode;
     if (trace_mode == CPD_TRACE_FP32) {
-        a.guards = Guards{0.f, 0.f, 0.f, 0.f};
+        a.guards = no_guards();
         a.yguard_rel = 0.0;
     } else {
         a.guards = default_guards();
