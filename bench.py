@@ -315,6 +315,7 @@ def main():
     import compound_prism_designer as cpd
 
     ctx = cpd.Context(dist.local)
+    ctx.set_autotune(True)  # the first warm-up call tunes the launch shape of this class
     spec, d = plain_design()
     flush, l2_note = l2_flusher()
     seeds = [0.5]
@@ -330,6 +331,7 @@ def main():
     for _ in range(args.warmup):
         step()
         flush()
+    plain_shape = ctx.launch_shape()
     clocks = ClockSampler(dist.local)
     dist.barrier()
     clocks.start()
@@ -406,7 +408,9 @@ def main():
             "metric": METRIC, "value": value, "unit": "designs/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": plain_config(l2_note),
+            "config": dict(plain_config(l2_note), launch_shape={"ray_tile": plain_shape[0],
+                                                                "warps_per_cta": plain_shape[1],
+                                                                "picked_by": "autotuner (first warm-up call)"}),
             "e2e": {"value": e2e, "unit": "designs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * wall_s / args.steps},
             "gpu_launches": launches_total, "clocks": clk, "wall_s": t_total,

@@ -665,17 +665,27 @@ CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double
 #endif
         return b >= 0 ? b : (int64_t)(0x8000000000000000ull - (uint64_t)b);
     };
-    auto ycount = [&](double thr, bool) -> uint32_t {
-        const double zt = (D.bym - thr) / D.bw;
-        if (zt != zt) return 0u;
-        const int64_t key = zkey(zt);
-        uint32_t lo = 0, hi = R;
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (zkey(zs[mid]) < key) lo = mid + 1;
-            else hi = mid;
+    // The four counts of a wavelength, searched in lockstep: the table is read by four
+    // independent chains of dependent loads instead of one chain four times as long.
+    auto ycount4 = [&](const double thr[4], uint32_t out[4]) {
+        int64_t key[4];
+        uint32_t lo[4], hi[4];
+        for (int i = 0; i < 4; i++) {
+            const double zt = (D.bym - thr[i]) / D.bw;
+            key[i] = zkey(zt);
+            lo[i] = 0;
+            hi[i] = zt != zt ? 0u : R;
         }
-        return lo;
+        while (lo[0] < hi[0] || lo[1] < hi[1] || lo[2] < hi[2] || lo[3] < hi[3]) {
+            for (int i = 0; i < 4; i++) {
+                if (lo[i] < hi[i]) {
+                    const uint32_t mid = (lo[i] + hi[i]) >> 1;
+                    if (zkey(zs[mid]) < key[i]) lo[i] = mid + 1;
+                    else hi[i] = mid;
+                }
+            }
+        }
+        for (int i = 0; i < 4; i++) out[i] = lo[i];
     };
     if (all_band) {
         P.band_lo = P.core_lo = P.core_hi = 0;
@@ -692,17 +702,17 @@ CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double
             P.band_lo = P.core_lo = 0;
             P.core_hi = P.band_hi = R;
         }
-    } else if (D.bw > 0.0) {
-        // j increasing <=> y decreasing: [yhi+g .. yhi-g] band first, core, [ylo+g .. ylo-g] band
-        P.band_lo = ycount(yhi + ghi, true);
-        P.core_lo = ycount(yhi - ghi, true);
-        P.core_hi = ycount(ylo + glo, false);
-        P.band_hi = ycount(ylo - glo, false);
     } else {
-        P.band_lo = ycount(ylo - glo, false);
-        P.core_lo = ycount(ylo + glo, false);
-        P.core_hi = ycount(yhi - ghi, true);
-        P.band_hi = ycount(yhi + ghi, true);
+        // bw > 0: j increasing <=> y decreasing: [yhi+g .. yhi-g] band first, core,
+        // [ylo+g .. ylo-g] band; bw < 0 the other way round
+        const double thr[4] = {D.bw > 0.0 ? yhi + ghi : ylo - glo, D.bw > 0.0 ? yhi - ghi : ylo + glo,
+                               D.bw > 0.0 ? ylo + glo : yhi - ghi, D.bw > 0.0 ? ylo - glo : yhi + ghi};
+        uint32_t c[4];
+        ycount4(thr, c);
+        P.band_lo = c[0];
+        P.core_lo = c[1];
+        P.core_hi = c[2];
+        P.band_hi = c[3];
     }
     if (P.core_hi < P.core_lo) P.core_hi = P.core_lo;
     if (P.band_hi < P.core_hi) P.band_hi = P.core_hi;

@@ -475,7 +475,7 @@ std::array<uint64_t, 5> tune_class(const std::vector<PassDesign> &ds, uint32_t m
 // so any candidate is safe to pick.
 int tune_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode, double *best_ms)
 {
-    static const uint32_t kTiles[] = {16, 32, 64, 128, 256};
+    static const uint32_t kTiles[] = {4, 8, 16, 32, 64, 128, 256};
     static const uint32_t kWarps[] = {2, 4, 8};
     const uint32_t rt0 = ctx->ray_tile, w0 = ctx->warps_per_cta;
     double best = 1e300;
@@ -830,7 +830,8 @@ int cpd_fitness_gpu(cpd_context *ctx, const cpd_design *d, const double *seeds, 
     if (max_n == 0 || max_eval == 0 || max_eval > CPD_MAX_RAYS) return CPD_INVALID_ARGUMENT;
     if ((uint64_t)max_n * nseeds > CPD_MAX_WAVELENGTHS) return CPD_INVALID_ARGUMENT;
     CPD_SYNC_ENTRY(ctx);
-    if (nwarp >= 1 && nwarp <= 8) ctx->warps_per_cta = nwarp;
+    const bool tune = ctx->autotune && !ctx->profiling;
+    if (!tune && nwarp >= 1 && nwarp <= 8) ctx->warps_per_cta = nwarp;
     DevDesign D;
     design_to_dev(*d, D);
     std::vector<double> lam(max_n);
@@ -840,6 +841,17 @@ int cpd_fitness_gpu(cpd_context *ctx, const cpd_design *d, const double *seeds, 
         seed_points(seeds[s], 0, max_n, lam.data());
         RayTablePtr rt = ray_table_cached(ctx, seeds[s], max_eval);
         std::vector<PassDesign> ds{PassDesign{&D, max_n, max_eval, lam.data(), rt.get()}};
+        if (tune && s == 0) {
+            // the autotuner replaces the reference's nwarp hint
+            auto it = ctx->tune_cache.find(tune_class(ds, CPD_TRACE_HYBRID));
+            if (it != ctx->tune_cache.end()) {
+                ctx->ray_tile = it->second.first;
+                ctx->warps_per_cta = it->second.second;
+            } else {
+                const int te = tune_pass(ctx, ds, CPD_TRACE_HYBRID, nullptr);
+                if (te) return te;
+            }
+        }
         int e = run_pass_checked(ctx, ctx->main, ds, CPD_TRACE_HYBRID, s == 0, nullptr, res, ctx->use_graphs);
         if (e) return e;
         rays += (uint64_t)max_n * max_eval;

@@ -238,15 +238,16 @@ int cpd_get_launch_shape(cpd_context *ctx, uint32_t *ray_tile, uint32_t *warps_p
 
 /* The project's launch-shape autotuner (no reference counterpart; the reference takes
  * a fixed nwarp hint, src/pylib.rs:1088). Times the batch with every ray tile in
- * {16, 32, 64, 128, 256} and warps per CTA in {2, 4, 8} (captured graph, minimum of two
+ * {4, 8, 16, 32, 64, 128, 256} and warps per CTA in {2, 4, 8} (captured graph, minimum of two
  * timed passes each), sets the fastest on the context and remembers it for the batch's
  * class: trace mode and the binary orders of magnitude of its design count, wavelength
  * rows, rays and widest detector. Results do not depend on the shape. */
 int cpd_autotune_batch(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items,
                        uint32_t n, uint32_t trace_mode, uint32_t *ray_tile, uint32_t *warps_per_cta,
                        double *best_ms);
-/* When on, cpd_fitness_gpu_batch uses the remembered shape of the batch's class, and
- * runs the autotuner first for a class it has not seen. Off by default. */
+/* When on, cpd_fitness_gpu_batch and cpd_fitness_gpu use the remembered shape of the
+ * pass's class, and run the autotuner first for a class they have not seen
+ * (cpd_fitness_gpu then ignores its nwarp hint). Off by default. */
 int cpd_set_autotune(cpd_context *ctx, int on);
 
 /* Device time of the last GPU call's kernels (CUDA events on the context stream), ms,
