@@ -385,7 +385,12 @@ def main():
                 bt.append(time.perf_counter() - t0)
                 bdev.append(ctx.last_timing()[0])
             nb = len(pop)
+            ctx.set_profiling(True)
+            cpd.fitness_batch(pop, seeds=0.5, max_n=Ws, max_eval=R_PLAIN, context=ctx)
+            bk = ctx.last_kernel_times()
+            ctx.set_profiling(False)
             extras["forms"] = {"batched": {
+                "kernel_ms": bk,
                 "workload": f"{nb} designs, G in 2..6, B in 16..128, W in 512..4096, R={R_PLAIN}",
                 "designs_per_s_device": nb / (min(bdev) / 1e3), "designs_per_s_e2e": nb / min(bt),
                 "ms_device": min(bdev), "ms_e2e": 1e3 * min(bt), "rays": int(sum(int(w) for w in Ws) * R_PLAIN),

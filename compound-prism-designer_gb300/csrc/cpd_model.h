@@ -137,6 +137,7 @@ struct ExactLam {
     double ci[CPD_MAX_GLASS];                     // dot(direction entering face k, N_k)
     double cr[CPD_MAX_GLASS];                     // refraction cosine at face k
     double n[CPD_MAX_GLASS];                      // index of glass k
+    double ts, tp;                                // s/p transmittance after the last flat face
 };
 
 // ----------------------------------------------------------------- exact f64 ops
@@ -191,6 +192,39 @@ CPD_HD double fma_(double a, double b, double c)
 #endif
 }
 CPD_HD double sqr(double a) { return mul(a, a); }
+
+// f64 reciprocal and square root to ~2^-44 relative, for quantities that only seed the
+// FP32 fast path or sit inside a guard band (never for a value the exact trace
+// reproduces): an FP32 hardware estimate refined by one Newton-Raphson step in f64
+// (y' = y + y(1 - xy); g' = g + (x - g^2) y/2 with y ~ 1/sqrt x). Outside the FP32
+// range they fall back to the IEEE operations. On the host both are the IEEE ones.
+CPD_HD double rcp_approx(double a)
+{
+#if defined(__CUDA_ARCH__)
+    const double m = fabs(a);
+    if (!(m > 1e-30 && m < 1e30)) return __ddiv_rn(1.0, a);
+    float s;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"((float)a));
+    const double y = (double)s;
+    return fma(y, fma(-a, y, 1.0), y);
+#else
+    return 1.0 / a;
+#endif
+}
+CPD_HD double sqrt_approx(double a)
+{
+#if defined(__CUDA_ARCH__)
+    if (!(a > 1e-30 && a < 1e30)) return __dsqrt_rn(a);
+    float s;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"((float)a));
+    const double y = (double)s;
+    const double g = a * y;
+    return fma(0.5 * y, fma(-g, g, a), g);
+#else
+    return std::sqrt(a);
+#endif
+}
+
 CPD_HD double trunc_(double a)
 {
 #if defined(__CUDA_ARCH__)
@@ -234,7 +268,7 @@ CPD_HD double dot(double ax, double ay, double bx, double by) { return add(mul(a
 CPD_HD bool refract(Ray &r, double nx, double ny, double n1, double n2, bool ar)
 {
     double ci = -dot(r.dx, r.dy, nx, ny);
-    double rr = div(n1, n2);
+    double rr = n2 == 1.0 ? n1 : div(n1, n2);  // x / 1 == x in IEEE arithmetic: no division for air
     double cr_sq = sub(1.0, mul(sqr(rr), sub(1.0, sqr(ci))));
     if (cr_sq < 0.0) return false;
     double cr = sqrt_(cr_sq);
@@ -392,11 +426,12 @@ CPD_HD int trace(const DevDesign &D, double lambda, double y, uint32_t &bin, dou
 // the detector -- is still done with the reference's operations, so the result is
 // bit-identical to trace(). The wavelength's flat faces do not reflect totally (else
 // lambda_setup drops it).
-CPD_HD int trace_lam(const DevDesign &D, const ExactLam &E, double y, uint32_t &bin, double &t)
+template <int G>
+CPD_HD int trace_lam_g(const DevDesign &D, const ExactLam &E, double y, uint32_t &bin, double &t)
 {
     Ray r{0.0, y, 1.0, 0.0, 1.0, 1.0};
     double n1 = 1.0;
-    for (int k = 0; k < D.G; k++) {
+    _Pragma("unroll") for (int k = 0; k < G; k++) {
         const double nx = D.pnx[k], ny = D.pny[k];
         const double ci = E.ci[k];
         if (ci == 0.0) return kNoHit;
@@ -406,28 +441,28 @@ CPD_HD int trace_lam(const DevDesign &D, const ExactLam &E, double y, uint32_t &
         if (!(0.0 <= hy && hy <= D.height)) return kNoHit;
         r.ox = fma_(r.dx, d, r.ox);
         r.oy = hy;
-        // Ray::refract (ray.rs:309-367) with the wavelength's direction and cosines
-        const double n2 = E.n[k];
-        const double cir = -ci;
-        const double cr = E.cr[k];
-        if (D.ar && cir > 0.5) {
-            r.ts = mul(r.ts, 0.99);
-            r.tp = mul(r.tp, 0.99);
-        } else {
-            const double a = mul(n1, cir), b = mul(n2, cr);
-            const double rs = sqr(div(sub(a, b), add(a, b)));
-            const double c = mul(n1, cr), e = mul(n2, cir);
-            const double rp = sqr(div(sub(c, e), add(c, e)));
-            r.ts = mul(r.ts, sub(1.0, rs));
-            r.tp = mul(r.tp, sub(1.0, rp));
-        }
+        // Ray::refract (ray.rs:309-367) with the wavelength's direction and cosines; the
+        // transmittance products are the wavelength's too (E.ts, E.tp)
         r.dx = E.dx[k];
         r.dy = E.dy[k];
-        n1 = n2;
+        n1 = E.n[k];
     }
+    r.ts = E.ts;
+    r.tp = E.tp;
     const int e = exit_face(D, r, n1);
     if (e) return e;
     return detector(D, r, bin, t);
+}
+CPD_HD int trace_lam(const DevDesign &D, const ExactLam &E, double y, uint32_t &bin, double &t)
+{
+    switch (D.G) {
+    case 1: return trace_lam_g<1>(D, E, y, bin, t);
+    case 2: return trace_lam_g<2>(D, E, y, bin, t);
+    case 3: return trace_lam_g<3>(D, E, y, bin, t);
+    case 4: return trace_lam_g<4>(D, E, y, bin, t);
+    case 5: return trace_lam_g<5>(D, E, y, bin, t);
+    default: return trace_lam_g<6>(D, E, y, bin, t);
+    }
 }
 }  // namespace x
 
@@ -474,7 +509,7 @@ CPD_HDN inline bool reference_ray(const DevDesign &D, const double *zs, LamParam
 {
     const uint32_t lo = P.core_lo, n = P.core_hi - P.core_lo;
     const double vx = D.cbx - D.ccx, vy = D.cby - D.ccy;  // bound centre m minus sphere centre c
-    const double rc = D.crad, rho2 = D.cbr2;
+    const double rc = D.crad, rho2 = D.cbr2, irc = x::rcp_approx(rc);
     const double qx = D.dpx - D.cbx, qy = D.dpy - D.cby;  // detector position minus m
     const unsigned char at16[9] = {8, 4, 12, 2, 6, 10, 14, 1, 15};
     for (int c = 0; c < 9; c++) {
@@ -488,7 +523,7 @@ CPD_HDN inline bool reference_ray(const DevDesign &D, const double *zs, LamParam
         const double cq = (ex_ * ex_ + ey_ * ey_) - rc * rc;
         const double disc = ud * ud - cq;
         if (!(disc > 0.0)) continue;
-        const double sd = sqrt(disc);
+        const double sd = x::sqrt_approx(disc);
         const double d1 = -ud - sd, d2 = -ud + sd;
         double sigma, s;
         const double p1x = wx + dx * d1, p1y = wy + dy * d1;
@@ -504,18 +539,18 @@ CPD_HDN inline bool reference_ray(const DevDesign &D, const double *zs, LamParam
         }
         const double px = wx + dx * s, py = wy + dy * s;
         const double mb = (px * px + py * py) - rho2;
-        const double nx = -(vx + px) / rc, ny = -(vy + py) / rc;
+        const double nx = -(vx + px) * irc, ny = -(vy + py) * irc;
         const double ci = -(dx * nx + dy * ny);
         const double crsq = 1.0 - r * r * (1.0 - ci * ci);
         if (!(crsq > 1e-6)) continue;
-        const double cr = sqrt(crsq);
+        const double cr = x::sqrt_approx(crsq);
         const double kk = r * ci - cr;
         const double ox = r * dx + kk * nx, oy = r * dy + kk * ny;
         const double cid = -(ox * D.dnx + oy * D.dny);
         if (!(cid > 0.05)) continue;
         const double gx = px - qx, gy = py - qy;
         const double gn = gx * D.dnx + gy * D.dny, gu = gx * D.dux + gy * D.duy;
-        const double T = gn / cid;
+        const double T = gn * x::rcp_approx(cid);
         const double du = ox * D.dux + oy * D.duy;
         const double pos = gu + du * T;
         split_f32(z, P.zref_hi, P.zref_lo);
@@ -557,8 +592,9 @@ CPD_HDN inline bool reference_ray(const DevDesign &D, const double *zs, LamParam
 // and square root), so only the direction chain -- which the exact re-trace and every
 // per-wavelength decision reuse bit for bit -- is formed with the reference's exact
 // operations; the y interval is accurate to ~1e-14 and guarded at 1e-11.
-CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double *zs, uint32_t R,
-                                 LamParams &P, double yguard_rel = kYGuardRel, ExactLam *E = nullptr)
+template <int G>
+CPD_HDN inline bool lambda_setup_g(const DevDesign &D, double lambda, const double *zs, uint32_t R, LamParams &P,
+                                   double yguard_rel, ExactLam *E)
 {
     using namespace x;
     {
@@ -566,8 +602,12 @@ CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double
         uint32_t *w = reinterpret_cast<uint32_t *>(&P);
         for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
     }
-    double nk[CPD_MAX_GLASS];
-    for (int k = 0; k < D.G; k++) nk[k] = calc_n(D.glass[k], lambda);  // independent chains
+    double nk[CPD_MAX_GLASS], rr[CPD_MAX_GLASS];
+    _Pragma("unroll") for (int k = 0; k < G; k++) nk[k] = calc_n(D.glass[k], lambda);  // independent chains
+    // Ray::refract's n1/n2 of every face: independent IEEE divisions, issued ahead of the
+    // direction chain instead of on it
+    _Pragma("unroll") for (int k = 0; k < G; k++) rr[k] = div(k ? nk[k - 1] : 1.0, nk[k]);
+    double ets = 1.0, etp = 1.0;  // exact s/p transmittance products for the re-trace
     // direction/transmittance, exactly as the sequential trace computes them
     double dx = 1.0, dy = 0.0, ts = 1.0, tp = 1.0;
     // position affine in y: o(y) = (ax + bx*y, ay + by*y)
@@ -599,13 +639,13 @@ CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double
             }
         }
     };
-    for (int k = 0; k < D.G; k++) {
+    _Pragma("unroll") for (int k = 0; k < G; k++) {
         const double n2 = nk[k];
         const double nx = D.pnx[k], ny = D.pny[k];
         const double ci = dot(dx, dy, nx, ny);
         if (ci == 0.0) return false;
-        // dist(y) = ((P - o(y)).N)/ci = e0 + e1*y
-        const double inv = 1.0 / ci;
+        // dist(y) = ((P - o(y)).N)/ci = e0 + e1*y (guarded: an approximate reciprocal)
+        const double inv = rcp_approx(ci);
         const double e0 = ((D.ppx[k] - ax) * nx + (D.ppy[k] - ay) * ny) * inv;
         const double e1 = -(bx * nx + by * ny) * inv;
         const double sc = (e0 < 0 ? -e0 : e0) + 30.0 * (e1 < 0 ? -e1 : e1) + D.height;
@@ -621,13 +661,13 @@ CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double
         // every later face depend on it); the s/p transmittances feed only the FP32 fast
         // path, so they are formed in FP32 (1 - R without cancellation).
         const double ci_r = -ci;  // -dot(d, N) of Ray::refract: the same dot product
-        const double rr = div(n1, n2);
-        const double cr_sq = sub(1.0, mul(sqr(rr), sub(1.0, sqr(ci_r))));
+        const double rk = rr[k];
+        const double cr_sq = sub(1.0, mul(sqr(rk), sub(1.0, sqr(ci_r))));
         if (cr_sq < 0.0) return false;  // TIR: the same for every ray
         const double cr = sqrt_(cr_sq);
-        const double kq = sub(mul(rr, ci_r), cr);
-        const double vx = add(mul(dx, rr), mul(nx, kq));
-        const double vy = add(mul(dy, rr), mul(ny, kq));
+        const double kq = sub(mul(rk, ci_r), cr);
+        const double vx = add(mul(dx, rk), mul(nx, kq));
+        const double vy = add(mul(dy, rk), mul(ny, kq));
         if (D.ar && ci_r > 0.5) {
             ts *= 0.99;
             tp *= 0.99;
@@ -644,14 +684,31 @@ CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double
             E->ci[k] = ci;
             E->cr[k] = cr;
             E->n[k] = n2;
+            // the sequential trace's transmittance update at this face, same operations
+            if (D.ar && ci_r > 0.5) {
+                ets = mul(ets, 0.99);
+                etp = mul(etp, 0.99);
+            } else {
+                const double a = mul(n1, ci_r), b = mul(n2, cr);
+                const double rs = sqr(div(sub(a, b), add(a, b)));
+                const double c = mul(n1, cr), e = mul(n2, ci_r);
+                const double rp = sqr(div(sub(c, e), add(c, e)));
+                ets = mul(ets, sub(1.0, rs));
+                etp = mul(etp, sub(1.0, rp));
+            }
         }
         dx = vx;
         dy = vy;
         n1 = n2;
     }
+    if (E) {
+        E->ts = ets;
+        E->tp = etp;
+    }
     if (!ok) return false;
-    const double ylo = L1 > 0.0 ? -L0 / L1 : -INFINITY, glo = L1 > 0.0 ? Lg / L1 : 0.0;
-    const double yhi = U1 > 0.0 ? U0 / U1 : INFINITY, ghi = U1 > 0.0 ? Ug / U1 : 0.0;
+    const double iL = L1 > 0.0 ? rcp_approx(L1) : 0.0, iU = U1 > 0.0 ? rcp_approx(U1) : 0.0;
+    const double ylo = L1 > 0.0 ? -L0 * iL : -INFINITY, glo = Lg * iL;
+    const double yhi = U1 > 0.0 ? U0 * iU : INFINITY, ghi = Ug * iU;
     // Sorted-ray index ranges. y_j = bym - bw z_j is monotone in z, so the index of a
     // height threshold T is the number of z_j below (bym - T)/bw. The guard widths are
     // many orders above the f64 rounding of that inversion, so the count is taken on
@@ -670,8 +727,9 @@ CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double
     auto ycount4 = [&](const double thr[4], uint32_t out[4]) {
         int64_t key[4];
         uint32_t lo[4], hi[4];
+        const double ibw = rcp_approx(D.bw);
         for (int i = 0; i < 4; i++) {
-            const double zt = (D.bym - thr[i]) / D.bw;
+            const double zt = (D.bym - thr[i]) * ibw;
             key[i] = zkey(zt);
             lo[i] = 0;
             hi[i] = zt != zt ? 0u : R;
@@ -725,6 +783,22 @@ CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double
     P.tp = (float)tp;
     if (P.core_hi > P.core_lo && !reference_ray(D, zs, P, ax, ay, bx, by, dx, dy, n1)) P.all_exact = 1;
     return P.band_hi > P.band_lo;
+}
+
+// lambda_setup for a prism count known at compile time: the face loops unroll, so the
+// independent work of one face (positions, constraints, transmittances) is scheduled
+// into the latency of the next face's exact direction step.
+CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double *zs, uint32_t R, LamParams &P,
+                                 double yguard_rel = kYGuardRel, ExactLam *E = nullptr)
+{
+    switch (D.G) {
+    case 1: return lambda_setup_g<1>(D, lambda, zs, R, P, yguard_rel, E);
+    case 2: return lambda_setup_g<2>(D, lambda, zs, R, P, yguard_rel, E);
+    case 3: return lambda_setup_g<3>(D, lambda, zs, R, P, yguard_rel, E);
+    case 4: return lambda_setup_g<4>(D, lambda, zs, R, P, yguard_rel, E);
+    case 5: return lambda_setup_g<5>(D, lambda, zs, R, P, yguard_rel, E);
+    default: return lambda_setup_g<6>(D, lambda, zs, R, P, yguard_rel, E);
+    }
 }
 
 // ----------------------------------------------------------------- FP32 fast path
