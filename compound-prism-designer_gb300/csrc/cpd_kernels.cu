@@ -1,6 +1,6 @@
 // cpd_kernels.cu -- the GB300 kernels of the fitness path.
 //
-// A pass over a set of designs runs four kernels on one stream:
+// A pass over a set of designs runs five kernels on one stream:
 //   setup    one thread per (design, wavelength): exact f64 flat-face chain ->
 //            LamParams; guard-band rays of the y interval go to the re-trace queue
 //   trace    persistent warps over work items (design, 32-wavelength block, ray
@@ -10,9 +10,9 @@
 //            64-bit atomic per run; guard-band rays go to the queue
 //   retrace  exact f64 trace of every queued ray (bit-identical to the reference's
 //            f64 CPU trace)
-//   entropy  per (design, row tile): p = sum/R, p log2 p, per-bin sums of p and p^2,
-//            all in FP64 with fixed-point accumulation (order independent); the last
-//            tile of each design runs the fused finalize (MI, SEM convergence).
+//   entropy  one warp per (design, row tile): p = sum/R, p log2 p, per-bin sums of p
+//            and p^2 in float-float with fixed-point accumulation (order independent)
+//   finalize one warp per design: H(D), MI, SEM convergence.
 #include <cuda_runtime.h>
 
 #include "cpd_gpu.cuh"
@@ -156,139 +156,141 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 }
 
 constexpr int kEntropyThreads = 256;
+constexpr int kFinalizeThreads = 128;
+constexpr uint32_t kRowsPerStep = 2;  // entropy rows read ahead per lane (x 4 bins)
 
-// Fused per-design finalize, run by the block that finished the design's last tile.
-__device__ void finalize(const LaunchArgs &a, uint32_t d, const DesignJob &J)
+// Per-design finalize, one warp per design after the entropy kernel: H(D) from the
+// per-bin sums, MI, and the SEM stop of cuda_fitness (src/cuda_fitness.rs:392-422).
+__global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(const LaunchArgs a)
 {
-    __shared__ double red[kEntropyThreads];
-    __shared__ double red_sem[kEntropyThreads];
-    __shared__ int red_conv[kEntropyThreads];
-    const uint32_t tid = threadIdx.x;
-    const unsigned long long rows = __ldcg(&a.acc[d].rows) + J.W;
-    const double n = (double)rows;
-    const double e2 = 5e-3 * 5e-3;
-    double hdet = 0.0, msem = 0.0;
-    int conv = 1;
-    const double p_unit = kTScaleInv / (double)J.R;  // p per count unit
-    for (uint32_t b = tid; b < J.B; b += blockDim.x) {
-        const double s1 = (double)__ldcg(&a.S1[J.acc_off + b]) * p_unit;  // sum over rows of p
-        const double s2 = (double)__ldcg(&a.S2[J.acc_off + b]) * kPScaleInv;
-        const double pbar = s1 / n;
-        if (pbar > 0.0) hdet += pbar * log2(pbar);
-        // Welford M2 of the per-wavelength p(d|lambda) (welford.rs:26-57)
-        double m2 = s2 - s1 * s1 / n;
-        if (m2 < 0.0) m2 = 0.0;
-        const double thr = e2 * (n * (n - 1.0));
-        conv &= (m2 < thr) ? 1 : 0;
-        const double sem = n > 1.0 ? sqrt(m2 / (n - 1.0) / n) : INFINITY;
-        msem = fmax(msem, sem);
-    }
-    red[tid] = hdet;
-    red_sem[tid] = msem;
-    red_conv[tid] = conv;
-    __syncthreads();
-    for (uint32_t s = blockDim.x >> 1; s > 0; s >>= 1) {
-        if (tid < s) {
-            red[tid] += red[tid + s];
-            red_sem[tid] = fmax(red_sem[tid], red_sem[tid + s]);
-            red_conv[tid] &= red_conv[tid + s];
+    // A pass whose re-trace queue overflowed is re-run by the host: write nothing.
+    if (a.ctl->overflow || a.ctl->queue_count > a.qcap) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; d < a.njobs; d += nw) {
+        const DesignJob J = a.jobs[d];
+        const unsigned long long rows = a.acc[d].rows + J.W;
+        const double n = (double)rows;
+        const double e2 = 5e-3 * 5e-3;
+        const double p_unit = kTScaleInv / (double)J.R;  // p per count unit
+        double hdet = 0.0, msem = 0.0;
+        int conv = 1;
+        for (uint32_t b = lane; b < J.B; b += 32u) {
+            const double s1 = (double)a.S1[J.acc_off + b] * p_unit;  // sum over rows of p
+            const double s2 = (double)a.S2[J.acc_off + b] * kPScaleInv;
+            const double pbar = s1 / n;
+            if (pbar > 0.0) hdet += pbar * log2(pbar);
+            // Welford M2 of the per-wavelength p(d|lambda) (welford.rs:26-57)
+            double m2 = s2 - s1 * s1 / n;
+            if (m2 < 0.0) m2 = 0.0;
+            conv &= (m2 < e2 * (n * (n - 1.0))) ? 1 : 0;
+            const double sem = n > 1.0 ? sqrt(m2 / (n - 1.0) / n) : INFINITY;
+            msem = fmax(msem, sem);
         }
-        __syncthreads();
-    }
-    if (tid == 0) {
-        const double H = (double)__ldcg(&a.acc[d].H) * kHScaleInv;
-        const double h_cond = -H / n;
-        DesignOut o;
-        o.h_cond = h_cond;
-        o.h_det = red[0];
-        o.info = h_cond - red[0];
-        o.max_sem = red_sem[0];
-        o.hits = __ldcg(&a.acc[d].hits);
-        o.retraced = __ldcg(&a.acc[d].retraced);
-        o.rows = rows;
-        o.fast = __ldcg(&a.acc[d].fast);
-        o.converged = red_conv[0];
-        o.pad = 0;
-        a.out[d] = o;
-        a.acc[d].rows = rows;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            hdet += __shfl_xor_sync(0xffffffffu, hdet, o);
+            msem = fmax(msem, __shfl_xor_sync(0xffffffffu, msem, o));
+        }
+        conv = __all_sync(0xffffffffu, conv);
+        if (lane == 0) {
+            const double H = (double)a.acc[d].H * kHScaleInv;
+            const double h_cond = -H / n;
+            DesignOut o;
+            o.h_cond = h_cond;
+            o.h_det = hdet;
+            o.info = h_cond - hdet;
+            o.max_sem = msem;
+            o.hits = a.acc[d].hits;
+            o.retraced = a.acc[d].retraced;
+            o.rows = rows;
+            o.fast = a.acc[d].fast;
+            o.converged = conv;
+            o.pad = 0;
+            a.out[d] = o;
+            a.acc[d].rows = rows;
+        }
     }
 }
 
-// Thread -> (bin, row group) map of an entropy tile: for B <= 256 each thread owns one
-// bin and every (256/B)-th row of the tile; for wider detectors each thread owns the
-// bins tid, tid+256, ... of every row. Per-thread partial sums are therefore fixed by
-// B alone, whatever else shares the launch.
-__global__ void __launch_bounds__(kEntropyThreads) entropy_kernel(const LaunchArgs a)
+// One warp per entropy tile (tile_rows = 1024 / B rows of one design, so ~1024 cells).
+// Lane -> (bin, row phase): for B <= 32 the lanes split into 32/B row phases of one
+// bin each; for wider detectors a lane owns bins lane, lane+32, ... of every row (in
+// groups of four, 128 bins per sweep). Every partial sum is therefore fixed by B and the
+// tile alone, whatever else shares the launch, and is converted to fixed point before
+// it is added across lanes, tiles and designs. Rows are read kRowsPerStep at a time so
+// that up to 4 kRowsPerStep loads per lane are in flight; each nonzero cell is zeroed after it is read,
+// which leaves the histogram clear for the next pass.
+__global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const LaunchArgs a)
 {
-    extern __shared__ unsigned long long sm[];  // S1[B], S2[B] of this tile
-    __shared__ unsigned long long hsum;
-    __shared__ int last;
     __shared__ float tab[4 * ff::kLogTable];
-    const uint32_t tid = threadIdx.x;
     // A pass whose re-trace queue overflowed is re-run by the host: leave every
     // accumulator untouched.
     if (a.ctl->overflow || a.ctl->queue_count > a.qcap) return;
-    for (uint32_t i = tid; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
+    for (uint32_t i = threadIdx.x; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
     __syncthreads();
-    for (uint64_t tile = blockIdx.x; tile < a.total_tiles; tile += gridDim.x) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t tile = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < a.total_tiles; tile += nw) {
         const uint32_t d = find_job<F_TILE>(a.jobs, a.njobs, tile);
         const DesignJob J = a.jobs[d];
-        const uint32_t tl = (uint32_t)(tile - J.tile_off);
-        const uint32_t r0 = tl * J.tile_rows;
-        const uint32_t r1 = min(r0 + J.tile_rows, J.W);
         const uint32_t B = J.B;
-        for (uint32_t b = tid; b < 2 * B; b += blockDim.x) sm[b] = 0ull;
-        if (tid == 0) hsum = 0ull;
-        __syncthreads();
+        const uint32_t groups = B <= 32u ? 32u / B : 1u;
+        const uint32_t grp = B <= 32u ? lane / B : 0u;
+        const uint32_t bin0 = B <= 32u ? lane % B : lane;
+        const bool active = grp < groups;
+        const uint32_t r0 = (uint32_t)(tile - J.tile_off) * J.tile_rows;
+        const uint32_t r1 = min(r0 + J.tile_rows, J.W);
         const double p_unit = kTScaleInv / (double)J.R;
         const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
         unsigned long long *base = a.hist + J.hist_off;
-        const uint32_t groups = B <= (uint32_t)kEntropyThreads ? (uint32_t)kEntropyThreads / B : 1u;
-        const uint32_t grp = tid / (B <= (uint32_t)kEntropyThreads ? B : (uint32_t)kEntropyThreads);
-        const uint32_t bin0 = B <= (uint32_t)kEntropyThreads ? tid % B : tid;
         ff::F2 h{0.f, 0.f};
-        if (grp < groups) {
-            for (uint32_t b = bin0; b < B; b += kEntropyThreads) {
-                unsigned long long c1 = 0ull;
-                ff::F2 q2{0.f, 0.f};
-                for (uint32_t row = r0 + grp; row < r1; row += groups) {
-                    unsigned long long *cell = base + (uint64_t)row * B + b;
-                    const unsigned long long c = *cell;
-                    if (c) {
-                        *cell = 0ull;  // leaves the histogram zeroed for the next pass
-                        // p = c unit and p log2 p in float-float (FP32 pipe)
-                        const ff::F2 p = ff::mul(ff::from_u64(c), unit);
-                        const ff::F2 lp = ff::add(ff::log2_u64(c, tab), lu);
-                        h = ff::add(h, ff::mul(p, lp));
-                        q2 = ff::add(q2, ff::mul(p, p));
-                        c1 += c;
+        for (uint32_t bg = 0; bg < B; bg += 128u) {
+            unsigned long long c1[4] = {0ull, 0ull, 0ull, 0ull};
+            ff::F2 q2[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+            for (uint32_t row = r0 + grp; row < r1; row += kRowsPerStep * groups) {
+                unsigned long long c[kRowsPerStep][4];
+#pragma unroll
+                for (int rr = 0; rr < (int)kRowsPerStep; rr++) {
+                    const uint32_t rw = row + (uint32_t)rr * groups;
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
+                        c[rr][i] = (active && rw < r1 && b < B) ? base[(uint64_t)rw * B + b] : 0ull;
                     }
-                    if (a.p_out) a.p_out[(uint64_t)row * B + b] = (double)c * p_unit;
                 }
-                if (c1) {
-                    atomicAdd(&sm[b], c1);
-                    atomicAdd(&sm[B + b], __double2ull_rn(((double)q2.hi + (double)q2.lo) * kPScale));
+#pragma unroll
+                for (int rr = 0; rr < (int)kRowsPerStep; rr++) {
+                    const uint32_t rw = row + (uint32_t)rr * groups;
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
+                        const unsigned long long cv = c[rr][i];
+                        if (cv) {
+                            base[(uint64_t)rw * B + b] = 0ull;
+                            // p = c unit and p log2 p in float-float (FP32 pipe)
+                            const ff::F2 p = ff::mul(ff::from_u64(cv), unit);
+                            const ff::F2 lp = ff::add(ff::log2_u64(cv, tab), lu);
+                            h = ff::add(h, ff::mul(p, lp));
+                            q2[i] = ff::add(q2[i], ff::mul(p, p));
+                            c1[i] += cv;
+                        }
+                        if (a.p_out && active && rw < r1 && b < B) a.p_out[(uint64_t)rw * B + b] = (double)cv * p_unit;
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
+                if (c1[i]) {
+                    atomicAdd(&a.S1[J.acc_off + b], c1[i]);
+                    atomicAdd(&a.S2[J.acc_off + b],
+                              __double2ull_rn(((double)q2[i].hi + (double)q2[i].lo) * kPScale));
                 }
             }
         }
-        unsigned long long hl = __double2ull_rn(-((double)h.hi + (double)h.lo) * kHScale);
-        hl = warp_sum_u64(hl);
-        if ((tid & 31u) == 0 && hl) atomicAdd(&hsum, hl);
-        __syncthreads();
-        for (uint32_t b = tid; b < B; b += blockDim.x) {
-            if (sm[b]) atomicAdd(&a.S1[J.acc_off + b], sm[b]);
-            if (sm[B + b]) atomicAdd(&a.S2[J.acc_off + b], sm[B + b]);
-        }
-        if (tid == 0 && hsum) atomicAdd(&a.acc[d].H, hsum);
-        __threadfence();
-        __syncthreads();
-        if (tid == 0) last = (atomicAdd(&a.tiles_done[d], 1u) == J.ntiles - 1u) ? 1 : 0;
-        __syncthreads();
-        if (last) {
-            __threadfence();
-            finalize(a, d, J);
-        }
-        __syncthreads();
+        const unsigned long long hl = warp_sum_u64(__double2ull_rn(-((double)h.hi + (double)h.lo) * kHScale));
+        if (lane == 0 && hl) atomicAdd(&a.acc[d].H, hl);
     }
 }
 
@@ -398,12 +400,19 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     launches++;
     if (ev) cudaEventRecord(ev[3], stream);
     if (a.total_tiles) {
-        uint32_t maxB = 0;
-        // the entropy kernel sizes its shared per-bin sums for the widest detector
-        maxB = CPD_MAX_BINS;
-        uint64_t grid = (uint64_t)num_sms * 8;
-        if (grid > a.total_tiles) grid = a.total_tiles;
-        entropy_kernel<<<(unsigned)grid, kEntropyThreads, 2 * maxB * sizeof(unsigned long long), stream>>>(a);
+        // one warp per tile, as many blocks as are resident at once
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, entropy_kernel, kEntropyThreads, 0);
+        if (per_sm < 1) per_sm = 1;
+        const uint64_t wpb = (uint64_t)kEntropyThreads / 32u;
+        uint64_t grid = (a.total_tiles + wpb - 1) / wpb;
+        if (grid > (uint64_t)num_sms * per_sm) grid = (uint64_t)num_sms * per_sm;
+        entropy_kernel<<<(unsigned)grid, kEntropyThreads, 0, stream>>>(a);
+        launches++;
+    }
+    {
+        const uint32_t wpb = kFinalizeThreads / 32u;
+        finalize_kernel<<<(a.njobs + wpb - 1) / wpb, kFinalizeThreads, 0, stream>>>(a);
         launches++;
     }
     if (ev) cudaEventRecord(ev[4], stream);

@@ -808,7 +808,11 @@ CPD_HD float fabs_f(float a) { return a < 0.f ? -a : a; }
 CPD_HD float sqrt_fast(float a)
 {
 #if defined(__CUDA_ARCH__)
-    return __fsqrt_rn(a);
+    // the hardware approximation (a couple of ulps): every decision that uses it sits
+    // behind a guard band thousands of ulps wide
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
 #else
     return std::sqrt(a);
 #endif
