@@ -59,6 +59,9 @@ struct DesignOut {
     int32_t pad;
 };
 
+// Cells per entropy tile (one warp): a design's tile is max(1, kTileCells / B) rows.
+constexpr uint32_t kTileCells = 512;
+
 struct LaunchArgs {
     const DevDesign *designs;
     const DesignJob *jobs;

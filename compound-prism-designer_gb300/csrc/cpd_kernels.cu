@@ -157,7 +157,6 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 
 constexpr int kEntropyThreads = 256;
 constexpr int kFinalizeThreads = 128;
-constexpr uint32_t kRowsPerStep = 2;  // entropy rows read ahead per lane (x 4 bins)
 
 // Per-design finalize, one warp per design after the entropy kernel: H(D) from the
 // per-bin sums, MI, and the SEM stop of cuda_fitness (src/cuda_fitness.rs:392-422).
@@ -213,14 +212,78 @@ __global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(const Launch
     }
 }
 
-// One warp per entropy tile (tile_rows = 1024 / B rows of one design, so ~1024 cells).
-// Lane -> (bin, row phase): for B <= 32 the lanes split into 32/B row phases of one
-// bin each; for wider detectors a lane owns bins lane, lane+32, ... of every row (in
-// groups of four, 128 bins per sweep). Every partial sum is therefore fixed by B and the
-// tile alone, whatever else shares the launch, and is converted to fixed point before
-// it is added across lanes, tiles and designs. Rows are read kRowsPerStep at a time so
-// that up to 4 kRowsPerStep loads per lane are in flight; each nonzero cell is zeroed after it is read,
-// which leaves the histogram clear for the next pass.
+// Entropy sums of the rows [r0, r1) of one design by one warp. Lane -> (bin, row phase):
+// for B <= 32 the lanes split into 32/B row phases of one bin each; for wider detectors
+// a lane owns bins lane, lane+32, ... of every row, NB of them per sweep. Every partial
+// sum is therefore fixed by B and the tile alone, whatever else shares the launch, and
+// is converted to fixed point before it is added across lanes, tiles and designs. Each
+// step reads 8/NB rows x NB bins, so eight loads per lane are in flight; each nonzero
+// cell is zeroed after it is read, which leaves the histogram clear for the next pass.
+template <int NB>
+__device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJob &J, uint32_t r0, uint32_t r1,
+                                             uint32_t lane, const float *tab, ff::F2 &h)
+{
+    constexpr uint32_t RS = 8u / NB;
+    const uint32_t B = J.B;
+    const uint32_t groups = B <= 32u ? 32u / B : 1u;
+    const uint32_t grp = B <= 32u ? lane / B : 0u;
+    const uint32_t bin0 = B <= 32u ? lane % B : lane;
+    const bool active = grp < groups;
+    const double p_unit = kTScaleInv / (double)J.R;
+    const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
+    unsigned long long *base = a.hist + J.hist_off;
+    for (uint32_t bg = 0; bg < B; bg += 32u * NB) {
+        unsigned long long c1[NB];
+        ff::F2 q2[NB];
+#pragma unroll
+        for (int i = 0; i < NB; i++) {
+            c1[i] = 0ull;
+            q2[i] = ff::F2{0.f, 0.f};
+        }
+        for (uint32_t row = r0 + grp; row < r1; row += RS * groups) {
+            unsigned long long c[RS][NB];
+#pragma unroll
+            for (uint32_t rr = 0; rr < RS; rr++) {
+                const uint32_t rw = row + rr * groups;
+#pragma unroll
+                for (int i = 0; i < NB; i++) {
+                    const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
+                    c[rr][i] = (active && rw < r1 && b < B) ? base[(uint64_t)rw * B + b] : 0ull;
+                }
+            }
+#pragma unroll
+            for (uint32_t rr = 0; rr < RS; rr++) {
+                const uint32_t rw = row + rr * groups;
+#pragma unroll
+                for (int i = 0; i < NB; i++) {
+                    const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
+                    const unsigned long long cv = c[rr][i];
+                    if (cv) {
+                        base[(uint64_t)rw * B + b] = 0ull;
+                        // p = c unit and p log2 p in float-float (FP32 pipe)
+                        const ff::F2 p = ff::mul(ff::from_u64(cv), unit);
+                        const ff::F2 lp = ff::add(ff::log2_u64(cv, tab), lu);
+                        h = ff::add(h, ff::mul(p, lp));
+                        q2[i] = ff::add(q2[i], ff::mul(p, p));
+                        c1[i] += cv;
+                    }
+                    if (a.p_out && active && rw < r1 && b < B) a.p_out[(uint64_t)rw * B + b] = (double)cv * p_unit;
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < NB; i++) {
+            const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
+            if (c1[i]) {
+                atomicAdd(&a.S1[J.acc_off + b], c1[i]);
+                atomicAdd(&a.S2[J.acc_off + b], __double2ull_rn(((double)q2[i].hi + (double)q2[i].lo) * kPScale));
+            }
+        }
+    }
+}
+
+// One warp per entropy tile: kTileCells cells of one design (tile_rows = kTileCells / B
+// rows, at least one).
 __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const LaunchArgs a)
 {
     __shared__ float tab[4 * ff::kLogTable];
@@ -234,61 +297,13 @@ __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const Launc
     for (uint64_t tile = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < a.total_tiles; tile += nw) {
         const uint32_t d = find_job<F_TILE>(a.jobs, a.njobs, tile);
         const DesignJob J = a.jobs[d];
-        const uint32_t B = J.B;
-        const uint32_t groups = B <= 32u ? 32u / B : 1u;
-        const uint32_t grp = B <= 32u ? lane / B : 0u;
-        const uint32_t bin0 = B <= 32u ? lane % B : lane;
-        const bool active = grp < groups;
         const uint32_t r0 = (uint32_t)(tile - J.tile_off) * J.tile_rows;
         const uint32_t r1 = min(r0 + J.tile_rows, J.W);
-        const double p_unit = kTScaleInv / (double)J.R;
-        const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
-        unsigned long long *base = a.hist + J.hist_off;
+        const uint32_t nb = (J.B + 31u) / 32u;  // bins per lane
         ff::F2 h{0.f, 0.f};
-        for (uint32_t bg = 0; bg < B; bg += 128u) {
-            unsigned long long c1[4] = {0ull, 0ull, 0ull, 0ull};
-            ff::F2 q2[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-            for (uint32_t row = r0 + grp; row < r1; row += kRowsPerStep * groups) {
-                unsigned long long c[kRowsPerStep][4];
-#pragma unroll
-                for (int rr = 0; rr < (int)kRowsPerStep; rr++) {
-                    const uint32_t rw = row + (uint32_t)rr * groups;
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
-                        c[rr][i] = (active && rw < r1 && b < B) ? base[(uint64_t)rw * B + b] : 0ull;
-                    }
-                }
-#pragma unroll
-                for (int rr = 0; rr < (int)kRowsPerStep; rr++) {
-                    const uint32_t rw = row + (uint32_t)rr * groups;
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
-                        const unsigned long long cv = c[rr][i];
-                        if (cv) {
-                            base[(uint64_t)rw * B + b] = 0ull;
-                            // p = c unit and p log2 p in float-float (FP32 pipe)
-                            const ff::F2 p = ff::mul(ff::from_u64(cv), unit);
-                            const ff::F2 lp = ff::add(ff::log2_u64(cv, tab), lu);
-                            h = ff::add(h, ff::mul(p, lp));
-                            q2[i] = ff::add(q2[i], ff::mul(p, p));
-                            c1[i] += cv;
-                        }
-                        if (a.p_out && active && rw < r1 && b < B) a.p_out[(uint64_t)rw * B + b] = (double)cv * p_unit;
-                    }
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
-                if (c1[i]) {
-                    atomicAdd(&a.S1[J.acc_off + b], c1[i]);
-                    atomicAdd(&a.S2[J.acc_off + b],
-                              __double2ull_rn(((double)q2[i].hi + (double)q2[i].lo) * kPScale));
-                }
-            }
-        }
+        if (nb >= 3u) entropy_tile<4>(a, J, r0, r1, lane, tab, h);
+        else if (nb == 2u) entropy_tile<2>(a, J, r0, r1, lane, tab, h);
+        else entropy_tile<1>(a, J, r0, r1, lane, tab, h);
         const unsigned long long hl = warp_sum_u64(__double2ull_rn(-((double)h.hi + (double)h.lo) * kHScale));
         if (lane == 0 && hl) atomicAdd(&a.acc[d].H, hl);
     }

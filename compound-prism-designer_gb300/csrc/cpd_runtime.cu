@@ -201,7 +201,7 @@ struct PassResult {
     bool overflow = false;
 };
 
-uint32_t tile_rows_for(uint32_t B) { return std::max<uint32_t>(1u, 1024u / B); }
+uint32_t tile_rows_for(uint32_t B) { return std::max<uint32_t>(1u, kTileCells / B); }
 
 // Device bytes one design occupies in a pass (histogram, per-row tables, ray tables):
 // the admission unit of the server.

@@ -129,7 +129,7 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     J.Rz = Rz;
     J.B = D.B;
     J.nchunk = std::max<uint32_t>(1u, (Rz + ray_tile - 1) / ray_tile);
-    J.tile_rows = std::max<uint32_t>(1u, 1024u / J.B);
+    J.tile_rows = std::max<uint32_t>(1u, kTileCells / J.B);
     J.ntiles = (W + J.tile_rows - 1) / J.tile_rows;
     ff::split(kTScaleInv / (double)R, J.unit_hi, J.unit_lo);
     ff::split(-31.0 - std::log2((double)R), J.lu_hi, J.lu_lo);
