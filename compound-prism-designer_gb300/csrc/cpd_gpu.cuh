@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include "cpd_df.h"
 #include "cpd_ff.h"
 #include "cpd_model.h"
 
@@ -73,7 +74,7 @@ struct LaunchArgs {
     const double *z64;
     const float *z32;     // (hi, lo) f32 pairs of the sorted z table
     LamParams *lp;
-    ExactLam *lx;         // per row: exact flat-face data for the re-trace
+    LamDF *lx;            // per row: float-float data for the re-trace
     unsigned long long *hist;
     unsigned long long *S1;
     unsigned long long *S2;

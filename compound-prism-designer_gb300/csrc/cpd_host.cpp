@@ -145,6 +145,47 @@ void design_to_dev(const cpd_design &d, DevDesign &D)
     f.bw = (float)D.bw;
     f.ar = D.ar;
     f.B = D.B;
+    DFConst &c = D.dc;
+    auto sp = [](double v) {
+        ff::F2 r;
+        ff::split(v, r.hi, r.lo);
+        return r;
+    };
+    for (int k = 0; k < CPD_MAX_GLASS; k++) {
+        for (int i = 0; i < 6; i++) c.glass[k][i] = sp(D.glass[k][i]);
+        c.ppx[k] = sp(D.ppx[k]);
+        c.ppy[k] = sp(D.ppy[k]);
+        c.pnx[k] = sp(D.pnx[k]);
+        c.pny[k] = sp(D.pny[k]);
+    }
+    c.height = sp(D.height);
+    c.ccx = sp(D.ccx);
+    c.ccy = sp(D.ccy);
+    c.rc2 = sp(D.crad * D.crad);
+    c.irc = sp(1.0 / D.crad);
+    c.cbx = sp(D.cbx);
+    c.cby = sp(D.cby);
+    c.cbr2 = sp(D.cbr2);
+    c.vx = sp(D.cbx - D.ccx);
+    c.vy = sp(D.cby - D.ccy);
+    c.bin_size = sp(D.bin_size);
+    c.slope = sp(D.slope);
+    c.islope = sp(1.0 / D.slope);
+    c.intercept = sp(D.intercept);
+    c.min_ci = sp(D.min_ci);
+    c.L = sp(D.L);
+    c.dnx = sp(D.dnx);
+    c.dny = sp(D.dny);
+    c.dpx = sp(D.dpx);
+    c.dpy = sp(D.dpy);
+    c.dux = sp(D.dux);
+    c.duy = sp(D.duy);
+    c.qx = sp(D.dpx - D.cbx);
+    c.qy = sp(D.dpy - D.cby);
+    c.wmin = sp(D.wmin);
+    c.wspan = sp(D.wmax - D.wmin);
+    c.bw = sp(D.bw);
+    c.bym = sp(D.bym);
 }
 
 // Shaw's inverse normal CDF (erf.rs:27-73), host-side: the ray tables are built here

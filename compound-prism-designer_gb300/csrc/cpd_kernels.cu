@@ -1,20 +1,22 @@
 // cpd_kernels.cu -- the GB300 kernels of the fitness path.
 //
 // A pass over a set of designs runs five kernels on one stream:
-//   setup    one thread per (design, wavelength): exact f64 flat-face chain ->
-//            LamParams; guard-band rays of the y interval go to the re-trace queue
+//   setup    one thread per (design, wavelength): the flat-face chain in float-float
+//            (cpd_df.h) -> LamParams for the fast path and LamDF for the re-trace;
+//            guard-band rays of the y interval go to the re-trace queue
 //   trace    persistent warps over work items (design, 32-wavelength block, ray
 //            chunk); lane = wavelength; FP32 exit face + detector per ray; hits
 //            accumulate per lane as run-length fixed-point sums (rays are sorted by
 //            start height, so consecutive rays mostly share a bin) flushed with one
 //            64-bit atomic per run; guard-band rays go to the queue
-//   retrace  exact f64 trace of every queued ray (bit-identical to the reference's
-//            f64 CPU trace)
+//   retrace  every queued ray: float-float re-trace (exact f64 in the FP64 study mode,
+//            bit-identical to the reference's f64 CPU trace)
 //   entropy  one warp per (design, row tile): p = sum/R, p log2 p, per-bin sums of p
 //            and p^2 in float-float with fixed-point accumulation (order independent)
 //   finalize one warp per design: H(D), MI, SEM convergence.
 #include <cuda_runtime.h>
 
+#include "cpd_df.h"
 #include "cpd_gpu.cuh"
 
 namespace cpd {
@@ -57,9 +59,8 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     const DesignJob &J = a.jobs[d];
     const uint32_t k = (uint32_t)(row - J.row_off);
     const DevDesign &D = a.designs[d];
-    const double lambda = x::wavelength(D, a.lam_u[J.lam_off + k]);
     LamParams P;
-    lambda_setup(D, lambda, a.z64 + J.ray_off, J.Rz, P, a.yguard_rel, a.lx + row);
+    lambda_setup_df(D, a.lam_u[J.lam_off + k], a.z32 + 2 * J.ray_off, J.Rz, P, a.yguard_rel, a.lx + row);
     if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
         for (uint32_t j = P.band_lo; j < P.band_hi; j++) push_ray(a, d, k, j);
         P.core_lo = P.core_hi = 0;
@@ -128,6 +129,8 @@ __global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
     }
 }
 
+// The queued rays: in the FP64 study mode the exact f64 trace of the reference
+// (bit-identical to its CPU path); otherwise the float-float re-trace.
 __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
 {
     const unsigned long long qn = a.ctl->queue_count;
@@ -137,11 +140,22 @@ __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
         const QEntry e = a.queue[i];
         const DevDesign &D = a.designs[e.design];
         const DesignJob &J = a.jobs[e.design];
-        const double y = x::beam_y(D, a.z64[J.ray_off + e.j]);
         uint32_t bin = 0;
-        double t = 0.0;
-        if (x::trace_lam(D, a.lx[J.row_off + e.k], y, bin, t) == 0) {
-            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, (unsigned long long)t_fixed64(t));
+        unsigned long long tq = 0;
+        bool hit;
+        if (a.mode == CPD_TRACE_FP64) {
+            double t = 0.0;
+            hit = x::trace(D, x::wavelength(D, a.lam_u[J.lam_off + e.k]), x::beam_y(D, a.z64[J.ray_off + e.j]), bin,
+                           t) == 0;
+            tq = t_fixed64(t);
+        } else {
+            float t = 0.f;
+            const float *z = a.z32 + 2 * (J.ray_off + e.j);
+            hit = trace_df(D, a.lx[J.row_off + e.k], z[0], z[1], bin, t);
+            tq = t_fixed(t);
+        }
+        if (hit) {
+            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, tq);
             atomicAdd(&a.acc[e.design].hits, 1ull);
         }
         atomicAdd(&a.acc[e.design].retraced, 1ull);
@@ -160,46 +174,71 @@ constexpr int kFinalizeThreads = 128;
 
 // Per-design finalize, one warp per design after the entropy kernel: H(D) from the
 // per-bin sums, MI, and the SEM stop of cuda_fitness (src/cuda_fitness.rs:392-422).
+// f64 costs ~64 cycles per warp instruction here, so pbar log2 pbar is formed in
+// float-float on the FP32 pipe: pbar = S1 / (n R 2^31) and log2 pbar = log2 S1 -
+// log2(n R) - 31, both logs of integers (ff::log2_u64, absolute error < 1e-12). Only the
+// Welford M2 of each bin and the final SEM square root are f64.
 __global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(const LaunchArgs a)
 {
+    __shared__ float tab[4 * ff::kLogTable];
     // A pass whose re-trace queue overflowed is re-run by the host: write nothing.
     if (a.ctl->overflow || a.ctl->queue_count > a.qcap) return;
+    for (uint32_t i = threadIdx.x; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
+    __syncthreads();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; d < a.njobs; d += nw) {
         const DesignJob J = a.jobs[d];
         const unsigned long long rows = a.acc[d].rows + J.W;
         const double n = (double)rows;
-        const double e2 = 5e-3 * 5e-3;
+        const double inv_n = 1.0 / n;
         const double p_unit = kTScaleInv / (double)J.R;  // p per count unit
-        double hdet = 0.0, msem = 0.0;
+        const double thr = 5e-3 * 5e-3 * (n * (n - 1.0));
+        // 1 / (n R 2^31) and log2(n R) + 31 as float-float
+        const unsigned long long nR = rows * (unsigned long long)J.R;
+        float ih, il;
+        {
+            const double inr = p_unit * inv_n;
+            ih = (float)inr;
+            il = (float)(inr - (double)ih);
+        }
+        const ff::F2 inv_nr{ih, il};
+        const ff::F2 lnr = ff::add_f(ff::log2_u64(nR, tab), 31.f);
+        ff::F2 hdet{0.f, 0.f};
+        double m2max = 0.0;
         int conv = 1;
         for (uint32_t b = lane; b < J.B; b += 32u) {
-            const double s1 = (double)a.S1[J.acc_off + b] * p_unit;  // sum over rows of p
-            const double s2 = (double)a.S2[J.acc_off + b] * kPScaleInv;
-            const double pbar = s1 / n;
-            if (pbar > 0.0) hdet += pbar * log2(pbar);
+            const unsigned long long c1 = a.S1[J.acc_off + b];
+            if (c1) {
+                const ff::F2 pbar = ff::mul(ff::from_u64(c1), inv_nr);
+                const ff::F2 lg = ff::add(ff::log2_u64(c1, tab), ff::F2{-lnr.hi, -lnr.lo});
+                hdet = ff::add(hdet, ff::mul(pbar, lg));
+            }
             // Welford M2 of the per-wavelength p(d|lambda) (welford.rs:26-57)
-            double m2 = s2 - s1 * s1 / n;
+            const double s1 = (double)c1 * p_unit;  // sum over rows of p
+            const double s2 = (double)a.S2[J.acc_off + b] * kPScaleInv;
+            double m2 = s2 - s1 * s1 * inv_n;
             if (m2 < 0.0) m2 = 0.0;
-            conv &= (m2 < e2 * (n * (n - 1.0))) ? 1 : 0;
-            const double sem = n > 1.0 ? sqrt(m2 / (n - 1.0) / n) : INFINITY;
-            msem = fmax(msem, sem);
+            conv &= (m2 < thr) ? 1 : 0;
+            m2max = fmax(m2max, m2);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            hdet += __shfl_xor_sync(0xffffffffu, hdet, o);
-            msem = fmax(msem, __shfl_xor_sync(0xffffffffu, msem, o));
+            const ff::F2 other{__shfl_xor_sync(0xffffffffu, hdet.hi, o), __shfl_xor_sync(0xffffffffu, hdet.lo, o)};
+            // the same pairs are added in the same order on every lane: a fixed tree
+            hdet = (lane & (uint32_t)o) ? ff::add(other, hdet) : ff::add(hdet, other);
+            m2max = fmax(m2max, __shfl_xor_sync(0xffffffffu, m2max, o));
         }
         conv = __all_sync(0xffffffffu, conv);
         if (lane == 0) {
             const double H = (double)a.acc[d].H * kHScaleInv;
-            const double h_cond = -H / n;
+            const double h_cond = -H * inv_n;
+            const double h_det = (double)hdet.hi + (double)hdet.lo;
             DesignOut o;
             o.h_cond = h_cond;
-            o.h_det = hdet;
-            o.info = h_cond - hdet;
-            o.max_sem = msem;
+            o.h_det = h_det;
+            o.info = h_cond - h_det;
+            o.max_sem = n > 1.0 ? sqrt(m2max / (n - 1.0) * inv_n) : INFINITY;
             o.hits = a.acc[d].hits;
             o.retraced = a.acc[d].retraced;
             o.rows = rows;
@@ -318,44 +357,50 @@ __global__ void __launch_bounds__(128) trace_pairs_kernel(const DevDesign *__res
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const DevDesign &D = *dd;
-    const double lambda = x::wavelength(D, lam_u[i]);
     const double z = z64[i];
     uint32_t bin = D.B;
     double t = 0.0;
     uint8_t fl = 0;
     if (isfinite(z)) {
-        bool exact = mode == CPD_TRACE_FP64;
-        if (!exact) {
+        if (mode == CPD_TRACE_FP64) {
+            uint32_t b = 0;
+            double te = 0.0;
+            if (x::trace(D, x::wavelength(D, lam_u[i]), x::beam_y(D, z), b, te) == 0) {
+                bin = b;
+                t = te;
+            }
+        } else {
+            float zz[2];
+            split_f32(z, zz[0], zz[1]);
             LamParams P;
+            LamDF E;
             const double yg = mode == CPD_TRACE_FP32 ? 0.0 : kYGuardRel;
-            lambda_setup(D, lambda, &z, 1u, P, yg);
-            if (P.core_lo == 0 && P.core_hi == 1 && P.all_exact) {
-                // the ray is its own reference and it has no usable exit/detector geometry
-                exact = mode == CPD_TRACE_HYBRID;
-            } else if (P.core_lo == 0 && P.core_hi == 1) {
+            lambda_setup_df(D, lam_u[i], zz, 1u, P, yg, &E);
+            bool retrace = false;
+            if (P.core_lo == 0 && P.core_hi == 1 && !P.all_exact) {
                 const Guards g = mode == CPD_TRACE_FP32 ? no_guards() : default_guards();
-                float zh, zl;
-                split_f32(z, zh, zl);
                 uint32_t b = 0;
                 float tf = 0.f;
-                const int r = fast_ray(D.fc, P, g, zh, zl, b, tf);
+                const int r = fast_ray(D.fc, P, g, zz[0], zz[1], b, tf);
                 if (r == RAY_HIT) {
                     bin = b;
                     t = tf;
                 } else if (r == RAY_FLAG) {
-                    exact = true;
+                    retrace = true;
                 }
             } else if (P.band_lo == 0 && P.band_hi == 1) {
-                exact = true;  // in a y-interval guard band
+                // in a y-interval guard band, or its own reference ray without a usable
+                // exit/detector geometry
+                retrace = mode == CPD_TRACE_HYBRID;
             }
-        }
-        if (exact) {
-            fl = mode == CPD_TRACE_FP64 ? 0 : 1;
-            uint32_t b = 0;
-            double te = 0.0;
-            if (x::trace(D, lambda, x::beam_y(D, z), b, te) == 0) {
-                bin = b;
-                t = te;
+            if (retrace) {
+                fl = 1;
+                uint32_t b = 0;
+                float tf = 0.f;
+                if (trace_df(D, E, zz[0], zz[1], b, tf)) {
+                    bin = b;
+                    t = tf;
+                }
             }
         }
     }

@@ -8,17 +8,17 @@
 //    -ffp-contract=off. Both therefore give the reference's own f64 results bit
 //    for bit, given the same tables. Transcendentals (log in the inverse normal
 //    CDF, sin/cos in design construction) are evaluated on the host only.
-//  * Per-wavelength setup (lambda_setup): all rays of one wavelength leave the
-//    Gaussian beam with direction (1,0) (Ray::new_from_start, ray.rs:277-279), and
-//    every face before the curved exit face is flat, so the direction and the s/p
-//    transmittances after each flat face are the same for every ray of that
-//    wavelength (the same f64 operations on the same operands). Positions on the
-//    flat faces are affine in the start height y, so the set of rays that clears
-//    every flat face is an interval of y, and, with the ray table sorted by
-//    z = norminv(u), a contiguous range of ray indices.
+//  * Per-wavelength setup (lambda_setup_df, cpd_df.h): all rays of one wavelength
+//    leave the Gaussian beam with direction (1,0) (Ray::new_from_start,
+//    ray.rs:277-279), and every face before the curved exit face is flat, so the
+//    direction and the s/p transmittances after each flat face are the same for every
+//    ray of that wavelength. Positions on the flat faces are affine in the start
+//    height y, so the set of rays that clears every flat face is an interval of y,
+//    and, with the ray table sorted by z = norminv(u), a contiguous range of ray
+//    indices.
 //  * FP32 fast path (fast_ray): per ray, only the exit face and the detector,
 //    with a guard margin on every decision; a ray inside any guard band is
-//    reported FLAG and re-traced with the exact model.
+//    reported FLAG and re-traced in float-float (trace_df, cpd_df.h).
 #pragma once
 
 #include <cstdint>
@@ -26,6 +26,7 @@
 #include <cstring>
 
 #include "../../include/cpd.h"
+#include "cpd_ff.h"
 
 #if defined(__CUDACC__)
 #define CPD_HD __host__ __device__ __forceinline__
@@ -88,7 +89,22 @@ struct alignas(16) FastConst {
     uint32_t B;
 };
 
-// Per design, on the device: the exact f64 tables plus the FP32 constants.
+// Float-float copies of the design tables (split on the host), for the per-wavelength
+// setup and the guard-band re-trace (cpd_df.h).
+struct alignas(16) DFConst {
+    ff::F2 glass[CPD_MAX_GLASS][6];
+    ff::F2 ppx[CPD_MAX_GLASS], ppy[CPD_MAX_GLASS], pnx[CPD_MAX_GLASS], pny[CPD_MAX_GLASS];
+    ff::F2 height;
+    ff::F2 ccx, ccy, rc2, irc;            // exit-face centre, radius^2, 1/radius
+    ff::F2 cbx, cby, cbr2, vx, vy;        // bound centre, bound radius^2, bound centre - centre
+    ff::F2 bin_size, slope, islope, intercept, min_ci, L;
+    ff::F2 dnx, dny, dpx, dpy, dux, duy;  // detector normal, position, direction
+    ff::F2 qx, qy;                        // detector position - bound centre
+    ff::F2 wmin, wspan, bw, bym;          // wavelength range, beam width and centre
+};
+
+// Per design, on the device: the exact f64 tables, their float-float copies and the
+// FP32 constants.
 struct alignas(16) DevDesign {
     int32_t G;
     uint32_t B;
@@ -102,9 +118,10 @@ struct alignas(16) DevDesign {
     double dnx, dny, dpx, dpy, dux, duy;
     double wmin, wmax, bw, bym;
     FastConst fc;
+    DFConst dc;
 };
 
-// Per (design, wavelength), written by lambda_setup. The FP32 fast path works in
+// Per (design, wavelength), written by lambda_setup_df. The FP32 fast path works in
 // differences from one reference ray of the wavelength, traced in f64 through the
 // exit face and onto the detector: every per-ray quantity is the reference value
 // plus a difference computed with a cancellation-free identity, so the FP32 error
@@ -129,16 +146,6 @@ struct alignas(16) LamParams {
     uint32_t pad[3];
 };
 
-// Exact per-face data of one wavelength, written by lambda_setup for the re-trace. The
-// sequential f64 trace computes these from the same operands for every ray of the
-// wavelength, so they are the values it would compute for any one ray.
-struct ExactLam {
-    double dx[CPD_MAX_GLASS], dy[CPD_MAX_GLASS];  // direction after face k
-    double ci[CPD_MAX_GLASS];                     // dot(direction entering face k, N_k)
-    double cr[CPD_MAX_GLASS];                     // refraction cosine at face k
-    double n[CPD_MAX_GLASS];                      // index of glass k
-    double ts, tp;                                // s/p transmittance after the last flat face
-};
 
 // ----------------------------------------------------------------- exact f64 ops
 
@@ -192,38 +199,6 @@ CPD_HD double fma_(double a, double b, double c)
 #endif
 }
 CPD_HD double sqr(double a) { return mul(a, a); }
-
-// f64 reciprocal and square root to ~2^-44 relative, for quantities that only seed the
-// FP32 fast path or sit inside a guard band (never for a value the exact trace
-// reproduces): an FP32 hardware estimate refined by one Newton-Raphson step in f64
-// (y' = y + y(1 - xy); g' = g + (x - g^2) y/2 with y ~ 1/sqrt x). Outside the FP32
-// range they fall back to the IEEE operations. On the host both are the IEEE ones.
-CPD_HD double rcp_approx(double a)
-{
-#if defined(__CUDA_ARCH__)
-    const double m = fabs(a);
-    if (!(m > 1e-30 && m < 1e30)) return __ddiv_rn(1.0, a);
-    float s;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"((float)a));
-    const double y = (double)s;
-    return fma(y, fma(-a, y, 1.0), y);
-#else
-    return 1.0 / a;
-#endif
-}
-CPD_HD double sqrt_approx(double a)
-{
-#if defined(__CUDA_ARCH__)
-    if (!(a > 1e-30 && a < 1e30)) return __dsqrt_rn(a);
-    float s;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"((float)a));
-    const double y = (double)s;
-    const double g = a * y;
-    return fma(0.5 * y, fma(-g, g, a), g);
-#else
-    return std::sqrt(a);
-#endif
-}
 
 CPD_HD double trunc_(double a)
 {
@@ -420,50 +395,6 @@ CPD_HD int trace(const DevDesign &D, double lambda, double y, uint32_t &bin, dou
     return detector(D, r, bin, t);
 }
 
-// The same exact trace with the wavelength's flat-face directions, cosines and glass
-// indices taken from E (written by lambda_setup): every operation whose operands differ
-// between rays -- the face intersections, the transmittance products, the exit face and
-// the detector -- is still done with the reference's operations, so the result is
-// bit-identical to trace(). The wavelength's flat faces do not reflect totally (else
-// lambda_setup drops it).
-template <int G>
-CPD_HD int trace_lam_g(const DevDesign &D, const ExactLam &E, double y, uint32_t &bin, double &t)
-{
-    Ray r{0.0, y, 1.0, 0.0, 1.0, 1.0};
-    double n1 = 1.0;
-    _Pragma("unroll") for (int k = 0; k < G; k++) {
-        const double nx = D.pnx[k], ny = D.pny[k];
-        const double ci = E.ci[k];
-        if (ci == 0.0) return kNoHit;
-        const double d = div(dot(sub(D.ppx[k], r.ox), sub(D.ppy[k], r.oy), nx, ny), ci);
-        if (!(d >= 0.0)) return kNoHit;
-        const double hy = fma_(r.dy, d, r.oy);
-        if (!(0.0 <= hy && hy <= D.height)) return kNoHit;
-        r.ox = fma_(r.dx, d, r.ox);
-        r.oy = hy;
-        // Ray::refract (ray.rs:309-367) with the wavelength's direction and cosines; the
-        // transmittance products are the wavelength's too (E.ts, E.tp)
-        r.dx = E.dx[k];
-        r.dy = E.dy[k];
-        n1 = E.n[k];
-    }
-    r.ts = E.ts;
-    r.tp = E.tp;
-    const int e = exit_face(D, r, n1);
-    if (e) return e;
-    return detector(D, r, bin, t);
-}
-CPD_HD int trace_lam(const DevDesign &D, const ExactLam &E, double y, uint32_t &bin, double &t)
-{
-    switch (D.G) {
-    case 1: return trace_lam_g<1>(D, E, y, bin, t);
-    case 2: return trace_lam_g<2>(D, E, y, bin, t);
-    case 3: return trace_lam_g<3>(D, E, y, bin, t);
-    case 4: return trace_lam_g<4>(D, E, y, bin, t);
-    case 5: return trace_lam_g<5>(D, E, y, bin, t);
-    default: return trace_lam_g<6>(D, E, y, bin, t);
-    }
-}
 }  // namespace x
 
 // ----------------------------------------------------------------- per-wavelength setup
@@ -498,308 +429,7 @@ CPD_HD void split_f32(double v, float &hi, float &lo)
     lo = (float)(v - (double)hi);
 }
 
-// Traces candidate reference rays of the core range in f64 through the exit face and
-// onto the detector line, and stores the first one for which every quantity the fast
-// path differentiates is defined: a secant exit intersection inside the bound, no total
-// internal reflection and a detector cosine above 0.05. (ax, ay) + (bx, by)*y is the
-// position on the last flat face, (dx, dy) the direction entering the exit face,
-// r the index of the last glass. Returns false if no candidate qualifies.
-CPD_HDN inline bool reference_ray(const DevDesign &D, const double *zs, LamParams &P, double ax, double ay,
-                                  double bx, double by, double dx, double dy, double r)
-{
-    const uint32_t lo = P.core_lo, n = P.core_hi - P.core_lo;
-    const double vx = D.cbx - D.ccx, vy = D.cby - D.ccy;  // bound centre m minus sphere centre c
-    const double rc = D.crad, rho2 = D.cbr2, irc = x::rcp_approx(rc);
-    const double qx = D.dpx - D.cbx, qy = D.dpy - D.cby;  // detector position minus m
-    const unsigned char at16[9] = {8, 4, 12, 2, 6, 10, 14, 1, 15};
-    for (int c = 0; c < 9; c++) {
-        uint32_t j = lo + (uint32_t)(((uint64_t)n * at16[c]) / 16u);
-        if (j >= P.core_hi) j = P.core_hi - 1;
-        const double z = zs[j];
-        const double y = D.bym - D.bw * z;
-        const double wx = ax + bx * y - D.cbx, wy = ay + by * y - D.cby;  // relative to m
-        const double ex_ = wx + vx, ey_ = wy + vy;                         // relative to c
-        const double ud = dx * ex_ + dy * ey_;
-        const double cq = (ex_ * ex_ + ey_ * ey_) - rc * rc;
-        const double disc = ud * ud - cq;
-        if (!(disc > 0.0)) continue;
-        const double sd = x::sqrt_approx(disc);
-        const double d1 = -ud - sd, d2 = -ud + sd;
-        double sigma, s;
-        const double p1x = wx + dx * d1, p1y = wy + dy * d1;
-        const double p2x = wx + dx * d2, p2y = wy + dy * d2;
-        if (d1 >= 0.0 && p1x * p1x + p1y * p1y <= rho2) {
-            sigma = -1.0;
-            s = d1;
-        } else if (d2 >= 0.0 && p2x * p2x + p2y * p2y <= rho2) {
-            sigma = 1.0;
-            s = d2;
-        } else {
-            continue;
-        }
-        const double px = wx + dx * s, py = wy + dy * s;
-        const double mb = (px * px + py * py) - rho2;
-        const double nx = -(vx + px) * irc, ny = -(vy + py) * irc;
-        const double ci = -(dx * nx + dy * ny);
-        const double crsq = 1.0 - r * r * (1.0 - ci * ci);
-        if (!(crsq > 1e-6)) continue;
-        const double cr = x::sqrt_approx(crsq);
-        const double kk = r * ci - cr;
-        const double ox = r * dx + kk * nx, oy = r * dy + kk * ny;
-        const double cid = -(ox * D.dnx + oy * D.dny);
-        if (!(cid > 0.05)) continue;
-        const double gx = px - qx, gy = py - qy;
-        const double gn = gx * D.dnx + gy * D.dny, gu = gx * D.dux + gy * D.duy;
-        const double T = gn * x::rcp_approx(cid);
-        const double du = ox * D.dux + oy * D.duy;
-        const double pos = gu + du * T;
-        split_f32(z, P.zref_hi, P.zref_lo);
-        P.dlx2 = (float)(2.0 * ex_);
-        P.dly2 = (float)(2.0 * ey_);
-        P.ud2 = (float)(2.0 * ud);
-        P.disc = (float)disc;
-        P.sd = (float)sd;
-        P.sigma = (float)sigma;
-        P.s = (float)s;
-        P.px2 = (float)(2.0 * px);
-        P.py2 = (float)(2.0 * py);
-        P.mb = (float)mb;
-        P.nx = (float)nx;
-        P.ny = (float)ny;
-        P.ci = (float)ci;
-        P.ci2 = (float)(2.0 * ci);
-        P.crsq = (float)crsq;
-        P.cr = (float)cr;
-        P.r = (float)r;
-        P.r2 = (float)(r * r);
-        P.kk = (float)kk;
-        P.cid = (float)cid;
-        P.gn = (float)gn;
-        P.T = (float)T;
-        P.du = (float)du;
-        P.pos = (float)pos;
-        return true;
-    }
-    return false;
-}
 
-// Computes the per-wavelength parameters from the exact f64 flat-face chain, given
-// the sorted ray table zs[0..R) (ascending z = norminv(u)). Returns false if no ray of
-// this wavelength clears the flat faces (all lost); band ranges may still be non-empty.
-// If E is given it receives the exact per-face data for the re-trace.
-//
-// f64 costs about 80 FP32 operations here (70-cycle DFMA latency, ~700-cycle divide
-// and square root), so only the direction chain -- which the exact re-trace and every
-// per-wavelength decision reuse bit for bit -- is formed with the reference's exact
-// operations; the y interval is accurate to ~1e-14 and guarded at 1e-11.
-template <int G>
-CPD_HDN inline bool lambda_setup_g(const DevDesign &D, double lambda, const double *zs, uint32_t R, LamParams &P,
-                                   double yguard_rel, ExactLam *E)
-{
-    using namespace x;
-    {
-        // zero every field (the struct is plain data)
-        uint32_t *w = reinterpret_cast<uint32_t *>(&P);
-        for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
-    }
-    double nk[CPD_MAX_GLASS], rr[CPD_MAX_GLASS];
-    _Pragma("unroll") for (int k = 0; k < G; k++) nk[k] = calc_n(D.glass[k], lambda);  // independent chains
-    // Ray::refract's n1/n2 of every face: independent IEEE divisions, issued ahead of the
-    // direction chain instead of on it
-    _Pragma("unroll") for (int k = 0; k < G; k++) rr[k] = div(k ? nk[k - 1] : 1.0, nk[k]);
-    double ets = 1.0, etp = 1.0;  // exact s/p transmittance products for the re-trace
-    // direction/transmittance, exactly as the sequential trace computes them
-    double dx = 1.0, dy = 0.0, ts = 1.0, tp = 1.0;
-    // position affine in y: o(y) = (ax + bx*y, ay + by*y)
-    double ax = 0.0, ay = 0.0, bx = 0.0, by = 1.0;
-    double n1 = 1.0;
-    // Tightest bounds y >= -L0/L1 (L1 > 0) and y <= U0/U1 (U1 > 0), kept as fractions and
-    // compared by cross-multiplication so that only the two winners are divided.
-    double L0 = 0.0, L1 = 0.0, Lg = 0.0, U0 = 0.0, U1 = 0.0, Ug = 0.0;
-    bool all_band = false;  // a y-independent constraint sits inside its guard: every ray is re-traced
-    bool ok = true;
-    auto constrain = [&](double c0, double c1, double scale) {
-        // c0 + c1*y >= 0 (up to rounding)
-        const double g = yguard_rel * (scale + 1.0);
-        if (c1 == 0.0) {
-            if (c0 < g && c0 > -g) all_band = true;
-            if (!(c0 > -g)) ok = false;
-        } else if (c1 > 0.0) {
-            if (L1 == 0.0 || c0 * L1 < L0 * c1) {
-                L0 = c0;
-                L1 = c1;
-                Lg = g;
-            }
-        } else {
-            const double u1 = -c1;
-            if (U1 == 0.0 || c0 * U1 < U0 * u1) {
-                U0 = c0;
-                U1 = u1;
-                Ug = g;
-            }
-        }
-    };
-    _Pragma("unroll") for (int k = 0; k < G; k++) {
-        const double n2 = nk[k];
-        const double nx = D.pnx[k], ny = D.pny[k];
-        const double ci = dot(dx, dy, nx, ny);
-        if (ci == 0.0) return false;
-        // dist(y) = ((P - o(y)).N)/ci = e0 + e1*y (guarded: an approximate reciprocal)
-        const double inv = rcp_approx(ci);
-        const double e0 = ((D.ppx[k] - ax) * nx + (D.ppy[k] - ay) * ny) * inv;
-        const double e1 = -(bx * nx + by * ny) * inv;
-        const double sc = (e0 < 0 ? -e0 : e0) + 30.0 * (e1 < 0 ? -e1 : e1) + D.height;
-        constrain(e0, e1, sc);                                   // dist >= 0
-        const double hy0 = ay + dy * e0, hy1 = by + dy * e1;     // hit y = hy0 + hy1*y
-        constrain(hy0, hy1, sc);                                 // 0 <= hit y
-        constrain(D.height - hy0, -hy1, sc);                     // hit y <= height
-        ax = ax + dx * e0;
-        ay = hy0;
-        bx = bx + dx * e1;
-        by = hy1;
-        // Ray::refract's direction with its exact operations (the TIR and AR decisions and
-        // every later face depend on it); the s/p transmittances feed only the FP32 fast
-        // path, so they are formed in FP32 (1 - R without cancellation).
-        const double ci_r = -ci;  // -dot(d, N) of Ray::refract: the same dot product
-        const double rk = rr[k];
-        const double cr_sq = sub(1.0, mul(sqr(rk), sub(1.0, sqr(ci_r))));
-        if (cr_sq < 0.0) return false;  // TIR: the same for every ray
-        const double cr = sqrt_(cr_sq);
-        const double kq = sub(mul(rk, ci_r), cr);
-        const double vx = add(mul(dx, rk), mul(nx, kq));
-        const double vy = add(mul(dy, rk), mul(ny, kq));
-        if (D.ar && ci_r > 0.5) {
-            ts *= 0.99;
-            tp *= 0.99;
-        } else {
-            const float f1 = (float)n1, f2 = (float)n2, fc = (float)ci_r, fr = (float)cr;
-            const float a = f1 * fc + f2 * fr, b = f1 * fr + f2 * fc;
-            const float k4 = 4.f * f1 * f2 * fc * fr;
-            ts *= (double)(k4 / (a * a));
-            tp *= (double)(k4 / (b * b));
-        }
-        if (E) {
-            E->dx[k] = vx;
-            E->dy[k] = vy;
-            E->ci[k] = ci;
-            E->cr[k] = cr;
-            E->n[k] = n2;
-            // the sequential trace's transmittance update at this face, same operations
-            if (D.ar && ci_r > 0.5) {
-                ets = mul(ets, 0.99);
-                etp = mul(etp, 0.99);
-            } else {
-                const double a = mul(n1, ci_r), b = mul(n2, cr);
-                const double rs = sqr(div(sub(a, b), add(a, b)));
-                const double c = mul(n1, cr), e = mul(n2, ci_r);
-                const double rp = sqr(div(sub(c, e), add(c, e)));
-                ets = mul(ets, sub(1.0, rs));
-                etp = mul(etp, sub(1.0, rp));
-            }
-        }
-        dx = vx;
-        dy = vy;
-        n1 = n2;
-    }
-    if (E) {
-        E->ts = ets;
-        E->tp = etp;
-    }
-    if (!ok) return false;
-    const double iL = L1 > 0.0 ? rcp_approx(L1) : 0.0, iU = U1 > 0.0 ? rcp_approx(U1) : 0.0;
-    const double ylo = L1 > 0.0 ? -L0 * iL : -INFINITY, glo = Lg * iL;
-    const double yhi = U1 > 0.0 ? U0 * iU : INFINITY, ghi = Ug * iU;
-    // Sorted-ray index ranges. y_j = bym - bw z_j is monotone in z, so the index of a
-    // height threshold T is the number of z_j below (bym - T)/bw. The guard widths are
-    // many orders above the f64 rounding of that inversion, so the count is taken on
-    // the z table with integer-ordered keys (no f64 arithmetic per search step).
-    auto zkey = [](double v) -> int64_t {
-        int64_t b;
-#if defined(__CUDA_ARCH__)
-        b = __double_as_longlong(v);
-#else
-        std::memcpy(&b, &v, 8);
-#endif
-        return b >= 0 ? b : (int64_t)(0x8000000000000000ull - (uint64_t)b);
-    };
-    // The four counts of a wavelength, searched in lockstep: the table is read by four
-    // independent chains of dependent loads instead of one chain four times as long.
-    auto ycount4 = [&](const double thr[4], uint32_t out[4]) {
-        int64_t key[4];
-        uint32_t lo[4], hi[4];
-        const double ibw = rcp_approx(D.bw);
-        for (int i = 0; i < 4; i++) {
-            const double zt = (D.bym - thr[i]) * ibw;
-            key[i] = zkey(zt);
-            lo[i] = 0;
-            hi[i] = zt != zt ? 0u : R;
-        }
-        while (lo[0] < hi[0] || lo[1] < hi[1] || lo[2] < hi[2] || lo[3] < hi[3]) {
-            for (int i = 0; i < 4; i++) {
-                if (lo[i] < hi[i]) {
-                    const uint32_t mid = (lo[i] + hi[i]) >> 1;
-                    if (zkey(zs[mid]) < key[i]) lo[i] = mid + 1;
-                    else hi[i] = mid;
-                }
-            }
-        }
-        for (int i = 0; i < 4; i++) out[i] = lo[i];
-    };
-    if (all_band) {
-        P.band_lo = P.core_lo = P.core_hi = 0;
-        P.band_hi = R;
-    } else if (D.bw == 0.0) {
-        // every ray starts at the same height
-        double y = D.bym;
-        if (y < ylo - glo || y > yhi + ghi) return false;
-        if ((y < ylo + glo) || (y > yhi - ghi)) {
-            P.band_lo = 0;
-            P.core_lo = P.core_hi = 0;
-            P.band_hi = R;
-        } else {
-            P.band_lo = P.core_lo = 0;
-            P.core_hi = P.band_hi = R;
-        }
-    } else {
-        // bw > 0: j increasing <=> y decreasing: [yhi+g .. yhi-g] band first, core,
-        // [ylo+g .. ylo-g] band; bw < 0 the other way round
-        const double thr[4] = {D.bw > 0.0 ? yhi + ghi : ylo - glo, D.bw > 0.0 ? yhi - ghi : ylo + glo,
-                               D.bw > 0.0 ? ylo + glo : yhi - ghi, D.bw > 0.0 ? ylo - glo : yhi + ghi};
-        uint32_t c[4];
-        ycount4(thr, c);
-        P.band_lo = c[0];
-        P.core_lo = c[1];
-        P.core_hi = c[2];
-        P.band_hi = c[3];
-    }
-    if (P.core_hi < P.core_lo) P.core_hi = P.core_lo;
-    if (P.band_hi < P.core_hi) P.band_hi = P.core_hi;
-    if (P.band_lo > P.core_lo) P.band_lo = P.core_lo;
-    P.w1x = (float)bx;
-    P.w1y = (float)by;
-    P.dx = (float)dx;
-    P.dy = (float)dy;
-    P.ts = (float)ts;
-    P.tp = (float)tp;
-    if (P.core_hi > P.core_lo && !reference_ray(D, zs, P, ax, ay, bx, by, dx, dy, n1)) P.all_exact = 1;
-    return P.band_hi > P.band_lo;
-}
-
-// lambda_setup for a prism count known at compile time: the face loops unroll, so the
-// independent work of one face (positions, constraints, transmittances) is scheduled
-// into the latency of the next face's exact direction step.
-CPD_HDN inline bool lambda_setup(const DevDesign &D, double lambda, const double *zs, uint32_t R, LamParams &P,
-                                 double yguard_rel = kYGuardRel, ExactLam *E = nullptr)
-{
-    switch (D.G) {
-    case 1: return lambda_setup_g<1>(D, lambda, zs, R, P, yguard_rel, E);
-    case 2: return lambda_setup_g<2>(D, lambda, zs, R, P, yguard_rel, E);
-    case 3: return lambda_setup_g<3>(D, lambda, zs, R, P, yguard_rel, E);
-    case 4: return lambda_setup_g<4>(D, lambda, zs, R, P, yguard_rel, E);
-    case 5: return lambda_setup_g<5>(D, lambda, zs, R, P, yguard_rel, E);
-    default: return lambda_setup_g<6>(D, lambda, zs, R, P, yguard_rel, E);
-    }
-}
 
 // ----------------------------------------------------------------- FP32 fast path
 

@@ -207,7 +207,7 @@ uint32_t tile_rows_for(uint32_t B) { return std::max<uint32_t>(1u, kTileCells / 
 // the admission unit of the server.
 uint64_t design_bytes(uint32_t W, uint32_t R, uint32_t B)
 {
-    return (uint64_t)W * (8ull * B + sizeof(LamParams) + sizeof(ExactLam) + 8) + 16ull * R + 16ull * B +
+    return (uint64_t)W * (8ull * B + sizeof(LamParams) + sizeof(LamDF) + 8) + 16ull * R + 16ull * B +
            sizeof(DevDesign) + sizeof(DesignJob) + sizeof(DesignAcc) + sizeof(DesignOut);
 }
 
@@ -277,7 +277,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     CPD_TRY(S.z64.ensure(sizeof(double) * std::max<uint64_t>(ray, 1)));
     CPD_TRY(S.z32.ensure(2 * sizeof(float) * std::max<uint64_t>(ray, 1)));
     CPD_TRY(S.lp.ensure(sizeof(LamParams) * std::max<uint64_t>(rows, 1)));
-    CPD_TRY(S.lx.ensure(sizeof(ExactLam) * std::max<uint64_t>(rows, 1)));
+    CPD_TRY(S.lx.ensure(sizeof(LamDF) * std::max<uint64_t>(rows, 1)));
     CPD_TRY(S.hist.ensure(hist_bytes));
     if (S.hist.cap != old_hist) S.hist_dirty = true;
     CPD_TRY(S.S1.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
@@ -318,7 +318,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     a.z64 = S.z64.as<double>();
     a.z32 = S.z32.as<float>();
     a.lp = S.lp.as<LamParams>();
-    a.lx = S.lx.as<ExactLam>();
+    a.lx = S.lx.as<LamDF>();
     a.hist = S.hist.as<unsigned long long>();
     a.S1 = S.S1.as<unsigned long long>();
     a.S2 = S.S2.as<unsigned long long>();

@@ -46,7 +46,7 @@ constexpr size_t kOffZ64 = kOffLam + al256(8 * kStaticMaxW);
 constexpr size_t kOffZ32 = kOffZ64 + al256(8 * kStaticMaxR);
 constexpr size_t kOffLp = kOffZ32 + al256(8 * kStaticMaxR);
 constexpr size_t kOffLx = kOffLp + al256(sizeof(LamParams) * kStaticMaxW);
-constexpr size_t kOffHist = kOffLx + al256(sizeof(ExactLam) * kStaticMaxW);
+constexpr size_t kOffHist = kOffLx + al256(sizeof(LamDF) * kStaticMaxW);
 constexpr size_t kOffPout = kOffHist + al256(8 * (size_t)kStaticMaxW * kStaticMaxB);
 constexpr size_t kOffQueue = kOffPout + al256(8 * (size_t)kStaticMaxW * kStaticMaxB);
 constexpr size_t kScratchBytes = kOffQueue + al256(sizeof(QEntry) * kStaticQueue);  // about 3 MiB
@@ -162,7 +162,7 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     a.z64 = reinterpret_cast<const double *>(b + kOffZ64);
     a.z32 = reinterpret_cast<const float *>(b + kOffZ32);
     a.lp = reinterpret_cast<LamParams *>(b + kOffLp);
-    a.lx = reinterpret_cast<ExactLam *>(b + kOffLx);
+    a.lx = reinterpret_cast<LamDF *>(b + kOffLx);
     a.hist = reinterpret_cast<unsigned long long *>(b + kOffHist);
     a.S1 = reinterpret_cast<unsigned long long *>(b + kOffS1);
     a.S2 = reinterpret_cast<unsigned long long *>(b + kOffS2);

@@ -4,15 +4,17 @@
 // sorted ray) of the given points, compares fast_ray -- run on the host, with IEEE
 // single-precision sqrt and division where the device uses its approximate MUFU
 // instructions -- with the exact trace: a ray the fast path reports HIT or LOST must
-// have the exact outcome and bin. Rays it flags are re-traced exactly on the device
-// and are only counted.
+// have the exact outcome and bin. Rays it flags are re-traced on the device and are
+// only counted. The float-float re-trace (trace_df) is checked on every ray: same
+// outcome and bin as the exact trace, transmittance within 2e-6 relative.
 //
 // usage: fastpath_check design.bin W R lam_u.bin ray_u.bin
-// prints: rays <n> mismatches <m> flagged <f> outside_band_hits <h>
+// prints: rays <n> mismatches <m> flagged <f> outside_band_hits <h> df_mismatches <d>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
 
+#include "cpd_df.h"
 #include "cpd_host.h"
 #include "cpd_model.h"
 
@@ -38,16 +40,22 @@ int main(int argc, char **argv)
     std::vector<double> z64;
     std::vector<float> z32;
     ray_table(ru.data(), R, z64, z32);
-    long n = 0, mism = 0, flag = 0, outside = 0;
+    long n = 0, mism = 0, flag = 0, outside = 0, dfmism = 0;
     for (int k = 0; k < W; k++) {
         const double lam = x::wavelength(D, lu[k]);
         LamParams P;
-        lambda_setup(D, lam, z64.data(), (uint32_t)z64.size(), P, kYGuardRel);
+        LamDF E;
+        lambda_setup_df(D, lu[k], z32.data(), (uint32_t)z64.size(), P, kYGuardRel, &E);
         for (uint32_t j = 0; j < z64.size(); j++) {
             n++;
             uint32_t b = 0;
             double t = 0;
             const int e = x::trace(D, lam, x::beam_y(D, z64[j]), b, t);
+            // the float-float re-trace must decide every ray like the exact trace
+            uint32_t bd = 0;
+            float td = 0.f;
+            const bool hd = trace_df(D, E, z32[2 * j], z32[2 * j + 1], bd, td);
+            if (hd != (e == 0) || (hd && (bd != b || std::fabs(td - t) > 2e-6 * t))) dfmism++;
             const bool in_band = j >= P.band_lo && j < P.band_hi;
             if (!in_band) {
                 outside += e == 0;
@@ -64,6 +72,7 @@ int main(int argc, char **argv)
             if ((r == RAY_HIT) != (e == 0) || (r == RAY_HIT && bf != b)) mism++;
         }
     }
-    std::printf("rays %ld mismatches %ld flagged %ld outside_band_hits %ld\n", n, mism, flag, outside);
+    std::printf("rays %ld mismatches %ld flagged %ld outside_band_hits %ld df_mismatches %ld\n", n, mism, flag, outside,
+                dfmism);
     return 0;
 }

@@ -1,9 +1,11 @@
-"""The FP32 fast path's decisions, checked on the host against the exact f64 trace
-(tests/fastpath_check.cpp compiled here with g++ from the product's model header).
+"""The FP32 fast path's decisions and the float-float re-trace, checked on the host
+against the exact f64 trace (tests/fastpath_check.cpp compiled here with g++ from the
+product's model headers).
 
 The host build uses IEEE single-precision sqrt and division where the device uses
-its approximate MUFU instructions, so this checks the guard-band logic, not the
-device rounding; the GPU parity tests check the device itself."""
+its approximate MUFU instructions (the float-float reciprocal and square root refine
+either to ~2^-46), so this checks the guard-band logic and the float-float algebra, not
+the device rounding; the GPU parity tests check the device itself."""
 import json
 import os
 import subprocess
@@ -44,7 +46,7 @@ def test_far_reference_ray_design(checker, tmp_path):
     ray_u = P.synth_points(pts["ray_seed"], pts["rays"], first=pts["ray_first"])
     r = _run(checker, tmp_path, spec, lam_u, ray_u)
     assert r["rays"] == len(lam_u) * len(ray_u)
-    assert r["mismatches"] == 0 and r["outside_band_hits"] == 0, r
+    assert r["mismatches"] == 0 and r["outside_band_hits"] == 0 and r["df_mismatches"] == 0, r
 
 
 def test_random_designs(checker, tmp_path):
@@ -54,5 +56,5 @@ def test_random_designs(checker, tmp_path):
     for G, B in [(2, 16), (3, 32), (4, 64), (5, 128), (6, 64), (6, 128)]:
         spec, _, _ = synth.random_design(rng, G, B)
         r = _run(checker, tmp_path, spec, lam_u, ray_u)
-        assert r["mismatches"] == 0 and r["outside_band_hits"] == 0, (G, B, r)
+        assert r["mismatches"] == 0 and r["outside_band_hits"] == 0 and r["df_mismatches"] == 0, (G, B, r)
         assert r["flagged"] < 0.01 * r["rays"], (G, B, r)
