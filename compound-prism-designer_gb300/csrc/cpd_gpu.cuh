@@ -39,6 +39,7 @@ struct alignas(16) QEntry {
 struct Control {
     unsigned long long item_counter;
     unsigned long long queue_count;
+    unsigned long long queue_head;  // queued rays taken by the trace kernel's re-trace
     unsigned int overflow;
     unsigned int pad;
 };
@@ -79,6 +80,7 @@ struct LaunchArgs {
     unsigned long long *S1;
     unsigned long long *S2;
     DesignAcc *acc;
+    unsigned int *tiles_done;  // per design, entropy tiles finished this pass (zeroed per pass)
     DesignOut *out;
     Control *ctl;
     QEntry *queue;
@@ -91,9 +93,11 @@ struct LaunchArgs {
     const float *logtab;  // float-float log2 table (cpd_ff.h), 4 x 256 floats
 };
 
-// Launches setup -> trace -> retrace -> entropy -> finalize on `stream`. Returns the
-// number of kernel launches issued. If `ev` is given (5 events), ev[0..3] are recorded
-// before setup, trace, retrace and entropy, and ev[4] after finalize.
+// Launches the kernels of a pass on `stream`: setup, then trace (which also re-traces
+// the flagged and queued rays) or, in the FP64 study mode, the exact re-trace of every
+// queued ray, then entropy (whose last tile of each design runs the finalize). Returns
+// the number of kernel launches issued. If `ev` is given (5 events), ev[0..3] are
+// recorded before setup, trace, retrace and entropy, and ev[4] after the last kernel.
 int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaStream_t stream,
                 cudaEvent_t *ev = nullptr);
 
