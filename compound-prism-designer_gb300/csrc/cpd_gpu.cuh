@@ -39,7 +39,6 @@ struct alignas(16) QEntry {
 struct Control {
     unsigned long long item_counter;
     unsigned long long queue_count;
-    unsigned long long queue_head;  // queued rays taken by the trace kernel's re-trace
     unsigned int overflow;
     unsigned int pad;
 };
@@ -93,11 +92,10 @@ struct LaunchArgs {
     const float *logtab;  // float-float log2 table (cpd_ff.h), 4 x 256 floats
 };
 
-// Launches the kernels of a pass on `stream`: setup, then trace (which also re-traces
-// the flagged and queued rays) or, in the FP64 study mode, the exact re-trace of every
-// queued ray, then entropy (whose last tile of each design runs the finalize). Returns
-// the number of kernel launches issued. If `ev` is given (5 events), ev[0..3] are
-// recorded before setup, trace, retrace and entropy, and ev[4] after the last kernel.
+// Launches setup -> trace -> retrace -> entropy on `stream` (the warp that finishes a
+// design's last entropy tile runs its finalize). Returns the number of kernel launches
+// issued. If `ev` is given (5 events), ev[i] is recorded before kernel i and ev[4]
+// after the last one.
 int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaStream_t stream,
                 cudaEvent_t *ev = nullptr);
 

@@ -51,28 +51,31 @@ __device__ __forceinline__ void push_ray(const LaunchArgs &a, uint32_t d, uint32
     else atomicOr(&a.ctl->overflow, 1u);
 }
 
-// Sorted-ray tables up to this many rays are staged in shared memory by the setup.
-constexpr uint32_t kStageRays = 2048;
-
-// One warp per block of 32 rows. The block first copies its design record and, for
-// tables of up to kStageRays rays, the design's sorted z table into shared memory with
-// wide coalesced loads, so the per-wavelength program runs on shared-memory operands
-// instead of a chain of dependent global loads.
+// One warp per block of 32 rows. The block first copies its design record into shared
+// memory with wide loads issued together, so the per-wavelength program runs on
+// shared-memory operands instead of a chain of dependent global loads.
 __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
 {
     __shared__ DevDesign sD;
-    extern __shared__ float sz[];  // 2 kStageRays floats
     const uint64_t row0 = blockIdx.x * (uint64_t)blockDim.x;
     const uint64_t row = row0 + threadIdx.x;
     const uint32_t d0 = find_job<F_ROW>(a.jobs, a.njobs, row0);
     const DesignJob &J0 = a.jobs[d0];
     {
+        // all loads first, then the stores, so that they are in flight together
+        constexpr uint32_t kWords = sizeof(DevDesign) / 16, kPer = (kWords + 31) / 32;
         const uint4 *src = reinterpret_cast<const uint4 *>(a.designs + d0);
         uint4 *dst = reinterpret_cast<uint4 *>(&sD);
-        for (uint32_t i = threadIdx.x; i < sizeof(DevDesign) / 16; i += blockDim.x) dst[i] = src[i];
-        if (J0.Rz <= kStageRays) {
-            const float *zs = a.z32 + 2 * J0.ray_off;
-            for (uint32_t i = threadIdx.x; i < 2 * J0.Rz; i += blockDim.x) sz[i] = zs[i];
+        uint4 v[kPer];
+#pragma unroll
+        for (uint32_t r = 0; r < kPer; r++) {
+            const uint32_t i = threadIdx.x + 32u * r;
+            if (i < kWords) v[r] = src[i];
+        }
+#pragma unroll
+        for (uint32_t r = 0; r < kPer; r++) {
+            const uint32_t i = threadIdx.x + 32u * r;
+            if (i < kWords) dst[i] = v[r];
         }
     }
     __syncthreads();
@@ -82,7 +85,7 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     const uint32_t k = (uint32_t)(row - J.row_off);
     const bool staged = d == d0;
     const DevDesign &D = staged ? sD : a.designs[d];
-    const float *z32 = staged && J.Rz <= kStageRays ? sz : a.z32 + 2 * J.ray_off;
+    const float *z32 = a.z32 + 2 * J.ray_off;
     LamParams P;
     lambda_setup_df(D, a.lam_u[J.lam_off + k], z32, J.Rz, P, a.yguard_rel, a.lx + row);
     if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
@@ -98,41 +101,13 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     a.lp[row] = P;
 }
 
-// Float-float re-trace of one queued or flagged ray and its accumulation. Rare (about
-// 0.1% of the rays), so it is kept out of line: the trace loop keeps its registers.
-__device__ __noinline__ void retrace_one(const DevDesign *designs, const DesignJob *jobs, const float *z32,
-                                         const LamDF *lx, unsigned long long *hist, DesignAcc *acc, QEntry e)
-{
-    const DesignJob &J = jobs[e.design];
-    const float *z = z32 + 2 * (J.ray_off + e.j);
-    uint32_t bin = 0;
-    float t = 0.f;
-    if (trace_df(designs[e.design], lx[J.row_off + e.k], z[0], z[1], bin, t)) {
-        atomicAdd(hist + J.hist_off + (uint64_t)e.k * J.B + bin, (unsigned long long)t_fixed(t));
-        atomicAdd(&acc[e.design].hits, 1ull);
-    }
-    atomicAdd(&acc[e.design].retraced, 1ull);
-}
-
-constexpr uint32_t kMaxWarpsPerCta = 8;
-
-// Persistent warps over work items (design, 32-wavelength block, ray chunk); lane =
-// wavelength. The rays of an item are stepped warp-synchronously so that the rays the
-// fast path flags can be collected with a ballot into a per-warp shared buffer and
-// re-traced 32 at a time with every lane busy; what is left in a buffer at the end,
-// and every ray the setup queued, is re-traced by the warps once the items run out.
 __global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
 {
-    __shared__ QEntry fbuf[kMaxWarpsPerCta][64];
     const uint32_t lane = threadIdx.x & 31u;
-    const unsigned full = 0xffffffffu;
-    QEntry *buf = fbuf[threadIdx.x >> 5];
-    uint32_t nbuf = 0;  // warp-uniform
-    const bool retrace = a.mode == CPD_TRACE_HYBRID;
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(&a.ctl->item_counter, 1ull);
-        item = __shfl_sync(full, item, 0);
+        item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= a.total_items) break;
         const uint32_t d = find_job<F_ITEM>(a.jobs, a.njobs, item);
         const DesignJob J = a.jobs[d];
@@ -150,70 +125,39 @@ __global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
             lo = max(j0, P.core_lo);
             hi = min(j1, P.core_hi);
         }
-        const uint32_t jmin = __reduce_min_sync(full, lo < hi ? lo : 0xffffffffu);
-        const uint32_t jmax = __reduce_max_sync(full, lo < hi ? hi : 0u);
         const float2 *__restrict__ zt = reinterpret_cast<const float2 *>(a.z32) + J.ray_off;
         unsigned long long *hrow = a.hist + J.hist_off + (uint64_t)k * J.B;
         uint32_t cur = 0xffffffffu;
         unsigned long long sum = 0ull;
         uint32_t nhit = 0;
         const Guards g = a.guards;
-        for (uint32_t j = jmin; j < jmax; ++j) {
-            int r = RAY_LOST;
-            if (j >= lo && j < hi) {
-                const float2 z = __ldg(zt + j);
-                uint32_t bin = 0;
-                float t = 0.f;
-                r = fast_ray(C, P, g, z.x, z.y, bin, t);
-                if (r == RAY_HIT) {
-                    if (bin != cur) {
-                        if (sum) atomicAdd(hrow + cur, sum);
-                        cur = bin;
-                        sum = 0ull;
-                    }
-                    sum += t_fixed(t);
-                    nhit++;
+        for (uint32_t j = lo; j < hi; ++j) {
+            const float2 z = __ldg(zt + j);
+            uint32_t bin = 0;
+            float t = 0.f;
+            const int r = fast_ray(C, P, g, z.x, z.y, bin, t);
+            if (r == RAY_HIT) {
+                if (bin != cur) {
+                    if (sum) atomicAdd(hrow + cur, sum);
+                    cur = bin;
+                    sum = 0ull;
                 }
-            }
-            const unsigned fm = __ballot_sync(full, r == RAY_FLAG);
-            if (fm && retrace) {
-                if (r == RAY_FLAG) buf[nbuf + __popc(fm & ((1u << lane) - 1u))] = QEntry{d, k, j, 0u};
-                nbuf += __popc(fm);
-                if (nbuf >= 32u) {
-                    __syncwarp();
-                    const QEntry e = buf[lane];
-                    __syncwarp();
-                    if (lane + 32u < nbuf) buf[lane] = buf[lane + 32u];
-                    nbuf -= 32u;
-                    __syncwarp();
-                    retrace_one(a.designs, a.jobs, a.z32, a.lx, a.hist, a.acc, e);
-                }
+                sum += t_fixed(t);
+                nhit++;
+            } else if (r == RAY_FLAG) {
+                push_ray(a, d, k, j);
             }
         }
         if (sum) atomicAdd(hrow + cur, sum);
-        nhit = __reduce_add_sync(full, nhit);
-        const uint32_t nfast = __reduce_add_sync(full, hi > lo ? hi - lo : 0u);
+        nhit = __reduce_add_sync(0xffffffffu, nhit);
+        const uint32_t nfast = __reduce_add_sync(0xffffffffu, hi > lo ? hi - lo : 0u);
         if (lane == 0 && nhit) atomicAdd(&a.acc[d].hits, (unsigned long long)nhit);
         if (lane == 0 && nfast) atomicAdd(&a.acc[d].fast, (unsigned long long)nfast);
     }
-    if (!retrace) return;
-    __syncwarp();
-    if (lane < nbuf) retrace_one(a.designs, a.jobs, a.z32, a.lx, a.hist, a.acc, buf[lane]);
-    // the rays the setup queued (y-interval guard bands, wavelengths without a
-    // reference ray): all written before this kernel started
-    const unsigned long long qc = a.ctl->queue_count;
-    const unsigned long long qn = qc < a.qcap ? qc : a.qcap;
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&a.ctl->queue_head, 32ull);
-        base = __shfl_sync(full, base, 0);
-        if (base >= qn) break;
-        if (base + lane < qn) retrace_one(a.designs, a.jobs, a.z32, a.lx, a.hist, a.acc, a.queue[base + lane]);
-    }
 }
 
-// FP64 study mode: every queued ray with the exact f64 trace of the reference
-// (bit-identical to its CPU path).
+// The queued rays: in the FP64 study mode the exact f64 trace of the reference
+// (bit-identical to its CPU path); otherwise the float-float re-trace.
 __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
 {
     const unsigned long long qn = a.ctl->queue_count;
@@ -224,10 +168,21 @@ __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
         const DevDesign &D = a.designs[e.design];
         const DesignJob &J = a.jobs[e.design];
         uint32_t bin = 0;
-        double t = 0.0;
-        if (x::trace(D, x::wavelength(D, a.lam_u[J.lam_off + e.k]), x::beam_y(D, a.z64[J.ray_off + e.j]), bin, t) ==
-            0) {
-            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, (unsigned long long)t_fixed64(t));
+        unsigned long long tq = 0;
+        bool hit;
+        if (a.mode == CPD_TRACE_FP64) {
+            double t = 0.0;
+            hit = x::trace(D, x::wavelength(D, a.lam_u[J.lam_off + e.k]), x::beam_y(D, a.z64[J.ray_off + e.j]), bin,
+                           t) == 0;
+            tq = t_fixed64(t);
+        } else {
+            float t = 0.f;
+            const float *z = a.z32 + 2 * (J.ray_off + e.j);
+            hit = trace_df(D, a.lx[J.row_off + e.k], z[0], z[1], bin, t);
+            tq = t_fixed(t);
+        }
+        if (hit) {
+            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, tq);
             atomicAdd(&a.acc[e.design].hits, 1ull);
         }
         atomicAdd(&a.acc[e.design].retraced, 1ull);
@@ -512,24 +467,24 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     if (a.total_rows) {
         // one warp per block: f64-pipe bound, so spreading rows over every SM matters
         const uint32_t blocks = (uint32_t)((a.total_rows + 31) / 32);
-        setup_kernel<<<blocks, 32, 2 * kStageRays * sizeof(float), stream>>>(a);
+        setup_kernel<<<blocks, 32, 0, stream>>>(a);
         launches++;
     }
     if (ev) cudaEventRecord(ev[1], stream);
-    if (a.mode != CPD_TRACE_FP64) {
-        // the full persistent grid: after the items, its warps drain the setup's queue
+    if (a.mode != CPD_TRACE_FP64 && a.total_items) {
         int per_sm = 0;
         const int threads = (int)warps_per_cta * 32;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel, threads, 0);
         if (per_sm < 1) per_sm = 1;
-        trace_kernel<<<(unsigned)(num_sms * per_sm), threads, 0, stream>>>(a);
+        uint64_t grid = (uint64_t)num_sms * per_sm;
+        const uint64_t need = (a.total_items + warps_per_cta - 1) / warps_per_cta;
+        if (grid > need) grid = need;
+        trace_kernel<<<(unsigned)grid, threads, 0, stream>>>(a);
         launches++;
     }
     if (ev) cudaEventRecord(ev[2], stream);
-    if (a.mode == CPD_TRACE_FP64) {
-        retrace_kernel<<<(unsigned)(num_sms * 8), 32, 0, stream>>>(a);
-        launches++;
-    }
+    retrace_kernel<<<(unsigned)(num_sms * 8), 32, 0, stream>>>(a);
+    launches++;
     if (ev) cudaEventRecord(ev[3], stream);
     if (a.total_tiles) {
         // one warp per tile, as many blocks as are resident at once
