@@ -143,6 +143,7 @@ void design_to_dev(const cpd_design &d, DevDesign &D)
     f.inv_slope = (float)(1.0 / D.slope);
     f.bin_size = (float)D.bin_size;
     f.bw = (float)D.bw;
+    f.hL = (float)(0.5 * D.L);
     f.ar = D.ar;
     f.B = D.B;
     DFConst &c = D.dc;

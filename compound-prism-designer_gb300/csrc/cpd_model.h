@@ -53,20 +53,15 @@ constexpr double kPScaleInv = 1.0 / 70368744177664.0;
 constexpr double kHScale = 1099511627776.0;          // 2^40, sum of -p log2 p
 constexpr double kHScaleInv = 1.0 / 1099511627776.0;
 
-// 2^31 t for t in [0, 1], rounded to nearest (ties up), with integer operations only
-// (no conversion instruction): t = 1.m x 2^(e-127) so 2^31 t = (1.m 2^23) x 2^(e-119).
+// 2^31 t for t in [0, 1], rounded to nearest even: one FP32-to-u32 conversion (the
+// conversion unit; a 64-bit conversion would go to the FP64 unit).
 CPD_HD uint32_t t_fixed(float t)
 {
 #if defined(__CUDA_ARCH__)
-    const uint32_t b = __float_as_uint(t);
+    return __float2uint_rn(t * 2147483648.0f);
 #else
-    uint32_t b;
-    std::memcpy(&b, &t, 4);
+    return (uint32_t)std::nearbyint((double)t * 2147483648.0);
 #endif
-    const int e = (int)(b >> 23) - 119;
-    const uint32_t m = (b & 0x7fffffu) | 0x800000u;
-    if (e >= 0) return m << (e > 8 ? 8 : e);
-    return e > -25 ? (m + (1u << (-e - 1))) >> (-e) : 0u;
 }
 
 // The same quantization of an f64 transmittance (exact re-trace path).
@@ -85,6 +80,7 @@ struct alignas(16) FastConst {
     float dnfx, dnfy, dufx, dufy;  // detector normal and direction
     float min_ci, L, c0, slope, inv_slope, bin_size;
     float bw;          // beam width
+    float hL;          // L / 2
     int32_t ar;
     uint32_t B;
 };
@@ -460,88 +456,99 @@ CPD_HD float div_fast(float a, float b)
 // the wavelength's reference ray. (zhi, zlo) is the ray's z = norminv(u) split into
 // f32 parts; the ray is known to clear every flat face. Returns RAY_HIT with (bin, t),
 // RAY_LOST, or RAY_FLAG when any decision is inside its guard band.
+// Every operation of the fast path is written out (mulr, addr, subr: rounded, never
+// fused; fmaf: fused), so that each inlined copy of it -- the trace kernel steps two rays
+// at a time -- gives the same bits for the same ray, and the host build computes what
+// the device computes (up to the hardware square root and reciprocal estimates).
+CPD_HD float mulr(float a, float b) { return ff::mul_rn(a, b); }
+CPD_HD float addr(float a, float b) { return ff::add_rn(a, b); }
+CPD_HD float subr(float a, float b) { return ff::sub_rn(a, b); }
+
 CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, float zhi, float zlo, uint32_t &bin,
                     float &t)
 {
     // start-height difference from the reference ray: y = bym - bw z
-    const float dz = (P.zref_hi - zhi) + (P.zref_lo - zlo);
-    const float dyy = D.bw * dz;
-    const float dwx = P.w1x * dyy, dwy = P.w1y * dyy;
+    const float dz = addr(subr(P.zref_hi, zhi), subr(P.zref_lo, zlo));
+    const float dyy = mulr(D.bw, dz);
+    const float dwx = mulr(P.w1x, dyy), dwy = mulr(P.w1y, dyy);
     // exit face: s^2 + 2 ud s + cq = 0, ud = d.(w - c), cq = |w - c|^2 - Rc^2
-    const float dud = fmaf(P.dx, dwx, P.dy * dwy);
-    const float dcq = fmaf(dwx, P.dlx2 + dwx, dwy * (P.dly2 + dwy));
-    const float ddisc = fmaf(dud, P.ud2 + dud, -dcq);
-    const float disc = P.disc + ddisc;
-    if (disc <= g.rel * P.disc) return disc > -g.rel * P.disc ? RAY_FLAG : RAY_LOST;
+    const float dud = fmaf(P.dx, dwx, mulr(P.dy, dwy));
+    const float dcq = fmaf(dwx, addr(P.dlx2, dwx), mulr(dwy, addr(P.dly2, dwy)));
+    const float ddisc = fmaf(dud, addr(P.ud2, dud), -dcq);
+    const float disc = addr(P.disc, ddisc);
+    const float gdisc = mulr(g.rel, P.disc);
+    if (disc <= gdisc) return disc > -gdisc ? RAY_FLAG : RAY_LOST;
     const float sd = sqrt_fast(disc);
     // the other root is 2 sd away along the ray: outside the bound when sd > rho
-    bool flag = sd < 1.01f * D.rho;
-    const float dsd = div_fast(ddisc, sd + P.sd);
+    bool flag = sd < mulr(1.01f, D.rho);
+    const float dsd = div_fast(ddisc, addr(sd, P.sd));
     const float ds = fmaf(P.sigma, dsd, -dud);
-    const float s = P.s + ds;
+    const float s = addr(P.s, ds);
     flag |= fabs_f(s) < g.dist;
     const float dpx = fmaf(P.dx, ds, dwx), dpy = fmaf(P.dy, ds, dwy);
-    const float mb = P.mb + fmaf(dpx, P.px2 + dpx, dpy * (P.py2 + dpy));
-    flag |= fabs_f(mb) < g.rel * D.rho2;
+    const float mb = addr(P.mb, fmaf(dpx, addr(P.px2, dpx), mulr(dpy, addr(P.py2, dpy))));
+    flag |= fabs_f(mb) < mulr(g.rel, D.rho2);
     if (s < 0.f || mb > 0.f) return flag ? RAY_FLAG : RAY_LOST;
     // refraction into air at the exit face, normal n = (c - p)/Rc
-    const float dnx = -dpx * D.inv_rc, dny = -dpy * D.inv_rc;
-    const float dci = -fmaf(P.dx, dnx, P.dy * dny);
-    const float ci = P.ci + dci;
-    const float dcr2 = P.r2 * dci * (P.ci2 + dci);
-    const float crsq = P.crsq + dcr2;
+    const float dnx = -mulr(dpx, D.inv_rc), dny = -mulr(dpy, D.inv_rc);
+    const float dci = -fmaf(P.dx, dnx, mulr(P.dy, dny));
+    const float ci = addr(P.ci, dci);
+    const float dcr2 = mulr(mulr(P.r2, dci), addr(P.ci2, dci));
+    const float crsq = addr(P.crsq, dcr2);
     if (crsq < g.cosine) return crsq > -g.cosine ? RAY_FLAG : RAY_LOST;
     const float cr = sqrt_fast(crsq);
-    const float dcr = div_fast(dcr2, cr + P.cr);
+    const float dcr = div_fast(dcr2, addr(cr, P.cr));
     const float dkk = fmaf(P.r, dci, -dcr);
-    const float nx = P.nx + dnx, ny = P.ny + dny;
-    const float dex = fmaf(P.kk, dnx, dkk * nx), dey = fmaf(P.kk, dny, dkk * ny);
+    const float nx = addr(P.nx, dnx), ny = addr(P.ny, dny);
+    const float dex = fmaf(P.kk, dnx, mulr(dkk, nx)), dey = fmaf(P.kk, dny, mulr(dkk, ny));
     float ts = P.ts, tp = P.tp;
-    if (D.ar) flag |= fabs_f(ci - 0.5f) < g.cosine;
+    if (D.ar) flag |= fabs_f(subr(ci, 0.5f)) < g.cosine;
     if (D.ar && ci > 0.5f) {
-        ts *= 0.99f;
-        tp *= 0.99f;
+        ts = mulr(ts, 0.99f);
+        tp = mulr(tp, 0.99f);
     } else {
         // 1 - Rs = 4 n1 n2 ci cr / (n1 ci + n2 cr)^2, 1 - Rp likewise with ci<->cr (n2 = 1)
         const float r = P.r;
         const float a = fmaf(r, ci, cr), b = fmaf(r, cr, ci);
-        const float a2 = a * a, b2 = b * b;
-        const float inv = div_fast(4.f * r * ci * cr, a2 * b2);
-        ts *= b2 * inv;
-        tp *= a2 * inv;
+        const float a2 = mulr(a, a), b2 = mulr(b, b);
+        const float inv = div_fast(mulr(mulr(mulr(4.f, r), ci), cr), mulr(a2, b2));
+        ts = mulr(ts, mulr(b2, inv));
+        tp = mulr(tp, mulr(a2, inv));
     }
     // detector line
-    const float dcid = -fmaf(dex, D.dnfx, dey * D.dnfy);
-    const float cid = P.cid + dcid;
-    if (cid <= D.min_ci + g.cosine) return cid > D.min_ci - g.cosine ? RAY_FLAG : RAY_LOST;
-    const float dgn = fmaf(dpx, D.dnfx, dpy * D.dnfy);
-    const float dgu = fmaf(dpx, D.dufx, dpy * D.dufy);
-    const float ddu = fmaf(dex, D.dufx, dey * D.dufy);
-    const float dT = div_fast(fmaf(dgn, P.cid, -P.gn * dcid), cid * P.cid);
-    const float tu = ddu * (P.T + dT), tt = P.du * dT;
-    const float dpos = tu + (tt + dgu);
-    const float pos = P.pos + dpos;
+    const float dcid = -fmaf(dex, D.dnfx, mulr(dey, D.dnfy));
+    const float cid = addr(P.cid, dcid);
+    if (cid <= addr(D.min_ci, g.cosine)) return cid > subr(D.min_ci, g.cosine) ? RAY_FLAG : RAY_LOST;
+    const float dgn = fmaf(dpx, D.dnfx, mulr(dpy, D.dnfy));
+    const float dgu = fmaf(dpx, D.dufx, mulr(dpy, D.dufy));
+    const float ddu = fmaf(dex, D.dufx, mulr(dey, D.dufy));
+    const float dT = div_fast(fmaf(dgn, P.cid, -mulr(P.gn, dcid)), mulr(cid, P.cid));
+    const float tu = mulr(ddu, addr(P.T, dT)), tt = mulr(P.du, dT);
+    const float dpos = addr(tu, addr(tt, dgu));
+    const float pos = addr(P.pos, dpos);
     // The position is the one unbounded quantity (a reference ray can land metres from
     // the detector): its guard grows with the magnitudes it was summed from.
-    const float gp = fmaf(g.pos_rel, fabs_f(P.pos) + fabs_f(tu) + fabs_f(tt) + fabs_f(dgu), g.pos);
-    if (pos < -gp || pos > D.L + gp) return RAY_LOST;
-    flag |= pos < gp || pos > D.L - gp;
-    const float xx = pos - D.c0;
-    float qf = floorf(xx * D.inv_slope);
-    float rem = fmaf(-qf, D.slope, xx);
-    if (rem < 0.f) {
-        qf -= 1.f;
-        rem += D.slope;
-    } else if (rem >= D.slope) {
-        qf += 1.f;
-        rem -= D.slope;
-    }
-    flag |= rem < gp || rem > D.slope - gp || fabs_f(rem - D.bin_size) < gp;
+    const float mag = addr(addr(addr(fabs_f(P.pos), fabs_f(tu)), fabs_f(tt)), fabs_f(dgu));
+    const float gp = fmaf(g.pos_rel, mag, g.pos);
+    // 0 <= pos <= L, as a distance from the detector's middle
+    const float dm = fabs_f(subr(pos, D.hL));
+    if (dm > addr(D.hL, gp)) return RAY_LOST;
+    flag |= dm > subr(D.hL, gp);
+    const float xx = subr(pos, D.c0);
+    const float qf = floorf(mulr(xx, D.inv_slope));
+    // within an ulp of a bin boundary the rounded quotient can be one off; such a
+    // remainder falls outside [gp, slope - gp] and the ray is flagged
+    const float rem = fmaf(-qf, D.slope, xx);
+    flag |= rem < gp || rem > subr(D.slope, gp) || fabs_f(subr(rem, D.bin_size)) < gp;
     if (flag) return RAY_FLAG;
-    const uint32_t b = qf <= 0.f ? 0u : (uint32_t)qf;
+#if defined(__CUDA_ARCH__)
+    const uint32_t b = __float2uint_rz(qf);  // saturating: negative -> 0
+#else
+    const uint32_t b = qf <= 0.f ? 0u : (qf >= 4294967295.f ? 4294967295u : (uint32_t)qf);
+#endif
     if (b < D.B && rem < D.bin_size) {
         bin = b;
-        t = (ts + tp) * 0.5f;
+        t = mulr(addr(ts, tp), 0.5f);
         return RAY_HIT;
     }
     return RAY_LOST;
