@@ -79,7 +79,6 @@ struct LaunchArgs {
     unsigned long long *S1;
     unsigned long long *S2;
     DesignAcc *acc;
-    unsigned int *tiles_done;  // per design, entropy tiles finished this pass (zeroed per pass)
     DesignOut *out;
     Control *ctl;
     QEntry *queue;
@@ -92,10 +91,9 @@ struct LaunchArgs {
     const float *logtab;  // float-float log2 table (cpd_ff.h), 4 x 256 floats
 };
 
-// Launches setup -> trace -> retrace -> entropy on `stream` (the warp that finishes a
-// design's last entropy tile runs its finalize). Returns the number of kernel launches
-// issued. If `ev` is given (5 events), ev[i] is recorded before kernel i and ev[4]
-// after the last one.
+// Launches setup -> trace -> retrace -> entropy -> finalize on `stream`. Returns the
+// number of kernel launches issued. If `ev` is given (5 events), ev[0..3] are recorded
+// before setup, trace, retrace and entropy, and ev[4] after finalize.
 int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaStream_t stream,
                 cudaEvent_t *ev = nullptr);
 

@@ -198,7 +198,7 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 
 constexpr int kEntropyThreads = 256;
 
-// Per-design finalize, by the warp that finishes the design's last entropy tile: H(D) from the
+// Per-design finalize by one warp: H(D) from the
 // per-bin sums, MI, and the SEM stop of cuda_fitness (src/cuda_fitness.rs:392-422).
 // f64 costs ~64 cycles per warp instruction here, so pbar log2 pbar is formed in
 // float-float on the FP32 pipe: pbar = S1 / (n R 2^31) and log2 pbar = log2 S1 -
@@ -340,8 +340,7 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
 }
 
 // One warp per entropy tile: kTileCells cells of one design (tile_rows = kTileCells / B
-// rows, at least one). Every warp orders its sums before counting its tile done; the
-// warp that counts a design's last tile finalizes it.
+// rows, at least one).
 __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const LaunchArgs a)
 {
     __shared__ float tab[4 * ff::kLogTable];
@@ -364,14 +363,22 @@ __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const Launc
         else entropy_tile<1>(a, J, r0, r1, lane, tab, h);
         const unsigned long long hl = warp_sum_u64(__double2ull_rn(-((double)h.hi + (double)h.lo) * kHScale));
         if (lane == 0 && hl) atomicAdd(&a.acc[d].H, hl);
-        // the warp that completes a design's last tile runs its finalize
-        __threadfence();
-        unsigned last = 0;
-        if (lane == 0) last = atomicAdd(&a.tiles_done[d], 1u) == J.ntiles - 1u ? 1u : 0u;
-        if (__shfl_sync(0xffffffffu, last, 0)) {
-            __threadfence();
-            finalize_warp(a, d, J, lane, tab);
-        }
+    }
+}
+
+// One warp per design after the entropy kernel.
+__global__ void __launch_bounds__(128) finalize_kernel(const LaunchArgs a)
+{
+    __shared__ float tab[4 * ff::kLogTable];
+    // A pass whose re-trace queue overflowed is re-run by the host: write nothing.
+    if (a.ctl->overflow || a.ctl->queue_count > a.qcap) return;
+    for (uint32_t i = threadIdx.x; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; d < a.njobs; d += nw) {
+        const DesignJob J = a.jobs[d];
+        finalize_warp(a, d, J, lane, tab);
     }
 }
 
@@ -497,6 +504,8 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         entropy_kernel<<<(unsigned)grid, kEntropyThreads, 0, stream>>>(a);
         launches++;
     }
+    finalize_kernel<<<(a.njobs + 3u) / 4u, 128, 0, stream>>>(a);
+    launches++;
     if (ev) cudaEventRecord(ev[4], stream);
     return launches;
 }

@@ -97,7 +97,7 @@ struct PassSlot {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
     cudaEvent_t kev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    DevBuf designs, jobs, lam_u, z64, z32, lp, lx, hist, S1, S2, acc, tiles, out, ctl, queue, pout;
+    DevBuf designs, jobs, lam_u, z64, z32, lp, lx, hist, S1, S2, acc, out, ctl, queue, pout;
     HostBuf h_designs, h_jobs, h_lam, h_z64, h_z32, h_out, h_ctl;
     bool hist_dirty = true;
     uint32_t qcap = 1u << 18;
@@ -128,8 +128,8 @@ struct PassSlot {
         if (stream) cudaStreamSynchronize(stream);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
-        for (DevBuf *b : {&designs, &jobs, &lam_u, &z64, &z32, &lp, &lx, &hist, &S1, &S2, &acc, &tiles, &out, &ctl,
-                          &queue, &pout})
+        for (DevBuf *b : {&designs, &jobs, &lam_u, &z64, &z32, &lp, &lx, &hist, &S1, &S2, &acc, &out, &ctl, &queue,
+                          &pout})
             b->release();
         for (HostBuf *b : {&h_designs, &h_jobs, &h_lam, &h_z64, &h_z32, &h_out, &h_ctl}) b->release();
         for (cudaEvent_t *ev : {&ev0, &ev1, &done, &kev[0], &kev[1], &kev[2], &kev[3], &kev[4]})
@@ -283,7 +283,6 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     CPD_TRY(S.S1.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
     CPD_TRY(S.S2.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
     CPD_TRY(S.acc.ensure(sizeof(DesignAcc) * n));
-    CPD_TRY(S.tiles.ensure(sizeof(unsigned int) * n));
     CPD_TRY(S.out.ensure(sizeof(DesignOut) * n));
     CPD_TRY(S.ctl.ensure(sizeof(Control)));
     CPD_TRY(S.queue.ensure(sizeof(QEntry) * S.qcap));
@@ -324,7 +323,6 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     a.S1 = S.S1.as<unsigned long long>();
     a.S2 = S.S2.as<unsigned long long>();
     a.acc = S.acc.as<DesignAcc>();
-    a.tiles_done = S.tiles.as<unsigned int>();
     a.out = S.out.as<DesignOut>();
     a.ctl = S.ctl.as<Control>();
     a.queue = S.queue.as<QEntry>();
@@ -348,7 +346,6 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     std::memcpy(key.data() + sizeof(a), extra, sizeof(extra));
     auto record = [&](cudaStream_t st) -> int {
         cudaMemsetAsync(S.ctl.p, 0, sizeof(Control), st);
-        cudaMemsetAsync(S.tiles.p, 0, sizeof(unsigned int) * n, st);
         const int l = launch_pass(a, ctx->num_sms, ctx->warps_per_cta, st, profile ? S.kev : nullptr);
         cudaMemcpyAsync(S.h_out.p, S.out.p, sizeof(DesignOut) * n, cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(S.h_ctl.p, S.ctl.p, sizeof(Control), cudaMemcpyDeviceToHost, st);

@@ -37,8 +37,7 @@ constexpr size_t kOffDesign = 0;
 constexpr size_t kOffJob = kOffDesign + al256(sizeof(DevDesign));
 constexpr size_t kOffCtl = kOffJob + al256(sizeof(DesignJob));
 constexpr size_t kOffAcc = kOffCtl + al256(sizeof(Control));
-constexpr size_t kOffTiles = kOffAcc + al256(sizeof(DesignAcc));
-constexpr size_t kOffOut = kOffTiles + al256(sizeof(unsigned int));
+constexpr size_t kOffOut = kOffAcc + al256(sizeof(DesignAcc));
 constexpr size_t kOffS1 = kOffOut + al256(sizeof(DesignOut));
 constexpr size_t kOffS2 = kOffS1 + al256(8 * kStaticMaxB);
 constexpr size_t kOffLog = kOffS2 + al256(8 * kStaticMaxB);
@@ -146,7 +145,6 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     // the array keeps the previous call's contents: clear everything that must start at zero
     if (cudaMemset(b + kOffCtl, 0, sizeof(Control)) != cudaSuccess ||
         cudaMemset(b + kOffAcc, 0, sizeof(DesignAcc)) != cudaSuccess ||
-        cudaMemset(b + kOffTiles, 0, sizeof(unsigned int)) != cudaSuccess ||
         cudaMemset(b + kOffS1, 0, 8 * (size_t)D.B) != cudaSuccess ||
         cudaMemset(b + kOffS2, 0, 8 * (size_t)D.B) != cudaSuccess ||
         cudaMemset(b + kOffHist, 0, 8 * cells) != cudaSuccess)
@@ -169,7 +167,6 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     a.S1 = reinterpret_cast<unsigned long long *>(b + kOffS1);
     a.S2 = reinterpret_cast<unsigned long long *>(b + kOffS2);
     a.acc = reinterpret_cast<DesignAcc *>(b + kOffAcc);
-    a.tiles_done = reinterpret_cast<unsigned int *>(b + kOffTiles);
     a.out = reinterpret_cast<DesignOut *>(b + kOffOut);
     a.ctl = reinterpret_cast<Control *>(b + kOffCtl);
     a.queue = reinterpret_cast<QEntry *>(b + kOffQueue);
