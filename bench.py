@@ -314,6 +314,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="main line only (for profiler runs)")
+    ap.add_argument("--shape", default=None,
+                    help="fixed launch shape RAY_TILE,WARPS instead of the autotuner (for profiler runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = Dist()
@@ -325,14 +327,19 @@ def main():
     import compound_prism_designer as cpd
 
     ctx = cpd.Context(dist.local)
-    ctx.set_autotune(True)  # the first warm-up call tunes the launch shape of this class
+    if args.shape:
+        rt, wp = (int(v) for v in args.shape.split(","))
+        ctx.set_launch_shape(rt, wp)
+    else:
+        ctx.set_autotune(True)  # the first warm-up call tunes the launch shape of this class
     spec, d = plain_design()
     flush, l2_note = l2_flusher()
     seeds = [0.5]
+    nwarp = ctx.launch_shape()[1] if args.shape else 8
 
     def step():
         t0 = time.perf_counter()
-        f = spec.gpu_fitness_full(seeds, max_n=W_PLAIN, nwarp=8, max_eval=R_PLAIN, context=ctx)
+        f = spec.gpu_fitness_full(seeds, max_n=W_PLAIN, nwarp=nwarp, max_eval=R_PLAIN, context=ctx)
         wall = time.perf_counter() - t0
         ms, launches = ctx.last_timing()
         h2d, d2h = ctx.last_transfer_bytes()
@@ -366,7 +373,7 @@ def main():
     if not args.no_extras and dist.rank == 0:
         try:
             ctx.set_profiling(True)
-            fp = spec.gpu_fitness_full(seeds, max_n=W_PLAIN, nwarp=8, max_eval=R_PLAIN, context=ctx)
+            fp = spec.gpu_fitness_full(seeds, max_n=W_PLAIN, nwarp=nwarp, max_eval=R_PLAIN, context=ctx)
             kt = ctx.last_kernel_times()
             ctx.set_profiling(False)
             peak = max(ctx.fp32_peak_tflops(2048) for _ in range(3))
@@ -425,7 +432,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(plain_config(l2_note), launch_shape={"ray_tile": plain_shape[0],
                                                                 "warps_per_cta": plain_shape[1],
-                                                                "picked_by": "autotuner (first warm-up call)"}),
+                                                                "picked_by": "--shape" if args.shape else
+                                                                "autotuner (first warm-up call)"}),
             "e2e": {"value": e2e, "unit": "designs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * wall_s / args.steps},
             "gpu_launches": launches_total, "clocks": clk, "wall_s": t_total,

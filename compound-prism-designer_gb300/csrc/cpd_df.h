@@ -201,15 +201,16 @@ CPD_HDN inline bool reference_ray_df(const DevDesign &D, const float *z32, LamPa
     return false;
 }
 
-// Per-wavelength setup in float-float for a prism count known at compile time.
-// u is the wavelength's u-point (lambda = wmin + (wmax - wmin) u); z32 the sorted ray
-// table as (hi, lo) float pairs, R entries. Fills P (fast-path constants and the band /
-// core ranges of sorted rays) and, if given, E. Returns false if no ray of this
-// wavelength clears the flat faces.
-template <int G>
-CPD_HDN inline bool lambda_setup_df_g(const DevDesign &D, double u, const float *z32, uint32_t R, LamParams &P,
-                                      double yguard_rel, LamDF *E)
+// Per-wavelength setup in float-float. u is the wavelength's u-point (lambda = wmin +
+// (wmax - wmin) u); z32 the sorted ray table as (hi, lo) float pairs, R entries. Fills P
+// (fast-path constants and the band / core ranges of sorted rays) and, if given, E.
+// Returns false if no ray of this wavelength clears the flat faces. The face loop is
+// kept rolled: one warp runs this program once per wavelength, so instruction fetch,
+// not scheduling freedom, is what a longer unrolled body would cost.
+CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z32, uint32_t R, LamParams &P,
+                                    double yguard_rel = kYGuardRel, LamDF *E = nullptr)
 {
+    const int G = D.G;
     using namespace df;
     const DFConst &C = D.dc;
     {
@@ -217,14 +218,6 @@ CPD_HDN inline bool lambda_setup_df_g(const DevDesign &D, double u, const float 
         for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
     }
     const F2 lambda = add(C.wmin, mul(C.wspan, from_d(u)));
-    F2 nk[G];
-#pragma unroll
-    for (int k = 0; k < G; k++) {
-        F2 s = C.glass[k][0];
-#pragma unroll
-        for (int i = 1; i < 6; i++) s = add(mul(s, lambda), C.glass[k][i]);
-        nk[k] = s;
-    }
     F2 dx = c(1.f), dy = c(0.f), ax = c(0.f), ay = c(0.f), bx = c(0.f), by = c(1.f), n1 = c(1.f);
     float ts = 1.f, tp = 1.f;
     // tightest bounds y >= -L0/L1 (L1 > 0) and y <= U0/U1 (U1 > 0), compared by
@@ -253,10 +246,12 @@ CPD_HDN inline bool lambda_setup_df_g(const DevDesign &D, double u, const float 
             }
         }
     };
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < G; k++) {
         if (lost) break;
-        const F2 n2 = nk[k];
+        F2 n2 = C.glass[k][0];  // Glass::calc_n (Horner, glasscat.rs:17-22)
+#pragma unroll
+        for (int i = 1; i < 6; i++) n2 = add(mul(n2, lambda), C.glass[k][i]);
         const F2 nx = C.pnx[k], ny = C.pny[k];
         const F2 ci = dot(dx, dy, nx, ny);
         if (ci.hi == 0.f) {  // parallel to the face: no ray meets it
@@ -382,18 +377,6 @@ CPD_HDN inline bool lambda_setup_df_g(const DevDesign &D, double u, const float 
     return P.band_hi > P.band_lo;
 }
 
-CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z32, uint32_t R, LamParams &P,
-                                    double yguard_rel = kYGuardRel, LamDF *E = nullptr)
-{
-    switch (D.G) {
-    case 1: return lambda_setup_df_g<1>(D, u, z32, R, P, yguard_rel, E);
-    case 2: return lambda_setup_df_g<2>(D, u, z32, R, P, yguard_rel, E);
-    case 3: return lambda_setup_df_g<3>(D, u, z32, R, P, yguard_rel, E);
-    case 4: return lambda_setup_df_g<4>(D, u, z32, R, P, yguard_rel, E);
-    case 5: return lambda_setup_df_g<5>(D, u, z32, R, P, yguard_rel, E);
-    default: return lambda_setup_df_g<6>(D, u, z32, R, P, yguard_rel, E);
-    }
-}
 
 // The float-float re-trace of one ray (start height from z = zh + zl): the flat faces
 // through the wavelength's y interval and affine position, then the curved exit face

@@ -51,32 +51,41 @@ __device__ __forceinline__ void push_ray(const LaunchArgs &a, uint32_t d, uint32
     else atomicOr(&a.ctl->overflow, 1u);
 }
 
-// One warp per block of 32 rows. The block first copies its design record into shared
-// memory with wide loads issued together, so the per-wavelength program runs on
-// shared-memory operands instead of a chain of dependent global loads.
+// Sorted-ray tables up to this many rays are staged in shared memory by the setup.
+constexpr uint32_t kStageRays = 2048;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+
+// One warp per block of 32 rows. The block first copies its design record and, for
+// tables of up to kStageRays rays, its sorted z table into shared memory with
+// asynchronous 16-byte copies that are all in flight at once (one memory latency
+// instead of a chain of dependent loads), so the per-wavelength program and its binary
+// searches run on shared-memory operands. Ray tables start 16-byte aligned (the host
+// pads each to an even number of rays).
 __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
 {
-    __shared__ DevDesign sD;
+    __shared__ __align__(16) DevDesign sD;
+    extern __shared__ __align__(16) float sz[];  // 2 kStageRays floats
     const uint64_t row0 = blockIdx.x * (uint64_t)blockDim.x;
     const uint64_t row = row0 + threadIdx.x;
     const uint32_t d0 = find_job<F_ROW>(a.jobs, a.njobs, row0);
     const DesignJob &J0 = a.jobs[d0];
+    const bool stage_z = J0.Rz <= kStageRays;
     {
-        // all loads first, then the stores, so that they are in flight together
-        constexpr uint32_t kWords = sizeof(DevDesign) / 16, kPer = (kWords + 31) / 32;
-        const uint4 *src = reinterpret_cast<const uint4 *>(a.designs + d0);
-        uint4 *dst = reinterpret_cast<uint4 *>(&sD);
-        uint4 v[kPer];
-#pragma unroll
-        for (uint32_t r = 0; r < kPer; r++) {
-            const uint32_t i = threadIdx.x + 32u * r;
-            if (i < kWords) v[r] = src[i];
+        const char *src = reinterpret_cast<const char *>(a.designs + d0);
+        char *dst = reinterpret_cast<char *>(&sD);
+        for (uint32_t i = threadIdx.x; i < sizeof(DevDesign) / 16; i += blockDim.x) cp_async16(dst + 16 * i, src + 16 * i);
+        if (stage_z) {
+            const char *zs = reinterpret_cast<const char *>(a.z32 + 2 * J0.ray_off);
+            char *zd = reinterpret_cast<char *>(sz);
+            const uint32_t n16 = (J0.Rz + 1u) / 2u;  // 16-byte chunks (two rays each)
+            for (uint32_t i = threadIdx.x; i < n16; i += blockDim.x) cp_async16(zd + 16 * i, zs + 16 * i);
         }
-#pragma unroll
-        for (uint32_t r = 0; r < kPer; r++) {
-            const uint32_t i = threadIdx.x + 32u * r;
-            if (i < kWords) dst[i] = v[r];
-        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
     }
     __syncthreads();
     if (row >= a.total_rows) return;
@@ -85,7 +94,7 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     const uint32_t k = (uint32_t)(row - J.row_off);
     const bool staged = d == d0;
     const DevDesign &D = staged ? sD : a.designs[d];
-    const float *z32 = a.z32 + 2 * J.ray_off;
+    const float *z32 = staged && stage_z ? sz : a.z32 + 2 * J.ray_off;
     LamParams P;
     lambda_setup_df(D, a.lam_u[J.lam_off + k], z32, J.Rz, P, a.yguard_rel, a.lx + row);
     if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
@@ -156,9 +165,30 @@ __global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
     }
 }
 
-// The queued rays: in the FP64 study mode the exact f64 trace of the reference
-// (bit-identical to its CPU path); otherwise the float-float re-trace.
+// The queued rays, hybrid mode: the float-float re-trace.
 __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
+{
+    const unsigned long long qn = a.ctl->queue_count;
+    const uint64_t n = qn < a.qcap ? qn : a.qcap;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const QEntry e = a.queue[i];
+        const DesignJob &J = a.jobs[e.design];
+        const float *z = a.z32 + 2 * (J.ray_off + e.j);
+        uint32_t bin = 0;
+        float t = 0.f;
+        if (trace_df(a.designs[e.design], a.lx[J.row_off + e.k], z[0], z[1], bin, t)) {
+            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, (unsigned long long)t_fixed(t));
+            atomicAdd(&a.acc[e.design].hits, 1ull);
+        }
+        atomicAdd(&a.acc[e.design].retraced, 1ull);
+    }
+}
+
+// The queued rays, FP64 study mode: the exact f64 trace of the reference
+// (bit-identical to its CPU path). A kernel of its own, so that the hybrid re-trace
+// does not carry this code.
+__global__ void __launch_bounds__(32) retrace_exact_kernel(const LaunchArgs a)
 {
     const unsigned long long qn = a.ctl->queue_count;
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
@@ -168,21 +198,10 @@ __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
         const DevDesign &D = a.designs[e.design];
         const DesignJob &J = a.jobs[e.design];
         uint32_t bin = 0;
-        unsigned long long tq = 0;
-        bool hit;
-        if (a.mode == CPD_TRACE_FP64) {
-            double t = 0.0;
-            hit = x::trace(D, x::wavelength(D, a.lam_u[J.lam_off + e.k]), x::beam_y(D, a.z64[J.ray_off + e.j]), bin,
-                           t) == 0;
-            tq = t_fixed64(t);
-        } else {
-            float t = 0.f;
-            const float *z = a.z32 + 2 * (J.ray_off + e.j);
-            hit = trace_df(D, a.lx[J.row_off + e.k], z[0], z[1], bin, t);
-            tq = t_fixed(t);
-        }
-        if (hit) {
-            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, tq);
+        double t = 0.0;
+        if (x::trace(D, x::wavelength(D, a.lam_u[J.lam_off + e.k]), x::beam_y(D, a.z64[J.ray_off + e.j]), bin, t) ==
+            0) {
+            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, (unsigned long long)t_fixed64(t));
             atomicAdd(&a.acc[e.design].hits, 1ull);
         }
         atomicAdd(&a.acc[e.design].retraced, 1ull);
@@ -474,7 +493,7 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     if (a.total_rows) {
         // one warp per block: f64-pipe bound, so spreading rows over every SM matters
         const uint32_t blocks = (uint32_t)((a.total_rows + 31) / 32);
-        setup_kernel<<<blocks, 32, 0, stream>>>(a);
+        setup_kernel<<<blocks, 32, 2 * kStageRays * sizeof(float), stream>>>(a);
         launches++;
     }
     if (ev) cudaEventRecord(ev[1], stream);
@@ -490,7 +509,8 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         launches++;
     }
     if (ev) cudaEventRecord(ev[2], stream);
-    retrace_kernel<<<(unsigned)(num_sms * 8), 32, 0, stream>>>(a);
+    if (a.mode == CPD_TRACE_FP64) retrace_exact_kernel<<<(unsigned)(num_sms * 8), 32, 0, stream>>>(a);
+    else retrace_kernel<<<(unsigned)(num_sms * 8), 32, 0, stream>>>(a);
     launches++;
     if (ev) cudaEventRecord(ev[3], stream);
     if (a.total_tiles) {

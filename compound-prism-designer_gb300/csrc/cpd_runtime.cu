@@ -247,7 +247,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         rows += J.W;
         hist += (uint64_t)J.W * J.B;
         lam += J.W;
-        if (owns_rays[i]) ray += J.Rz;
+        if (owns_rays[i]) ray += (J.Rz + 1u) & ~1u;  // even: every table starts 16-byte aligned
         accc += J.B;
         items += (uint64_t)((J.W + 31) / 32) * J.nchunk;
         tiles += J.ntiles;
