@@ -43,13 +43,18 @@ struct Control {
     unsigned int pad;
 };
 
+// Copies of each per-design ray counter: thousands of warps add to the counters of one
+// design, and same-address atomics serialize in L2, so each warp adds to one of
+// kSpread copies and the finalize sums them.
+constexpr int kSpread = 16;
+
 // Per-design accumulators that persist across the seeds of one call.
 struct DesignAcc {
-    unsigned long long H;         // sum over rows and bins of -p log2 p, 2^-40 units
-    unsigned long long hits;      // rays that reached a bin
-    unsigned long long retraced;  // rays re-traced in exact f64
-    unsigned long long rows;      // wavelength rows accumulated
-    unsigned long long fast;      // rays evaluated by the FP32 fast path
+    unsigned long long H;                  // sum over rows and bins of -p log2 p, 2^-40 units
+    unsigned long long rows;               // wavelength rows accumulated
+    unsigned long long hits[kSpread];      // rays that reached a bin
+    unsigned long long retraced[kSpread];  // rays re-traced
+    unsigned long long fast[kSpread];      // rays evaluated by the FP32 fast path
 };
 
 // Per-design result of the fused finalize (cumulative over passes).

@@ -160,8 +160,9 @@ __global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
         if (sum) atomicAdd(hrow + cur, sum);
         nhit = __reduce_add_sync(0xffffffffu, nhit);
         const uint32_t nfast = __reduce_add_sync(0xffffffffu, hi > lo ? hi - lo : 0u);
-        if (lane == 0 && nhit) atomicAdd(&a.acc[d].hits, (unsigned long long)nhit);
-        if (lane == 0 && nfast) atomicAdd(&a.acc[d].fast, (unsigned long long)nfast);
+        const uint32_t sp = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % (uint32_t)kSpread;
+        if (lane == 0 && nhit) atomicAdd(&a.acc[d].hits[sp], (unsigned long long)nhit);
+        if (lane == 0 && nfast) atomicAdd(&a.acc[d].fast[sp], (unsigned long long)nfast);
     }
 }
 
@@ -179,9 +180,9 @@ __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
         float t = 0.f;
         if (trace_df(a.designs[e.design], a.lx[J.row_off + e.k], z[0], z[1], bin, t)) {
             atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, (unsigned long long)t_fixed(t));
-            atomicAdd(&a.acc[e.design].hits, 1ull);
+            atomicAdd(&a.acc[e.design].hits[i % kSpread], 1ull);
         }
-        atomicAdd(&a.acc[e.design].retraced, 1ull);
+        atomicAdd(&a.acc[e.design].retraced[i % kSpread], 1ull);
     }
 }
 
@@ -202,9 +203,9 @@ __global__ void __launch_bounds__(32) retrace_exact_kernel(const LaunchArgs a)
         if (x::trace(D, x::wavelength(D, a.lam_u[J.lam_off + e.k]), x::beam_y(D, a.z64[J.ray_off + e.j]), bin, t) ==
             0) {
             atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, (unsigned long long)t_fixed64(t));
-            atomicAdd(&a.acc[e.design].hits, 1ull);
+            atomicAdd(&a.acc[e.design].hits[i % kSpread], 1ull);
         }
-        atomicAdd(&a.acc[e.design].retraced, 1ull);
+        atomicAdd(&a.acc[e.design].retraced[i % kSpread], 1ull);
     }
 }
 
@@ -267,6 +268,10 @@ __device__ void finalize_warp(const LaunchArgs &a, uint32_t d, const DesignJob &
             m2max = fmax(m2max, __shfl_xor_sync(0xffffffffu, m2max, o));
         }
         conv = __all_sync(0xffffffffu, conv);
+        const bool cp = lane < (uint32_t)kSpread;
+        const unsigned long long hits = warp_sum_u64(cp ? __ldcg(&a.acc[d].hits[lane]) : 0ull);
+        const unsigned long long retraced = warp_sum_u64(cp ? __ldcg(&a.acc[d].retraced[lane]) : 0ull);
+        const unsigned long long fast = warp_sum_u64(cp ? __ldcg(&a.acc[d].fast[lane]) : 0ull);
         if (lane == 0) {
             const double H = (double)__ldcg(&a.acc[d].H) * kHScaleInv;
             const double h_cond = -H * inv_n;
@@ -276,10 +281,10 @@ __device__ void finalize_warp(const LaunchArgs &a, uint32_t d, const DesignJob &
             o.h_det = h_det;
             o.info = h_cond - h_det;
             o.max_sem = n > 1.0 ? sqrt(m2max / (n - 1.0) * inv_n) : INFINITY;
-            o.hits = __ldcg(&a.acc[d].hits);
-            o.retraced = __ldcg(&a.acc[d].retraced);
+            o.hits = hits;
+            o.retraced = retraced;
             o.rows = rows;
-            o.fast = __ldcg(&a.acc[d].fast);
+            o.fast = fast;
             o.converged = conv;
             o.pad = 0;
             a.out[d] = o;
@@ -317,34 +322,39 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
             q2[i] = ff::F2{0.f, 0.f};
         }
         for (uint32_t row = r0 + grp; row < r1; row += RS * groups) {
-            unsigned long long c[RS][NB];
+            unsigned long long c[RS * NB];
 #pragma unroll
             for (uint32_t rr = 0; rr < RS; rr++) {
                 const uint32_t rw = row + rr * groups;
 #pragma unroll
                 for (int i = 0; i < NB; i++) {
                     const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
-                    c[rr][i] = (active && rw < r1 && b < B) ? base[(uint64_t)rw * B + b] : 0ull;
+                    c[rr * NB + i] = (active && rw < r1 && b < B) ? base[(uint64_t)rw * B + b] : 0ull;
                 }
             }
+            // one copy of the cell code, not RS x NB: the plain call runs each tile once,
+            // so instruction fetch is what an unrolled body would cost
+#pragma unroll 1
+            for (uint32_t q = 0; q < RS * NB; q++) {
+                const uint32_t rw = row + (q / NB) * groups;
+                const uint32_t i = q % NB;
+                const uint32_t b = bg + bin0 + 32u * i;
+                const unsigned long long cv = c[q];
+                if (cv) {
+                    base[(uint64_t)rw * B + b] = 0ull;
+                    // p = c unit and p log2 p in float-float (FP32 pipe)
+                    const ff::F2 p = ff::mul(ff::from_u64(cv), unit);
+                    const ff::F2 lp = ff::add(ff::log2_u64(cv, tab), lu);
+                    h = ff::add(h, ff::mul(p, lp));
+                    const ff::F2 pp = ff::mul(p, p);
 #pragma unroll
-            for (uint32_t rr = 0; rr < RS; rr++) {
-                const uint32_t rw = row + rr * groups;
-#pragma unroll
-                for (int i = 0; i < NB; i++) {
-                    const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
-                    const unsigned long long cv = c[rr][i];
-                    if (cv) {
-                        base[(uint64_t)rw * B + b] = 0ull;
-                        // p = c unit and p log2 p in float-float (FP32 pipe)
-                        const ff::F2 p = ff::mul(ff::from_u64(cv), unit);
-                        const ff::F2 lp = ff::add(ff::log2_u64(cv, tab), lu);
-                        h = ff::add(h, ff::mul(p, lp));
-                        q2[i] = ff::add(q2[i], ff::mul(p, p));
-                        c1[i] += cv;
-                    }
-                    if (a.p_out && active && rw < r1 && b < B) a.p_out[(uint64_t)rw * B + b] = (double)cv * p_unit;
+                    for (int ii = 0; ii < NB; ii++)
+                        if (ii == (int)i) {
+                            q2[ii] = ff::add(q2[ii], pp);
+                            c1[ii] += cv;
+                        }
                 }
+                if (a.p_out && active && rw < r1 && b < B) a.p_out[(uint64_t)rw * B + b] = (double)cv * p_unit;
             }
         }
 #pragma unroll
