@@ -255,6 +255,26 @@ def serving_form(ctx, generations=200):
     return out
 
 
+def run_batch_only(args):
+    """--batch-only N: the batched form on N designs (W 512..4096, R 1024), one pass per
+    step, for profiler captures; prints one JSON line of device times."""
+    import compound_prism_designer as cpd
+
+    pop, Ws, _ = batched_population()
+    pop, Ws = pop[:args.batch_only], Ws[:args.batch_only]
+    ctx = cpd.Context(0)
+    rt, wp = (int(v) for v in (args.shape or "64,8").split(","))
+    ctx.set_launch_shape(rt, wp)
+    for _ in range(args.warmup):
+        cpd.fitness_batch(pop, seeds=0.5, max_n=Ws, max_eval=R_PLAIN, context=ctx)
+    ms = []
+    for _ in range(args.steps):
+        cpd.fitness_batch(pop, seeds=0.5, max_n=Ws, max_eval=R_PLAIN, context=ctx)
+        ms.append(ctx.last_timing()[0])
+    print(json.dumps({"form": "batched", "designs": len(pop), "rays": int(sum(int(w) for w in Ws) * R_PLAIN),
+                      "ms": ms, "shape": [rt, wp]}), flush=True)
+
+
 def run_reference(args, dist):
     """--impl reference: the reference CPU algorithm (oracle port) on the same workload."""
     if dist.rank != 0:
@@ -316,6 +336,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="main line only (for profiler runs)")
     ap.add_argument("--shape", default=None,
                     help="fixed launch shape RAY_TILE,WARPS instead of the autotuner (for profiler runs)")
+    ap.add_argument("--batch-only", type=int, default=0, metavar="N",
+                    help="profiler run: only the batched form, on the first N designs of its population")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = Dist()
@@ -326,6 +348,9 @@ def main():
     import numpy as np
     import compound_prism_designer as cpd
 
+    if args.batch_only:
+        run_batch_only(args)
+        return
     ctx = cpd.Context(dist.local)
     if args.shape:
         rt, wp = (int(v) for v in args.shape.split(","))
