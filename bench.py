@@ -41,10 +41,11 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 METRIC = "MI fitness designs/sec, batched-serving vs plain at <=1e-4 rel MI err; p50/p99 ms"
 G_PLAIN, B_PLAIN, W_PLAIN, R_PLAIN = 6, 64, 4096, 1024
-# FP32 arithmetic of fast_ray on its full path (exit face, refraction, Fresnel,
-# detector, binning): adds/muls count 1, FMAs 2; the 5 MUFU ops (2 sqrt, 3 reciprocal/
-# divide) are not counted. Derivation in the design doc.
-FLOP_PER_FAST_RAY = 110
+# FP32 arithmetic of fast_ray on its full path for an anti-reflection-coated design (exit
+# face, refraction, detector, binning and the guard-band thresholds): adds/muls count 1,
+# FMAs 2; the 5 hardware estimates (2 sqrt, 3 reciprocals) and the floor are not counted.
+# Rays lost early execute fewer, so this is an upper bound per evaluated ray.
+FLOP_PER_FAST_RAY = 102
 
 
 def dist_info():
@@ -318,7 +319,7 @@ def plain_config(l2):
 
 def traffic_from_profiles():
     """dram bytes per trace-kernel launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "fitness_pass_config1.md")
+    p = os.path.join(ROOT, "profiles", "fitness_pass_plain_g6_b64_w4096_r1024.md")
     try:
         txt = open(p).read()
     except OSError:
