@@ -139,12 +139,11 @@ __global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
         uint32_t cur = 0xffffffffu;
         unsigned long long sum = 0ull;
         uint32_t nhit = 0;
-        const Guards g = a.guards;
         for (uint32_t j = lo; j < hi; ++j) {
             const float2 z = __ldg(zt + j);
             uint32_t bin = 0;
             float t = 0.f;
-            const int r = fast_ray(C, P, g, z.x, z.y, bin, t);
+            const int r = fast_ray(C, P, a.guards, z.x, z.y, bin, t);
             if (r == RAY_HIT) {
                 if (bin != cur) {
                     if (sum) atomicAdd(hrow + cur, sum);

@@ -353,7 +353,7 @@ CPD_HD int detector(const DevDesign &D, const Ray &r, uint32_t &bin, double &t, 
     if (!(q == q) || q <= 0.0) b = 0;
     else if (q >= 4294967295.0) b = 4294967295u;
     else b = (uint32_t)q;
-    if (b < D.B && rem < D.bin_size) {
+    if ((b < D.B) & (rem < D.bin_size)) {
         bin = b;
         t = mul(add(r.ts, r.tp), 0.5);
         return 0;
@@ -488,7 +488,7 @@ CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, flo
     const float dpx = fmaf(P.dx, ds, dwx), dpy = fmaf(P.dy, ds, dwy);
     const float mb = addr(P.mb, fmaf(dpx, addr(P.px2, dpx), mulr(dpy, addr(P.py2, dpy))));
     flag |= fabs_f(mb) < mulr(g.rel, D.rho2);
-    if (s < 0.f || mb > 0.f) return flag ? RAY_FLAG : RAY_LOST;
+    if ((s < 0.f) | (mb > 0.f)) return flag ? RAY_FLAG : RAY_LOST;
     // refraction into air at the exit face, normal n = (c - p)/Rc
     const float dnx = -mulr(dpx, D.inv_rc), dny = -mulr(dpy, D.inv_rc);
     const float dci = -fmaf(P.dx, dnx, mulr(P.dy, dny));
@@ -539,14 +539,14 @@ CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, flo
     // within an ulp of a bin boundary the rounded quotient can be one off; such a
     // remainder falls outside [gp, slope - gp] and the ray is flagged
     const float rem = fmaf(-qf, D.slope, xx);
-    flag |= rem < gp || rem > subr(D.slope, gp) || fabs_f(subr(rem, D.bin_size)) < gp;
+    flag |= (rem < gp) | (rem > subr(D.slope, gp)) | (fabs_f(subr(rem, D.bin_size)) < gp);
     if (flag) return RAY_FLAG;
 #if defined(__CUDA_ARCH__)
     const uint32_t b = __float2uint_rz(qf);  // saturating: negative -> 0
 #else
     const uint32_t b = qf <= 0.f ? 0u : (qf >= 4294967295.f ? 4294967295u : (uint32_t)qf);
 #endif
-    if (b < D.B && rem < D.bin_size) {
+    if ((b < D.B) & (rem < D.bin_size)) {
         bin = b;
         t = mulr(addr(ts, tp), 0.5f);
         return RAY_HIT;
