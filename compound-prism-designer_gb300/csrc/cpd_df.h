@@ -219,7 +219,10 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
     }
     const F2 lambda = add(C.wmin, mul(C.wspan, from_d(u)));
     F2 dx = c(1.f), dy = c(0.f), ax = c(0.f), ay = c(0.f), bx = c(0.f), by = c(1.f), n1 = c(1.f);
-    float ts = 1.f, tp = 1.f;
+    // s/p transmittance products in float-float: the AR factor 0.99 is not a float, and
+    // six float roundings would bias every ray of the wavelength by ~6e-8
+    F2 ts = c(1.f), tp = c(1.f);
+    const F2 ar99{0.99f, -9.5367431640625e-09f};  // 0.99 = hi + lo to ~1e-17
     // tightest bounds y >= -L0/L1 (L1 > 0) and y <= U0/U1 (U1 > 0), compared by
     // cross-multiplication so that only the two winners are divided
     F2 L0 = c(0.f), L1 = c(0.f), U0 = c(0.f), U1 = c(0.f);
@@ -283,15 +286,15 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
         const F2 kq = sub(mul(rr, ci_r), cr);
         const F2 vx = add(mul(dx, rr), mul(nx, kq)), vy = add(mul(dy, rr), mul(ny, kq));
         if (D.ar && ci_r.hi > 0.5f) {
-            ts *= 0.99f;
-            tp *= 0.99f;
+            ts = mul(ts, ar99);
+            tp = mul(tp, ar99);
         } else {
             // 1 - R without cancellation: 4 n1 n2 ci cr / (n1 ci + n2 cr)^2 (s), ci <-> cr (p)
             const float f1 = n1.hi, f2 = n2.hi, fc = ci_r.hi, fr = cr.hi;
             const float a = f1 * fc + f2 * fr, b = f1 * fr + f2 * fc;
             const float k4 = 4.f * f1 * f2 * fc * fr;
-            ts *= k4 / (a * a);
-            tp *= k4 / (b * b);
+            ts = mulf(ts, k4 / (a * a));
+            tp = mulf(tp, k4 / (b * b));
         }
         dx = vx;
         dy = vy;
@@ -309,8 +312,8 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
         E->dx = dx;
         E->dy = dy;
         E->n = n1;
-        E->ts = ts;
-        E->tp = tp;
+        E->ts = ts.hi;
+        E->tp = tp.hi;
         E->lost = lost ? 1u : 0u;
         E->pad[0] = E->pad[1] = E->pad[2] = 0u;
     }
@@ -371,8 +374,8 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
     P.w1y = by.hi;
     P.dx = dx.hi;
     P.dy = dy.hi;
-    P.ts = ts;
-    P.tp = tp;
+    P.ts = ts.hi;
+    P.tp = tp.hi;
     if (P.core_hi > P.core_lo && !reference_ray_df(D, z32, P, ax, ay, bx, by, dx, dy, n1)) P.all_exact = 1;
     return P.band_hi > P.band_lo;
 }
