@@ -98,9 +98,11 @@ struct LaunchArgs {
 
 // Launches setup -> trace -> retrace -> entropy -> finalize on `stream`. Returns the
 // number of kernel launches issued. If `ev` is given (5 events), ev[0..3] are recorded
-// before setup, trace, retrace and entropy, and ev[4] after finalize.
+// before setup, trace, retrace and entropy, and ev[4] after finalize. With `pdl` (and no
+// events) each kernel after the setup is a programmatic dependent launch: its blocks
+// become resident while its predecessor runs and wait for its results.
 int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaStream_t stream,
-                cudaEvent_t *ev = nullptr);
+                cudaEvent_t *ev = nullptr, bool pdl = false);
 
 // One thread per (lam_u[i], z[i]) pair: the twin of propagation_test_kernel.
 void launch_trace_pairs(const DevDesign *d, const double *lam_u, const double *z64, uint32_t n, uint32_t mode,

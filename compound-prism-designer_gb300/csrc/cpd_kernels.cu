@@ -68,6 +68,9 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 // pads each to an even number of rays).
 __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
 {
+    // lets the trace kernel's blocks become resident now; they wait for this grid's
+    // results in cudaGridDependencySynchronize
+    cudaTriggerProgrammaticLaunchCompletion();
     __shared__ __align__(16) DevDesign sD;
     extern __shared__ __align__(16) float sz[];  // 2 kStageRays floats
     const uint64_t row0 = blockIdx.x * (uint64_t)blockDim.x;
@@ -112,6 +115,8 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
 
 __global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
 {
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();  // setup's LamParams and queue
     const uint32_t lane = threadIdx.x & 31u;
     for (;;) {
         unsigned long long item = 0;
@@ -168,6 +173,8 @@ __global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
 // The queued rays, hybrid mode: the float-float re-trace.
 __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
 {
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();  // the queue of the setup and trace kernels
     const unsigned long long qn = a.ctl->queue_count;
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -190,6 +197,8 @@ __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
 // does not carry this code.
 __global__ void __launch_bounds__(32) retrace_exact_kernel(const LaunchArgs a)
 {
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();  // the queue of the setup and trace kernels
     const unsigned long long qn = a.ctl->queue_count;
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -372,11 +381,13 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
 __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const LaunchArgs a)
 {
     __shared__ float tab[4 * ff::kLogTable];
+    cudaTriggerProgrammaticLaunchCompletion();
+    for (uint32_t i = threadIdx.x; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
+    __syncthreads();
+    cudaGridDependencySynchronize();  // the histogram of the trace and re-trace kernels
     // A pass whose re-trace queue overflowed is re-run by the host: leave every
     // accumulator untouched.
     if (a.ctl->overflow || a.ctl->queue_count > a.qcap) return;
-    for (uint32_t i = threadIdx.x; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
-    __syncthreads();
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t tile = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < a.total_tiles; tile += nw) {
@@ -398,10 +409,11 @@ __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const Launc
 __global__ void __launch_bounds__(128) finalize_kernel(const LaunchArgs a)
 {
     __shared__ float tab[4 * ff::kLogTable];
-    // A pass whose re-trace queue overflowed is re-run by the host: write nothing.
-    if (a.ctl->overflow || a.ctl->queue_count > a.qcap) return;
     for (uint32_t i = threadIdx.x; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
     __syncthreads();
+    cudaGridDependencySynchronize();  // the entropy kernel's sums
+    // A pass whose re-trace queue overflowed is re-run by the host: write nothing.
+    if (a.ctl->overflow || a.ctl->queue_count > a.qcap) return;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; d < a.njobs; d += nw) {
@@ -495,14 +507,36 @@ __global__ void fma_peak_kernel(float *out, uint32_t iters)
 
 }  // namespace
 
-int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaStream_t stream, cudaEvent_t *ev)
+// A launch that, with `pdl`, may start before the previous kernel on the stream has
+// finished (programmatic dependent launch): the kernel waits for its predecessor's
+// results in cudaGridDependencySynchronize.
+void launch_k(void (*k)(const LaunchArgs), unsigned grid, unsigned block, size_t smem, cudaStream_t st, bool pdl,
+              const LaunchArgs &a)
 {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k, a);
+}
+
+int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaStream_t stream, cudaEvent_t *ev,
+                bool pdl)
+{
+    // per-kernel events would stand between the kernels
+    pdl = pdl && ev == nullptr;
     int launches = 0;
     if (ev) cudaEventRecord(ev[0], stream);
     if (a.total_rows) {
         // one warp per block: f64-pipe bound, so spreading rows over every SM matters
         const uint32_t blocks = (uint32_t)((a.total_rows + 31) / 32);
-        setup_kernel<<<blocks, 32, 2 * kStageRays * sizeof(float), stream>>>(a);
+        launch_k(setup_kernel, blocks, 32, 2 * kStageRays * sizeof(float), stream, false, a);
         launches++;
     }
     if (ev) cudaEventRecord(ev[1], stream);
@@ -514,12 +548,12 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         uint64_t grid = (uint64_t)num_sms * per_sm;
         const uint64_t need = (a.total_items + warps_per_cta - 1) / warps_per_cta;
         if (grid > need) grid = need;
-        trace_kernel<<<(unsigned)grid, threads, 0, stream>>>(a);
+        launch_k(trace_kernel, (unsigned)grid, threads, 0, stream, pdl, a);
         launches++;
     }
     if (ev) cudaEventRecord(ev[2], stream);
-    if (a.mode == CPD_TRACE_FP64) retrace_exact_kernel<<<(unsigned)(num_sms * 8), 32, 0, stream>>>(a);
-    else retrace_kernel<<<(unsigned)(num_sms * 8), 32, 0, stream>>>(a);
+    launch_k(a.mode == CPD_TRACE_FP64 ? retrace_exact_kernel : retrace_kernel, (unsigned)(num_sms * 8), 32, 0, stream,
+             pdl, a);
     launches++;
     if (ev) cudaEventRecord(ev[3], stream);
     if (a.total_tiles) {
@@ -530,10 +564,10 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         const uint64_t wpb = (uint64_t)kEntropyThreads / 32u;
         uint64_t grid = (a.total_tiles + wpb - 1) / wpb;
         if (grid > (uint64_t)num_sms * per_sm) grid = (uint64_t)num_sms * per_sm;
-        entropy_kernel<<<(unsigned)grid, kEntropyThreads, 0, stream>>>(a);
+        launch_k(entropy_kernel, (unsigned)grid, kEntropyThreads, 0, stream, pdl, a);
         launches++;
     }
-    finalize_kernel<<<(a.njobs + 3u) / 4u, 128, 0, stream>>>(a);
+    launch_k(finalize_kernel, (a.njobs + 3u) / 4u, 128, 0, stream, pdl, a);
     launches++;
     if (ev) cudaEventRecord(ev[4], stream);
     return launches;

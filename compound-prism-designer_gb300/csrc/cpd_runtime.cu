@@ -346,7 +346,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     std::memcpy(key.data() + sizeof(a), extra, sizeof(extra));
     auto record = [&](cudaStream_t st) -> int {
         cudaMemsetAsync(S.ctl.p, 0, sizeof(Control), st);
-        const int l = launch_pass(a, ctx->num_sms, ctx->warps_per_cta, st, profile ? S.kev : nullptr);
+        const int l = launch_pass(a, ctx->num_sms, ctx->warps_per_cta, st, profile ? S.kev : nullptr, true);
         cudaMemcpyAsync(S.h_out.p, S.out.p, sizeof(DesignOut) * n, cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(S.h_ctl.p, S.ctl.p, sizeof(Control), cudaMemcpyDeviceToHost, st);
         return l;
