@@ -97,8 +97,11 @@ struct PassSlot {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
     cudaEvent_t kev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    DevBuf designs, jobs, lam_u, z64, z32, lp, lx, hist, S1, S2, acc, out, ctl, queue, pout;
-    HostBuf h_designs, h_jobs, h_lam, h_z64, h_z32, h_out, h_ctl;
+    // inputs (designs, jobs, wavelength points, ray tables) in one arena, uploaded with one
+    // copy; outputs (DesignOut[n] then Control) in one buffer, read back with one copy
+    DevBuf in, lp, lx, hist, S1, S2, acc, outs, queue, pout;
+    HostBuf h_in, h_outs;
+    size_t ctl_off = 0;
     bool hist_dirty = true;
     uint32_t qcap = 1u << 18;
     std::vector<uint8_t> graph_key;
@@ -128,10 +131,8 @@ struct PassSlot {
         if (stream) cudaStreamSynchronize(stream);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
-        for (DevBuf *b : {&designs, &jobs, &lam_u, &z64, &z32, &lp, &lx, &hist, &S1, &S2, &acc, &out, &ctl, &queue,
-                          &pout})
-            b->release();
-        for (HostBuf *b : {&h_designs, &h_jobs, &h_lam, &h_z64, &h_z32, &h_out, &h_ctl}) b->release();
+        for (DevBuf *b : {&in, &lp, &lx, &hist, &S1, &S2, &acc, &outs, &queue, &pout}) b->release();
+        for (HostBuf *b : {&h_in, &h_outs}) b->release();
         for (cudaEvent_t *ev : {&ev0, &ev1, &done, &kev[0], &kev[1], &kev[2], &kev[3], &kev[4]})
             if (*ev) cudaEventDestroy(*ev), *ev = nullptr;
         if (stream) cudaStreamDestroy(stream);
@@ -150,13 +151,14 @@ struct cpd_context {
     std::mutex mu;        // serialises the synchronous entry points (main slot)
     std::mutex cache_mu;  // ray-table cache
     PassSlot main;
-    DevBuf pair_lam, pair_z, pair_bins, pair_ts, pair_flags, peak, logtab;
+    DevBuf pair_design, pair_lam, pair_z, pair_bins, pair_ts, pair_flags, peak, logtab;
     uint32_t ray_tile = 32;
     uint32_t warps_per_cta = 8;
     bool profiling = false;
     bool use_graphs = true;
     bool autotune = false;
     std::map<RayKey, RayTablePtr> ray_cache;
+    std::map<RayKey, std::shared_ptr<const std::vector<double>>> lam_cache;  // wavelength u-points per (seed, W)
     // launch shape picked by the autotuner per class of batch
     std::map<std::array<uint64_t, 5>, std::pair<uint32_t, uint32_t>> tune_cache;
 };
@@ -186,6 +188,25 @@ RayTablePtr ray_table_cached(cpd_context *ctx, double seed, uint32_t R)
     std::lock_guard<std::mutex> lk(ctx->cache_mu);
     if (ctx->ray_cache.size() > 256) ctx->ray_cache.clear();
     return ctx->ray_cache.emplace(key, t).first->second;
+}
+
+// The wavelength u-points of the GPU seed policy, u_i = fract(fma(i, 1/phi, seed)),
+// cached per (seed, W) like the ray tables (an optimizer reuses its seeds).
+std::shared_ptr<const std::vector<double>> lam_points_cached(cpd_context *ctx, double seed, uint32_t W)
+{
+    uint64_t bits;
+    std::memcpy(&bits, &seed, 8);
+    RayKey key{bits, W};
+    {
+        std::lock_guard<std::mutex> lk(ctx->cache_mu);
+        auto it = ctx->lam_cache.find(key);
+        if (it != ctx->lam_cache.end()) return it->second;
+    }
+    auto v = std::make_shared<std::vector<double>>(W);
+    seed_points(seed, 0, W, v->data());
+    std::lock_guard<std::mutex> lk(ctx->cache_mu);
+    if (ctx->lam_cache.size() > 256) ctx->lam_cache.clear();
+    return ctx->lam_cache.emplace(key, v).first->second;
 }
 
 // One design's sampling inputs for a pass.
@@ -252,30 +273,32 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         items += (uint64_t)((J.W + 31) / 32) * J.nchunk;
         tiles += J.ntiles;
     }
-    // staging
-    CPD_TRY(S.h_designs.ensure(sizeof(DevDesign) * n));
-    CPD_TRY(S.h_jobs.ensure(sizeof(DesignJob) * n));
-    CPD_TRY(S.h_lam.ensure(sizeof(double) * std::max<uint64_t>(lam, 1)));
-    CPD_TRY(S.h_z64.ensure(sizeof(double) * std::max<uint64_t>(ray, 1)));
-    CPD_TRY(S.h_z32.ensure(2 * sizeof(float) * std::max<uint64_t>(ray, 1)));
-    CPD_TRY(S.h_out.ensure(sizeof(DesignOut) * n));
-    CPD_TRY(S.h_ctl.ensure(sizeof(Control)));
+    // one input arena: designs | jobs | wavelength points | z64 | z32 (256-byte sections)
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t o_job = al(sizeof(DevDesign) * n);
+    const size_t o_lam = o_job + al(sizeof(DesignJob) * n);
+    const size_t o_z64 = o_lam + al(sizeof(double) * lam);
+    const size_t o_z32 = o_z64 + al(sizeof(double) * ray);
+    const size_t in_bytes = o_z32 + al(2 * sizeof(float) * ray);
+    const size_t ctl_off = al(sizeof(DesignOut) * n);
+    const size_t out_bytes = ctl_off + sizeof(Control);
+    CPD_TRY(S.h_in.ensure(in_bytes));
+    CPD_TRY(S.h_outs.ensure(out_bytes));
+    char *hin = S.h_in.as<char>();
     for (uint32_t i = 0; i < n; i++) {
-        S.h_designs.as<DevDesign>()[i] = *ds[i].dev;
-        S.h_jobs.as<DesignJob>()[i] = jobs[i];
-        std::memcpy(S.h_lam.as<double>() + jobs[i].lam_off, ds[i].lam_u, sizeof(double) * ds[i].W);
+        reinterpret_cast<DevDesign *>(hin)[i] = *ds[i].dev;
+        reinterpret_cast<DesignJob *>(hin + o_job)[i] = jobs[i];
+        std::memcpy(reinterpret_cast<double *>(hin + o_lam) + jobs[i].lam_off, ds[i].lam_u, sizeof(double) * ds[i].W);
         if (!owns_rays[i]) continue;
-        std::memcpy(S.h_z64.as<double>() + jobs[i].ray_off, ds[i].rays->z64.data(), sizeof(double) * jobs[i].Rz);
-        std::memcpy(S.h_z32.as<float>() + 2 * jobs[i].ray_off, ds[i].rays->z32.data(), 2 * sizeof(float) * jobs[i].Rz);
+        std::memcpy(reinterpret_cast<double *>(hin + o_z64) + jobs[i].ray_off, ds[i].rays->z64.data(),
+                    sizeof(double) * jobs[i].Rz);
+        std::memcpy(reinterpret_cast<float *>(hin + o_z32) + 2 * jobs[i].ray_off, ds[i].rays->z32.data(),
+                    2 * sizeof(float) * jobs[i].Rz);
     }
     // device buffers
     const size_t hist_bytes = sizeof(unsigned long long) * std::max<uint64_t>(hist, 1);
     const size_t old_hist = S.hist.cap;
-    CPD_TRY(S.designs.ensure(sizeof(DevDesign) * n));
-    CPD_TRY(S.jobs.ensure(sizeof(DesignJob) * n));
-    CPD_TRY(S.lam_u.ensure(sizeof(double) * std::max<uint64_t>(lam, 1)));
-    CPD_TRY(S.z64.ensure(sizeof(double) * std::max<uint64_t>(ray, 1)));
-    CPD_TRY(S.z32.ensure(2 * sizeof(float) * std::max<uint64_t>(ray, 1)));
+    CPD_TRY(S.in.ensure(in_bytes));
     CPD_TRY(S.lp.ensure(sizeof(LamParams) * std::max<uint64_t>(rows, 1)));
     CPD_TRY(S.lx.ensure(sizeof(LamDF) * std::max<uint64_t>(rows, 1)));
     CPD_TRY(S.hist.ensure(hist_bytes));
@@ -283,48 +306,45 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     CPD_TRY(S.S1.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
     CPD_TRY(S.S2.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
     CPD_TRY(S.acc.ensure(sizeof(DesignAcc) * n));
-    CPD_TRY(S.out.ensure(sizeof(DesignOut) * n));
-    CPD_TRY(S.ctl.ensure(sizeof(Control)));
+    CPD_TRY(S.outs.ensure(out_bytes));
     CPD_TRY(S.queue.ensure(sizeof(QEntry) * S.qcap));
     if (p_out_host) CPD_TRY(S.pout.ensure(hist_bytes));
+    S.ctl_off = ctl_off;
 
     cudaStream_t s = S.stream;
     if (S.hist_dirty) {
         CPD_TRY(cudaMemsetAsync(S.hist.p, 0, S.hist.cap, s));
         S.hist_dirty = false;
     }
-    CPD_TRY(cudaMemcpyAsync(S.designs.p, S.h_designs.p, sizeof(DevDesign) * n, cudaMemcpyHostToDevice, s));
-    CPD_TRY(cudaMemcpyAsync(S.jobs.p, S.h_jobs.p, sizeof(DesignJob) * n, cudaMemcpyHostToDevice, s));
-    CPD_TRY(cudaMemcpyAsync(S.lam_u.p, S.h_lam.p, sizeof(double) * lam, cudaMemcpyHostToDevice, s));
-    CPD_TRY(cudaMemcpyAsync(S.z64.p, S.h_z64.p, sizeof(double) * ray, cudaMemcpyHostToDevice, s));
-    CPD_TRY(cudaMemcpyAsync(S.z32.p, S.h_z32.p, 2 * sizeof(float) * ray, cudaMemcpyHostToDevice, s));
-    S.h2d += sizeof(DevDesign) * n + sizeof(DesignJob) * n + sizeof(double) * lam + (sizeof(double) + 2 * sizeof(float)) * ray;
-    S.d2h += sizeof(DesignOut) * n + sizeof(Control) + (p_out_host ? sizeof(double) * hist : 0);
+    CPD_TRY(cudaMemcpyAsync(S.in.p, S.h_in.p, in_bytes, cudaMemcpyHostToDevice, s));
+    S.h2d += in_bytes;
+    S.d2h += out_bytes + (p_out_host ? sizeof(double) * hist : 0);
     if (fresh) {
         CPD_TRY(cudaMemsetAsync(S.S1.p, 0, sizeof(unsigned long long) * accc, s));
         CPD_TRY(cudaMemsetAsync(S.S2.p, 0, sizeof(unsigned long long) * accc, s));
         CPD_TRY(cudaMemsetAsync(S.acc.p, 0, sizeof(DesignAcc) * n, s));
     }
+    char *din = S.in.as<char>();
 
     LaunchArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.designs = S.designs.as<DevDesign>();
-    a.jobs = S.jobs.as<DesignJob>();
+    a.designs = reinterpret_cast<const DevDesign *>(din);
+    a.jobs = reinterpret_cast<const DesignJob *>(din + o_job);
     a.njobs = n;
     a.total_rows = rows;
     a.total_items = items;
     a.total_tiles = tiles;
-    a.lam_u = S.lam_u.as<double>();
-    a.z64 = S.z64.as<double>();
-    a.z32 = S.z32.as<float>();
+    a.lam_u = reinterpret_cast<const double *>(din + o_lam);
+    a.z64 = reinterpret_cast<const double *>(din + o_z64);
+    a.z32 = reinterpret_cast<const float *>(din + o_z32);
     a.lp = S.lp.as<LamParams>();
     a.lx = S.lx.as<LamDF>();
     a.hist = S.hist.as<unsigned long long>();
     a.S1 = S.S1.as<unsigned long long>();
     a.S2 = S.S2.as<unsigned long long>();
     a.acc = S.acc.as<DesignAcc>();
-    a.out = S.out.as<DesignOut>();
-    a.ctl = S.ctl.as<Control>();
+    a.out = S.outs.as<DesignOut>();
+    a.ctl = reinterpret_cast<Control *>(S.outs.as<char>() + ctl_off);
     a.queue = S.queue.as<QEntry>();
     a.qcap = S.qcap;
     a.ray_tile = ctx->ray_tile;
@@ -345,10 +365,9 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     const uint32_t extra[3] = {n, ctx->warps_per_cta, (uint32_t)ctx->num_sms};
     std::memcpy(key.data() + sizeof(a), extra, sizeof(extra));
     auto record = [&](cudaStream_t st) -> int {
-        cudaMemsetAsync(S.ctl.p, 0, sizeof(Control), st);
+        cudaMemsetAsync(a.ctl, 0, sizeof(Control), st);
         const int l = launch_pass(a, ctx->num_sms, ctx->warps_per_cta, st, profile ? S.kev : nullptr, true);
-        cudaMemcpyAsync(S.h_out.p, S.out.p, sizeof(DesignOut) * n, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(S.h_ctl.p, S.ctl.p, sizeof(Control), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(S.h_outs.p, S.outs.p, out_bytes, cudaMemcpyDeviceToHost, st);
         return l;
     };
     CPD_TRY(cudaEventRecord(S.ev0, s));
@@ -395,10 +414,10 @@ int pass_finish(PassSlot &S, PassResult &res)
             cudaEventElapsedTime(&km, S.kev[i], S.kev[i + 1]);
             S.kernel_ms[i] = km;
         }
-    const Control *c = S.h_ctl.as<Control>();
+    const Control *c = reinterpret_cast<const Control *>(S.h_outs.as<char>() + S.ctl_off);
     res.overflow = c->overflow != 0 || c->queue_count > S.qcap;
     if (res.overflow) S.hist_dirty = true;
-    res.outs.assign(S.h_out.as<DesignOut>(), S.h_out.as<DesignOut>() + S.n);
+    res.outs.assign(S.h_outs.as<DesignOut>(), S.h_outs.as<DesignOut>() + S.n);
     return CPD_OK;
 }
 
@@ -739,8 +758,8 @@ void cpd_context_destroy(cpd_context *ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     ctx->main.destroy();
-    for (DevBuf *b : {&ctx->pair_lam, &ctx->pair_z, &ctx->pair_bins, &ctx->pair_ts, &ctx->pair_flags, &ctx->peak,
-                      &ctx->logtab})
+    for (DevBuf *b : {&ctx->pair_design, &ctx->pair_lam, &ctx->pair_z, &ctx->pair_bins, &ctx->pair_ts,
+                      &ctx->pair_flags, &ctx->peak, &ctx->logtab})
         b->release();
     delete ctx;
 }
@@ -831,13 +850,12 @@ int cpd_fitness_gpu(cpd_context *ctx, const cpd_design *d, const double *seeds, 
     if (!tune && nwarp >= 1 && nwarp <= 8) ctx->warps_per_cta = nwarp;
     DevDesign D;
     design_to_dev(*d, D);
-    std::vector<double> lam(max_n);
     PassResult res;
     uint64_t rays = 0;
     for (uint32_t s = 0; s < nseeds; s++) {
-        seed_points(seeds[s], 0, max_n, lam.data());
+        const auto lam = lam_points_cached(ctx, seeds[s], max_n);
         RayTablePtr rt = ray_table_cached(ctx, seeds[s], max_eval);
-        std::vector<PassDesign> ds{PassDesign{&D, max_n, max_eval, lam.data(), rt.get()}};
+        std::vector<PassDesign> ds{PassDesign{&D, max_n, max_eval, lam->data(), rt.get()}};
         if (tune && s == 0) {
             // the autotuner replaces the reference's nwarp hint
             auto it = ctx->tune_cache.find(tune_class(ds, CPD_TRACE_HYBRID));
@@ -949,17 +967,17 @@ int cpd_trace_rays(cpd_context *ctx, const cpd_design *d, const double *lam_u, c
     std::vector<double> z(n);
     for (uint32_t i = 0; i < n; i++) z[i] = norminv(ray_u[i]);
     cudaStream_t s = S.stream;
-    CPD_TRY(S.designs.ensure(sizeof(DevDesign)));
+    CPD_TRY(ctx->pair_design.ensure(sizeof(DevDesign)));
     CPD_TRY(ctx->pair_lam.ensure(sizeof(double) * n));
     CPD_TRY(ctx->pair_z.ensure(sizeof(double) * n));
     CPD_TRY(ctx->pair_bins.ensure(sizeof(uint32_t) * n));
     CPD_TRY(ctx->pair_ts.ensure(sizeof(double) * n));
     CPD_TRY(ctx->pair_flags.ensure(n));
-    CPD_TRY(cudaMemcpyAsync(S.designs.p, &D, sizeof(DevDesign), cudaMemcpyHostToDevice, s));
+    CPD_TRY(cudaMemcpyAsync(ctx->pair_design.p, &D, sizeof(DevDesign), cudaMemcpyHostToDevice, s));
     CPD_TRY(cudaMemcpyAsync(ctx->pair_lam.p, lam_u, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     CPD_TRY(cudaMemcpyAsync(ctx->pair_z.p, z.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
     CPD_TRY(cudaEventRecord(S.ev0, s));
-    launch_trace_pairs(S.designs.as<DevDesign>(), ctx->pair_lam.as<double>(), ctx->pair_z.as<double>(), n,
+    launch_trace_pairs(ctx->pair_design.as<DevDesign>(), ctx->pair_lam.as<double>(), ctx->pair_z.as<double>(), n,
                        trace_mode, ctx->pair_bins.as<uint32_t>(), ctx->pair_ts.as<double>(),
                        ctx->pair_flags.as<uint8_t>(), s);
     CPD_TRY(cudaGetLastError());
