@@ -104,6 +104,9 @@ struct LaunchArgs {
 int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaStream_t stream,
                 cudaEvent_t *ev = nullptr, bool pdl = false);
 
+// Warps of the trace kernel resident at once with this block shape.
+uint64_t trace_resident_warps(int num_sms, uint32_t warps_per_cta);
+
 // One thread per (lam_u[i], z[i]) pair: the twin of propagation_test_kernel.
 void launch_trace_pairs(const DevDesign *d, const double *lam_u, const double *z64, uint32_t n, uint32_t mode,
                         uint32_t *bins, double *ts, uint8_t *flags, cudaStream_t stream);

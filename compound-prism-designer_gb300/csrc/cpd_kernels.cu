@@ -573,6 +573,14 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     return launches;
 }
 
+uint64_t trace_resident_warps(int num_sms, uint32_t warps_per_cta)
+{
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel, (int)warps_per_cta * 32, 0);
+    if (per_sm < 1) per_sm = 1;
+    return (uint64_t)num_sms * (uint64_t)per_sm * warps_per_cta;
+}
+
 void launch_trace_pairs(const DevDesign *d, const double *lam_u, const double *z64, uint32_t n, uint32_t mode,
                         uint32_t *bins, double *ts, uint8_t *flags, cudaStream_t stream)
 {

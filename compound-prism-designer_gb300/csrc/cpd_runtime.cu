@@ -497,8 +497,25 @@ int tune_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode
     double best = 1e300;
     uint32_t brt = rt0, bw = w0;
     PassResult res;
-    for (uint32_t rt : kTiles)
-        for (uint32_t w : kWarps) {
+    // Besides the powers of two: tiles that make the work items a whole number of rounds
+    // of the resident warps (2..6 items per warp), so that the last round is not a tail.
+    std::vector<std::pair<uint32_t, uint32_t>> cands;
+    for (uint32_t w : kWarps) {
+        for (uint32_t rt : kTiles) cands.push_back({rt, w});
+        uint64_t blocks = 0, rays = 0;
+        for (const PassDesign &p : ds) {
+            blocks += (p.W + 31) / 32;
+            rays += (uint64_t)((p.W + 31) / 32) * p.rays->z64.size();
+        }
+        const uint64_t warps = trace_resident_warps(ctx->num_sms, w);
+        for (uint64_t k = 2; k <= 6 && blocks; k++) {
+            const uint64_t per = (rays + k * warps - 1) / (k * warps);  // rays per item
+            if (per >= 2 && per <= 4096) cands.push_back({(uint32_t)per, w});
+        }
+    }
+    for (const auto &cw : cands) {
+        const uint32_t rt = cw.first, w = cw.second;
+        {
             ctx->ray_tile = rt;
             ctx->warps_per_cta = w;
             double m = 1e300;
@@ -517,6 +534,7 @@ int tune_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode
                 bw = w;
             }
         }
+    }
     ctx->ray_tile = brt;
     ctx->warps_per_cta = bw;
     ctx->tune_cache[tune_class(ds, mode)] = {brt, bw};

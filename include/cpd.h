@@ -238,7 +238,8 @@ int cpd_get_launch_shape(cpd_context *ctx, uint32_t *ray_tile, uint32_t *warps_p
 
 /* The project's launch-shape autotuner (no reference counterpart; the reference takes
  * a fixed nwarp hint, src/pylib.rs:1088). Times the batch with every ray tile in
- * {4, 8, 16, 32, 64, 128, 256} and warps per CTA in {2, 4, 8} (captured graph, minimum of two
+ * {4, 8, 16, 32, 64, 128, 256}, plus the tiles that split the work into 2..6 whole rounds of
+ * the resident warps, and warps per CTA in {2, 4, 8} (captured graph, minimum of two
  * timed passes each), sets the fastest on the context and remembers it for the batch's
  * class: trace mode and the binary orders of magnitude of its design count, wavelength
  * rows, rays and widest detector. Results do not depend on the shape. */
