@@ -205,6 +205,8 @@ def serving_form(ctx, generations=200):
     optimizer's gpu_fitness sampling), once with batches submitted back to back
     (capacity) and once as a Poisson process at 70% of that capacity (latency). Beside
     it, the plain one-design call on the same sampling."""
+    import ctypes as C
+
     import numpy as np
     import compound_prism_designer as cpd
     from compound_prism_designer import _native as N
@@ -228,6 +230,17 @@ def serving_form(ctx, generations=200):
         N.lib.cpd_fitness_gpu(ctx.handle, x, seeds.ctypes.data_as(N._dp), 1, W, 2, R, f)
     plain = len(dd) / (time.perf_counter() - t0)
     out["plain_designs_per_s"] = plain
+    # the server's passes hold up to 256 designs of this sampling: tune the launch shape on
+    # such a pass (the server uses the context's shape) and time it alone
+    n_b = min(256, len(dd))
+    darr = (N.Design * n_b)(*dd[:n_b])
+    items = (N.BatchItem * n_b)()
+    for i in range(n_b):
+        items[i].seed, items[i].max_n, items[i].max_eval = 0.5, W, R
+    rt_, w_, ms_ = C.c_uint32(0), C.c_uint32(0), C.c_double(0.0)
+    N.lib.cpd_autotune_batch(ctx.handle, darr, items, n_b, 0, C.byref(rt_), C.byref(w_), C.byref(ms_))
+    out["pass_shape"] = {"ray_tile": rt_.value, "warps_per_cta": w_.value}
+    out["gpu_pass_designs_per_s"] = n_b / (ms_.value * 1e-3)
     with cpd.Server(mem_budget_bytes=8 << 30, slots=2, max_designs_per_pass=256, context=ctx) as sv:
         gen.serve(sv, generations=5, seed=1)  # warm-up: buffers, caches
         # the server alone: 64 requests of 1024 pre-built designs submitted at once
