@@ -40,7 +40,7 @@ struct Control {
     unsigned long long item_counter;
     unsigned long long queue_count;
     unsigned int overflow;
-    unsigned int pad;
+    unsigned int tiles_done;  // entropy tiles finished (single-design passes)
 };
 
 // Copies of each per-design ray counter: thousands of warps add to the counters of one

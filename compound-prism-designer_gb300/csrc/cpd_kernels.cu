@@ -402,6 +402,18 @@ __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const Launc
         else entropy_tile<1>(a, J, r0, r1, lane, tab, h);
         const unsigned long long hl = warp_sum_u64(__double2ull_rn(-((double)h.hi + (double)h.lo) * kHScale));
         if (lane == 0 && hl) atomicAdd(&a.acc[d].H, hl);
+        if (a.njobs == 1) {
+            // a single design (the plain call): the warp that finishes its last tile runs
+            // the finalize, which saves a launch; with many designs the per-tile fences
+            // would cost more than the separate finalize kernel
+            __threadfence();
+            unsigned last = 0;
+            if (lane == 0) last = atomicAdd(&a.ctl->tiles_done, 1u) == J.ntiles - 1u ? 1u : 0u;
+            if (__shfl_sync(0xffffffffu, last, 0)) {
+                __threadfence();
+                finalize_warp(a, d, J, lane, tab);
+            }
+        }
     }
 }
 
@@ -567,8 +579,10 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         launch_k(entropy_kernel, (unsigned)grid, kEntropyThreads, 0, stream, pdl, a);
         launches++;
     }
-    launch_k(finalize_kernel, (a.njobs + 3u) / 4u, 128, 0, stream, pdl, a);
-    launches++;
+    if (a.njobs > 1 || !a.total_tiles) {
+        launch_k(finalize_kernel, (a.njobs + 3u) / 4u, 128, 0, stream, pdl, a);
+        launches++;
+    }
     if (ev) cudaEventRecord(ev[4], stream);
     return launches;
 }
