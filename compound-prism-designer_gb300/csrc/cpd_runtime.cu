@@ -316,14 +316,8 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         CPD_TRY(cudaMemsetAsync(S.hist.p, 0, S.hist.cap, s));
         S.hist_dirty = false;
     }
-    CPD_TRY(cudaMemcpyAsync(S.in.p, S.h_in.p, in_bytes, cudaMemcpyHostToDevice, s));
     S.h2d += in_bytes;
     S.d2h += out_bytes + (p_out_host ? sizeof(double) * hist : 0);
-    if (fresh) {
-        CPD_TRY(cudaMemsetAsync(S.S1.p, 0, sizeof(unsigned long long) * accc, s));
-        CPD_TRY(cudaMemsetAsync(S.S2.p, 0, sizeof(unsigned long long) * accc, s));
-        CPD_TRY(cudaMemsetAsync(S.acc.p, 0, sizeof(DesignAcc) * n, s));
-    }
     char *din = S.in.as<char>();
 
     LaunchArgs a;
@@ -360,24 +354,36 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     a.logtab = ctx->logtab.as<float>();
 
     // The device work of a pass, captured once per signature and replayed.
-    std::vector<uint8_t> key(sizeof(a) + 3 * sizeof(uint32_t));
+    // The whole pass -- input upload, accumulator clears, kernels, read-back, and the two
+    // timing events around the kernels -- is one graph, captured once per signature.
+    std::vector<uint8_t> key(sizeof(a) + 6 * sizeof(uint64_t));
     std::memcpy(key.data(), &a, sizeof(a));
-    const uint32_t extra[3] = {n, ctx->warps_per_cta, (uint32_t)ctx->num_sms};
+    const uint64_t extra[6] = {n, ctx->warps_per_cta, (uint64_t)ctx->num_sms, in_bytes, out_bytes,
+                               fresh ? accc + 1 : 0};
     std::memcpy(key.data() + sizeof(a), extra, sizeof(extra));
-    auto record = [&](cudaStream_t st) -> int {
+    auto record = [&](cudaStream_t st, bool capturing) -> int {
+        const unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+        cudaMemcpyAsync(S.in.p, S.h_in.p, in_bytes, cudaMemcpyHostToDevice, st);
+        if (fresh) {
+            cudaMemsetAsync(S.S1.p, 0, sizeof(unsigned long long) * accc, st);
+            cudaMemsetAsync(S.S2.p, 0, sizeof(unsigned long long) * accc, st);
+            cudaMemsetAsync(S.acc.p, 0, sizeof(DesignAcc) * n, st);
+        }
         cudaMemsetAsync(a.ctl, 0, sizeof(Control), st);
+        // External: under stream capture these become event-record nodes of the graph
+        cudaEventRecordWithFlags(S.ev0, st, evf);
         const int l = launch_pass(a, ctx->num_sms, ctx->warps_per_cta, st, profile ? S.kev : nullptr, true);
+        cudaEventRecordWithFlags(S.ev1, st, evf);
         cudaMemcpyAsync(S.h_outs.p, S.outs.p, out_bytes, cudaMemcpyDeviceToHost, st);
         return l;
     };
-    CPD_TRY(cudaEventRecord(S.ev0, s));
     if (use_graph && !profile) {
         if (!S.graph_exec || key != S.graph_key) {
             if (S.graph_exec) cudaGraphExecDestroy(S.graph_exec);
             S.graph_exec = nullptr;
             cudaGraph_t g = nullptr;
             CPD_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            S.graph_launches = record(s);
+            S.graph_launches = record(s, true);
             CPD_TRY(cudaStreamEndCapture(s, &g));
             const cudaError_t e = cudaGraphInstantiate(&S.graph_exec, g, 0);
             cudaGraphDestroy(g);
@@ -387,10 +393,9 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         CPD_TRY(cudaGraphLaunch(S.graph_exec, s));
         S.launches = S.graph_launches;
     } else {
-        S.launches = record(s);
+        S.launches = record(s, false);
         CPD_TRY(cudaGetLastError());
     }
-    CPD_TRY(cudaEventRecord(S.ev1, s));
     if (p_out_host)
         CPD_TRY(cudaMemcpyAsync(p_out_host, S.pout.p, sizeof(double) * hist, cudaMemcpyDeviceToHost, s));
     CPD_TRY(cudaEventRecord(S.done, s));
