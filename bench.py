@@ -326,7 +326,8 @@ def plain_config(l2):
     return {"workload": f"plain gpu_fitness call, one design per call: {G_PLAIN} prisms, {B_PLAIN} bins, "
                         f"{W_PLAIN} wavelengths x {R_PLAIN} rays ({W_PLAIN * R_PLAIN} rays)",
             "prisms": G_PLAIN, "bins": B_PLAIN, "wavelengths": W_PLAIN, "rays_per_wavelength": R_PLAIN,
-            "trace": "fp32 with exact-f64 guard-band re-trace", "accumulation": "int64 fixed point + f64 entropy",
+            "trace": "fp32 fast path; guard-band rays re-traced in float-float",
+            "accumulation": "int64 fixed point; float-float entropy",
             "l2": l2}
 
 
