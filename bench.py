@@ -6,7 +6,8 @@ with FP64/int64 accumulation and entropy. A step is one gpu_fitness call of one
 design. Also measured on the same run, under "forms": the batched population form
 (1024 designs of mixed G, B, W in one captured launch sequence) and the serving form
 (a continuous-batching server fed by a synthetic generational optimizer: designs/s,
-p50/p99 request latency).
+p50/p99 request latency), and adaptive sampling (the reference kernel's per-wavelength SEM
+stop) beside fixed N at the reference optimizer's sampling.
 
   value   designs/s with inputs resident on the device: 1 / (device time of the pass)
   e2e     designs/s through the C ABI with host buffers (design + point tables H2D,
@@ -197,6 +198,48 @@ def cpu_oracle_rate(d, W, R, target_s=10.0, nthreads=None):
     return {"value": rate, "unit": "designs/s", "cores": nthreads, "kind": "port",
             "sample": f"{done} wavelength rows ({done / W:.2f} designs) x {R} rays of the benchmark design "
                       f"({done * R} rays, {dt:.1f} s, {nthreads} threads)"}
+
+
+def adaptive_form(ctx, n=256):
+    """Adaptive sampling (the reference kernel's per-wavelength SEM stop) at the reference
+    optimizer's sampling, 128 wavelengths x up to 8192 rays: the plain call over n
+    generation-0 designs and the same designs as one batched pass, each beside fixed N."""
+    import numpy as np
+    from compound_prism_designer import _native as N
+    from compound_prism_designer import generations as gen
+
+    W, R = 128, 8192
+    rng = np.random.default_rng(11)
+    cat = gen.glass_catalog(rng, 64)
+    pop = gen.initial_population(rng, n, cat)
+    designs, ok = gen.build(pop, cat)
+    dd = [N.Design.from_buffer_copy(designs[i].tobytes()) for i in range(len(designs))]
+    nb = len(dd)
+    darr = (N.Design * nb)(*dd)
+    items = (N.BatchItem * nb)()
+    for i in range(nb):
+        items[i].seed, items[i].max_n, items[i].max_eval = 0.5, W, R
+    outs = (N.Fitness * nb)()
+    seeds = np.array([0.5])
+    f = N.Fitness()
+    out = {"workload": f"{nb} designs (G in 2..6, B in 16..128), {W} wavelengths x up to {R} rays, seed 0.5"}
+    for name, sampling in (("fixed", 0), ("adaptive", N.SAMPLING_ADAPTIVE)):
+        for x in dd[:4]:
+            N.lib.cpd_fitness_gpu_ex(ctx.handle, x, seeds.ctypes.data_as(N._dp), 1, W, 2, R, sampling, f)
+        rays = 0
+        t0 = time.perf_counter()
+        for x in dd:
+            N.lib.cpd_fitness_gpu_ex(ctx.handle, x, seeds.ctypes.data_as(N._dp), 1, W, 2, R, sampling, f)
+            rays += f.rays
+        out[f"plain_{name}_designs_per_s"] = nb / (time.perf_counter() - t0)
+        out[f"plain_{name}_rays_fraction"] = rays / (nb * W * R)
+        ms = []
+        for _ in range(4):
+            N.lib.cpd_fitness_gpu_batch(ctx.handle, darr, items, nb, N.TRACE_HYBRID | sampling, outs)
+            ms.append(ctx.last_timing()[0])
+        out[f"batch_{name}_ms_device"] = min(ms[1:])
+        out[f"batch_{name}_designs_per_s_device"] = nb / (min(ms[1:]) / 1e3)
+    return out
 
 
 def serving_form(ctx, generations=200):
@@ -460,6 +503,10 @@ def main():
             extras.setdefault("forms", {})["serving"] = serving_form(ctx)
         except Exception as e:  # noqa: BLE001
             extras.setdefault("forms", {})["serving"] = {"error": repr(e)}
+        try:
+            extras.setdefault("forms", {})["adaptive"] = adaptive_form(ctx)
+        except Exception as e:  # noqa: BLE001
+            extras.setdefault("forms", {})["adaptive"] = {"error": repr(e)}
         try:
             extras["cpu_baseline"] = cpu_oracle_rate(d, W_PLAIN, R_PLAIN)
         except Exception as e:  # noqa: BLE001

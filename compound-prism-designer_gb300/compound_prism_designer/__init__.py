@@ -26,11 +26,16 @@ __all__ = [
     "UniformWavelengthDistribution", "GaussianBeam", "FiberBeam", "CompoundPrism",
     "position_detector_array", "DetectorArray", "Spectrometer", "Context", "default_context",
     "fitness_batch", "autotune_batch", "build_designs", "Server", "TRACE_HYBRID", "TRACE_FP32", "TRACE_FP64",
+    "SAMPLING_ADAPTIVE", "SAMPLING_EXACT",
 ]
 
 TRACE_HYBRID = N.TRACE_HYBRID
 TRACE_FP32 = N.TRACE_FP32
 TRACE_FP64 = N.TRACE_FP64
+# OR into a trace mode (TRACE_HYBRID | SAMPLING_ADAPTIVE), or pass adaptive=True to
+# gpu_fitness: the reference kernel's per-wavelength SEM stop (src/spectrometer/kernel.rs:127-178)
+SAMPLING_ADAPTIVE = N.SAMPLING_ADAPTIVE
+SAMPLING_EXACT = N.SAMPLING_EXACT
 
 
 class RayTraceError(Exception):
@@ -451,25 +456,34 @@ class Spectrometer:
         return DesignFitness(f.size, f.info, f.deviation)
 
     def gpu_fitness(self, seeds, *, max_n: int = 256, nwarp: int = 2, max_eval: int = 16_384,
-                    context: Optional[Context] = None) -> Optional[DesignFitness]:
-        """GPU fitness (src/pylib.rs:1085-1135): None if the SEM stop was not met."""
-        f = self.gpu_fitness_full(seeds, max_n=max_n, nwarp=nwarp, max_eval=max_eval, context=context)
+                    adaptive: bool = False, context: Optional[Context] = None) -> Optional[DesignFitness]:
+        """GPU fitness (src/pylib.rs:1085-1135): None if the SEM stop was not met.
+        adaptive: each wavelength stops at the reference kernel's per-wavelength SEM test
+        (src/spectrometer/kernel.rs:127-178) instead of using all max_eval rays."""
+        f = self.gpu_fitness_full(seeds, max_n=max_n, nwarp=nwarp, max_eval=max_eval, adaptive=adaptive,
+                                  context=context)
         if f.status == N.NOT_CONVERGED:
             return None
         return DesignFitness(f.size, f.info, f.deviation)
 
     def gpu_fitness_full(self, seeds, *, max_n: int = 256, nwarp: int = 2, max_eval: int = 16_384,
-                         context: Optional[Context] = None) -> N.Fitness:
+                         adaptive: bool = False, context: Optional[Context] = None) -> N.Fitness:
         seeds = np.ascontiguousarray(np.atleast_1d(seeds), dtype=np.float64)
         ctx = context or default_context()
         f = N.Fitness()
-        _check(N.lib.cpd_fitness_gpu(ctx.handle, C.byref(self.design), _dp(seeds), seeds.size, int(max_n),
-                                     int(nwarp), int(max_eval), C.byref(f)), "gpu_fitness")
+        if adaptive:
+            _check(N.lib.cpd_fitness_gpu_ex(ctx.handle, C.byref(self.design), _dp(seeds), seeds.size, int(max_n),
+                                            int(nwarp), int(max_eval), N.SAMPLING_ADAPTIVE, C.byref(f)),
+                   "gpu_fitness")
+        else:
+            _check(N.lib.cpd_fitness_gpu(ctx.handle, C.byref(self.design), _dp(seeds), seeds.size, int(max_n),
+                                         int(nwarp), int(max_eval), C.byref(f)), "gpu_fitness")
         return f
 
     def gpu_fitness_points(self, lam_u, ray_u, *, mode: int = TRACE_HYBRID, want_p: bool = False,
                            context: Optional[Context] = None):
-        """Fixed-N estimator on explicit wavelength and ray u-points (parity entry)."""
+        """The estimator on explicit wavelength and ray u-points (parity entry): fixed N, or
+        adaptive sampling with mode | SAMPLING_ADAPTIVE (rays taken in the given order)."""
         lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
         ray_u = np.ascontiguousarray(ray_u, dtype=np.float64)
         ctx = context or default_context()

@@ -35,6 +35,8 @@ RAYTRACE_ERRORS = (RAYTRACE_NO_SURFACE_INTERSECTION, RAYTRACE_OUT_OF_BOUNDS,
 TRACE_HYBRID = 0
 TRACE_FP32 = 1
 TRACE_FP64 = 2
+SAMPLING_ADAPTIVE = 0x10  # OR-ed into a trace mode: the per-wavelength SEM stop
+SAMPLING_EXACT = 0x20     # with SAMPLING_ADAPTIVE: every wavelength on the exact path
 
 
 class SpectrometerParams(C.Structure):
@@ -137,6 +139,8 @@ SIGNATURES = [
     ("cpd_context_destroy", None, [_ctxp]),
     ("cpd_fitness_gpu", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                   C.POINTER(Fitness)]),
+    ("cpd_fitness_gpu_ex", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, C.c_uint32, C.c_uint32,
+                                     C.c_uint32, C.c_uint32, C.POINTER(Fitness)]),
     ("cpd_fitness_gpu_points", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, _dp, C.c_uint32, C.c_uint32,
                                          C.POINTER(Fitness), _dp]),
     ("cpd_fitness_gpu_points_static", C.c_int, [C.POINTER(Design), _dp, C.c_uint32, _dp, C.c_uint32, C.c_uint32,

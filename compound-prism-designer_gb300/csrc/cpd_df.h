@@ -116,7 +116,8 @@ struct alignas(16) LamDF {
     ff::F2 n;           // index of the last glass
     float ts, tp;       // s/p transmittance entering the exit face
     uint32_t lost;      // no ray of this wavelength reaches the exit face
-    uint32_t pad[3];
+    float ts_lo, tp_lo; // low words: ts, tp as float-float
+    uint32_t pad;
 };
 
 // The fast path's reference ray (see LamParams) in float-float: the first candidate of
@@ -207,8 +208,11 @@ CPD_HDN inline bool reference_ray_df(const DevDesign &D, const float *z32, LamPa
 // Returns false if no ray of this wavelength clears the flat faces. The face loop is
 // kept rolled: one warp runs this program once per wavelength, so instruction fetch,
 // not scheduling freedom, is what a longer unrolled body would cost.
+// With df_fresnel the Fresnel factors of the flat faces are formed in float-float too,
+// so that E's transmittances match the f64 trace to ~2^-44 (the adaptive mode's exact
+// path needs them); otherwise each factor is an FP32 value (~1e-7).
 CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z32, uint32_t R, LamParams &P,
-                                    double yguard_rel = kYGuardRel, LamDF *E = nullptr)
+                                    double yguard_rel = kYGuardRel, LamDF *E = nullptr, bool df_fresnel = false)
 {
     const int G = D.G;
     using namespace df;
@@ -285,9 +289,14 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
         const F2 cr = sqrt(cr_sq);
         const F2 kq = sub(mul(rr, ci_r), cr);
         const F2 vx = add(mul(dx, rr), mul(nx, kq)), vy = add(mul(dy, rr), mul(ny, kq));
-        if (D.ar && ci_r.hi > 0.5f) {
+        if (D.ar && lt(c(0.5f), ci_r)) {
             ts = mul(ts, ar99);
             tp = mul(tp, ar99);
+        } else if (df_fresnel) {
+            const F2 a = add(mul(n1, ci_r), mul(n2, cr)), b = add(mul(n1, cr), mul(n2, ci_r));
+            const F2 k4 = mulf(mul(mul(n1, n2), mul(ci_r, cr)), 4.f);
+            ts = mul(ts, div(k4, sqr(a)));
+            tp = mul(tp, div(k4, sqr(b)));
         } else {
             // 1 - R without cancellation: 4 n1 n2 ci cr / (n1 ci + n2 cr)^2 (s), ci <-> cr (p)
             const float f1 = n1.hi, f2 = n2.hi, fc = ci_r.hi, fr = cr.hi;
@@ -315,7 +324,9 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
         E->ts = ts.hi;
         E->tp = tp.hi;
         E->lost = lost ? 1u : 0u;
-        E->pad[0] = E->pad[1] = E->pad[2] = 0u;
+        E->ts_lo = ts.lo;
+        E->tp_lo = tp.lo;
+        E->pad = 0u;
     }
     if (lost) return false;
     // Sorted-ray index ranges: y_j = bym - bw z_j is monotone in z, so the index of a
@@ -386,7 +397,12 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
 // (SphericalLikeSurface::intersection + RadialBounds, geometry.rs:161-216, 85-91;
 // Ray::refract into air, ray.rs:309-367) and the detector (ray.rs:390-402,
 // spectrometer.rs:265-303). Returns true and (bin, t) on a hit.
-CPD_HDN inline bool trace_df(const DevDesign &D, const LamDF &E, float zh, float zl, uint32_t &bin, float &t)
+// One ray in float-float from the wavelength's LamDF. kExactT: the transmittance too
+// (exit-face Fresnel factors in float-float from E's float-float flat-face products),
+// returned as tfix = 2^31 t rounded as t_fixed64 does; otherwise t is an FP32 value.
+template <bool kExactT>
+CPD_HDN inline bool trace_df_(const DevDesign &D, const LamDF &E, float zh, float zl, uint32_t &bin, float &t,
+                              uint32_t &tfix)
 {
     using namespace df;
     const DFConst &C = D.dc;
@@ -428,9 +444,22 @@ CPD_HDN inline bool trace_df(const DevDesign &D, const LamDF &E, float zh, float
     const F2 k = sub(mul(rr, ci), cr);
     const F2 vx = add(mul(E.dx, rr), mul(nx, k)), vy = add(mul(E.dy, rr), mul(ny, k));
     float ts = E.ts, tp = E.tp;
-    if (D.ar && ci.hi > 0.5f) {
-        ts *= 0.99f;
-        tp *= 0.99f;
+    F2 tsd{E.ts, E.ts_lo}, tpd{E.tp, E.tp_lo};
+    if (D.ar && lt(c(0.5f), ci)) {
+        if (kExactT) {
+            const F2 ar99{0.99f, -9.5367431640625e-09f};  // 0.99 = hi + lo to ~1e-17
+            tsd = mul(tsd, ar99);
+            tpd = mul(tpd, ar99);
+        } else {
+            ts *= 0.99f;
+            tp *= 0.99f;
+        }
+    } else if (kExactT) {
+        // 1 - R_s = 4 n ci cr / (n ci + cr)^2, 1 - R_p = 4 n ci cr / (n cr + ci)^2 (n2 = 1)
+        const F2 a = add(mul(rr, ci), cr), b = add(mul(rr, cr), ci);
+        const F2 k4 = mulf(mul(rr, mul(ci, cr)), 4.f);
+        tsd = mul(tsd, div(k4, sqr(a)));
+        tpd = mul(tpd, div(k4, sqr(b)));
     } else {
         const float f1 = rr.hi, fc = ci.hi, fr = cr.hi;
         const float a = f1 * fc + fr, b = f1 * fr + fc;
@@ -459,10 +488,32 @@ CPD_HDN inline bool trace_df(const DevDesign &D, const LamDF &E, float zh, float
     const uint32_t b = q <= 0.f ? 0u : (q >= 4294967295.f ? 4294967295u : (uint32_t)q);
     if (b < D.B && lt(rem, C.bin_size)) {
         bin = b;
-        t = (ts + tp) * 0.5f;
+        if (kExactT) {
+            const F2 s = add(tsd, tpd);  // t = s / 2, exactly
+            t = 0.5f * s.hi;
+            tfix = t_fixed64(0.5 * ((double)s.hi + (double)s.lo));
+        } else {
+            t = (ts + tp) * 0.5f;
+        }
         return true;
     }
     return false;
+}
+
+// The re-trace of a flagged ray: bin and an FP32 transmittance.
+CPD_HDN inline bool trace_df(const DevDesign &D, const LamDF &E, float zh, float zl, uint32_t &bin, float &t)
+{
+    uint32_t tfix = 0;
+    return trace_df_<false>(D, E, zh, zl, bin, t, tfix);
+}
+
+// The adaptive mode's exact path: bin and tfix = 2^31 t (t to ~2^-44), for E filled by
+// lambda_setup_df with df_fresnel.
+CPD_HDN inline bool trace_df_exact(const DevDesign &D, const LamDF &E, float zh, float zl, uint32_t &bin,
+                                   uint32_t &tfix)
+{
+    float t = 0.f;
+    return trace_df_<true>(D, E, zh, zl, bin, t, tfix);
 }
 
 }  // namespace cpd

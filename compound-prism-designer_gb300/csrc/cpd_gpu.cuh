@@ -19,6 +19,7 @@ struct alignas(16) DesignJob {
     uint64_t hist_off;   // first histogram cell (rows x B, u64)
     uint64_t lam_off;    // first wavelength u-point
     uint64_t ray_off;    // first entry of the sorted ray tables
+    uint64_t rank_off;   // first entry of the rank table (adaptive sampling)
     uint64_t acc_off;    // first per-bin accumulator (B cells in each of S1, S2)
     uint64_t item_off;   // first trace work item
     uint64_t tile_off;   // first entropy tile
@@ -30,7 +31,8 @@ struct alignas(16) DesignJob {
     float lu_hi, lu_lo;      // log2 of that unit, float-float
 };
 
-// A ray whose FP32 result fell inside a guard band: (design, wavelength row, ray).
+// A ray whose FP32 result fell inside a guard band: (design, wavelength row, ray). In
+// adaptive sampling: a wavelength row whose stop decision needs the exact path (j unused).
 struct alignas(16) QEntry {
     uint32_t design, k, j, pad;
 };
@@ -78,6 +80,7 @@ struct LaunchArgs {
     const double *lam_u;
     const double *z64;
     const float *z32;     // (hi, lo) f32 pairs of the sorted z table
+    const uint32_t *rank; // adaptive sampling: ray index -> sorted position (~0u: no start height)
     LamParams *lp;
     LamDF *lx;            // per row: float-float data for the re-trace
     unsigned long long *hist;
@@ -90,13 +93,40 @@ struct LaunchArgs {
     uint32_t qcap;
     uint32_t ray_tile;
     uint32_t mode;        // CPD_TRACE_*
+    uint32_t adaptive;    // per-wavelength SEM stop: 1, or 2 with every row on the exact path
+    uint32_t max_B;       // widest detector of the launch
     Guards guards;
     double yguard_rel;
     double *p_out;        // optional W x B for the single design of the launch
     const float *logtab;  // float-float log2 table (cpd_ff.h), 4 x 256 floats
 };
 
-// Launches setup -> trace -> retrace -> entropy -> finalize on `stream`. Returns the
+// Most warps that trace one wavelength's rounds at once under adaptive sampling.
+constexpr uint32_t kMaxAdaptWarps = 4;
+
+// Per-bin state of one wavelength under adaptive sampling: shared memory, one array per
+// field (consecutive bins in consecutive words), carved from B-sized slices.
+struct BinStates {
+    unsigned long long *s1;  // sum of t_fixed over the bin's hits
+    unsigned long long *q1;  // sum of t_q
+    unsigned long long *q2;  // sum of t_q^2
+    uint32_t *n;             // Welford samples: the sizes of the rounds that hit the bin
+    uint32_t *h;             // hits
+    __device__ BinStates(void *base, uint32_t B)
+    {
+        s1 = static_cast<unsigned long long *>(base);
+        q1 = s1 + B;
+        q2 = q1 + B;
+        n = reinterpret_cast<uint32_t *>(q2 + B);
+        h = n + B;
+    }
+};
+// Bytes of shared memory the bin states of a B-bin detector take.
+constexpr size_t bin_state_bytes(uint32_t B) { return (size_t)B * (3 * 8 + 2 * 4); }
+
+// Launches setup -> trace -> retrace -> entropy -> finalize on `stream` (adaptive
+// sampling: setup -> adaptive rounds -> exact rounds of the unsure rows -> entropy ->
+// finalize). Returns the
 // number of kernel launches issued. If `ev` is given (5 events), ev[0..3] are recorded
 // before setup, trace, retrace and entropy, and ev[4] after finalize. With `pdl` (and no
 // events) each kernel after the setup is a programmatic dependent launch: its blocks

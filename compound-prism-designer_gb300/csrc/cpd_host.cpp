@@ -211,17 +211,24 @@ double norminv(double x)
     return std::copysign(v * p / q, x - 0.5);
 }
 
-void ray_table(const double *ray_u, uint32_t R, std::vector<double> &z64, std::vector<float> &z32)
+void ray_table(const double *ray_u, uint32_t R, std::vector<double> &z64, std::vector<float> &z32,
+               std::vector<uint32_t> *rank)
 {
-    z64.clear();
-    z64.reserve(R);
+    std::vector<std::pair<double, uint32_t>> zj;
+    zj.reserve(R);
     for (uint32_t j = 0; j < R; j++) {
         double z = norminv(ray_u[j]);
-        if (std::isfinite(z)) z64.push_back(z);  // a non-finite start height never reaches a face
+        if (std::isfinite(z)) zj.emplace_back(z, j);  // a non-finite start height never reaches a face
     }
-    std::sort(z64.begin(), z64.end());
-    z32.resize(2 * z64.size());
-    for (size_t j = 0; j < z64.size(); j++) split_f32(z64[j], z32[2 * j], z32[2 * j + 1]);
+    std::sort(zj.begin(), zj.end());
+    z64.resize(zj.size());
+    z32.resize(2 * zj.size());
+    if (rank) rank->assign(R, 0xffffffffu);
+    for (size_t i = 0; i < zj.size(); i++) {
+        z64[i] = zj[i].first;
+        split_f32(z64[i], z32[2 * i], z32[2 * i + 1]);
+        if (rank) (*rank)[zj[i].second] = (uint32_t)i;
+    }
 }
 
 // The GPU point policy: u_i = fract(fma(i0 + i, 1/phi, seed)) (kernel.rs:128-130 in f64).

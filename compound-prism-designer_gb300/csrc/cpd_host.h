@@ -14,7 +14,10 @@ void design_to_dev(const cpd_design &d, DevDesign &D);
 double norminv(double u);
 // Sorted ray table: z = norminv(u) ascending, non-finite values dropped; z32 holds
 // the f32 (hi, lo) split of each z, interleaved.
-void ray_table(const double *ray_u, uint32_t R, std::vector<double> &z64, std::vector<float> &z32);
+// rank (optional): for each ray index j, its position in the sorted table (~0u if its
+// start height is not finite).
+void ray_table(const double *ray_u, uint32_t R, std::vector<double> &z64, std::vector<float> &z32,
+               std::vector<uint32_t> *rank = nullptr);
 // u_i = fract(fma(first + i, 1/phi, seed)), i < n.
 void seed_points(double seed, uint32_t first, uint32_t n, double *out);
 }  // namespace cpd

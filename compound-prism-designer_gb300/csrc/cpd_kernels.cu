@@ -99,8 +99,10 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     const DevDesign &D = staged ? sD : a.designs[d];
     const float *z32 = staged && stage_z ? sz : a.z32 + 2 * J.ray_off;
     LamParams P;
-    lambda_setup_df(D, a.lam_u[J.lam_off + k], z32, J.Rz, P, a.yguard_rel, a.lx + row);
-    if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
+    lambda_setup_df(D, a.lam_u[J.lam_off + k], z32, J.Rz, P, a.yguard_rel, a.lx + row, a.adaptive != 0);
+    if (a.adaptive) {
+        // the adaptive rounds trace every ray of the band themselves
+    } else if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
         for (uint32_t j = P.band_lo; j < P.band_hi; j++) push_ray(a, d, k, j);
         P.core_lo = P.core_hi = 0;
     } else if (P.all_exact) {
@@ -214,6 +216,215 @@ __global__ void __launch_bounds__(32) retrace_exact_kernel(const LaunchArgs a)
             atomicAdd(&a.acc[e.design].hits[i % kSpread], 1ull);
         }
         atomicAdd(&a.acc[e.design].retraced[i % kSpread], 1ull);
+    }
+}
+
+// ------------------------------------------------------------------ adaptive sampling
+
+// The float-float exact trace of one ray as (bin or ~0u, t_fixed).
+__device__ __forceinline__ uint2 trace_df_exact_packed(const DevDesign &D, const LamDF &E, float zh, float zl)
+{
+    uint32_t b = 0, tx = 0;
+    return trace_df_exact(D, E, zh, zl, b, tx) ? make_uint2(b, tx) : make_uint2(0xffffffffu, 0u);
+}
+
+// The same, out of line: the fast kernel takes it for ~0.1% of its rays, and inlined its
+// float-float code would set the register budget of the whole kernel.
+__device__ __noinline__ uint2 trace_df_exact_call(const DevDesign &D, const LamDF &E, float zh, float zl)
+{
+    return trace_df_exact_packed(D, E, zh, zl);
+}
+
+// Per-block scratch of the adaptive kernels: KW warps trace KW rounds of one wavelength
+// at once (warp w takes round g0 + w of the group), and warp 0 then applies them in order.
+struct RoundSlots {
+    uint32_t bin[kMaxAdaptWarps][32];  // ~0u: no hit
+    uint32_t tf[kMaxAdaptWarps][32];   // t_fixed of a hit
+    uint32_t df[kMaxAdaptWarps];       // ballot of the rays traced in float-float
+    uint32_t flag;                     // 0 go on, 1 stopped or out of rays, 2 unsure
+    uint32_t count;                    // rays consumed
+};
+
+// One wavelength row under adaptive sampling (the stop rule of src/spectrometer/
+// kernel.rs:127-178, restated with exact integer Welford sums: cpd_model.h, sem_test)
+// by one block of KW warps; st holds the row's B bin states in shared memory.
+// Tracing: lane l of warp w takes ray g0 + 32 w + l in index order; `rank` maps it to its
+// place in the sorted z table, whose band / core ranges (from the setup) say how to trace
+// it: lost outside the band, the FP32 fast path inside the core, the float-float trace
+// (exact transmittance) otherwise or when the fast path flags it.
+// Applying a round (warp 0): its hits add to their bins' sums with shared-memory integer
+// atomics (order-independent), one leader lane per bin hit adds the round's size to the
+// bin's Welford count and runs its SEM test, all bins at once. Rounds of a group after the
+// one that stops the wavelength were traced for nothing and are dropped.
+// kExact: every ray by the float-float trace and the exact test. Otherwise a row whose
+// stop decision the FP32 transmittances cannot settle (sem_test: SEM_UNSURE) is queued
+// for the exact path and leaves nothing behind.
+template <bool kExact>
+__device__ void adaptive_row(const LaunchArgs &a, uint64_t row, void *st_base, RoundSlots &rs, uint32_t KW,
+                             uint32_t warp, uint32_t lane)
+{
+    const uint32_t d = find_job<F_ROW>(a.jobs, a.njobs, row);
+    const DesignJob &J = a.jobs[d];
+    const uint32_t k = (uint32_t)(row - J.row_off);
+    const uint32_t B = J.B, R = J.R;
+    const DevDesign &D = a.designs[d];
+    if (!kExact && a.adaptive == 2u) {
+        // verification mode: every row on the exact path
+        if (warp == 0 && lane == 0) {
+            const unsigned long long pos = atomicAdd(&a.ctl->queue_count, 1ull);
+            if (pos < a.qcap) a.queue[pos] = QEntry{d, k, 0u, 0u};
+            else atomicOr(&a.ctl->overflow, 1u);
+        }
+        return;
+    }
+    const FastConst C = D.fc;
+    const LamParams P = a.lp[row];
+    const LamDF &E = a.lx[row];
+    const BinStates st(st_base, B);
+    for (uint32_t b = warp * 32u + lane; b < B; b += KW * 32u) {
+        st.s1[b] = st.q1[b] = st.q2[b] = 0ull;
+        st.n[b] = st.h[b] = 0u;
+    }
+    if (warp == 0 && lane == 0) {
+        rs.flag = 0u;
+        rs.count = 0u;
+    }
+    __syncthreads();
+    const uint32_t *rank = a.rank + J.rank_off;
+    const float2 *zt = reinterpret_cast<const float2 *>(a.z32) + J.ray_off;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint32_t count = 0, hits = 0, ndf = 0;  // warp 0
+    // no ray clears the flat faces: every round runs without a hit
+    const uint32_t g_start = P.band_lo >= P.band_hi ? R : 0u;
+    if (g_start == R && warp == 0) count = R;
+    for (uint32_t g0 = g_start; g0 < R; g0 += KW * kRoundRays) {
+        {
+            const uint32_t j = g0 + warp * kRoundRays + lane;
+            uint32_t bin = 0xffffffffu, tf = 0u;
+            bool used_df = false;
+            if (j < R) {
+                const uint32_t s = rank[j];  // ~0u (no finite start height) is outside the band
+                if (s >= P.band_lo && s < P.band_hi) {
+                    const float2 z = zt[s];
+                    int res = RAY_FLAG;
+                    if (!kExact && !P.all_exact && s >= P.core_lo && s < P.core_hi) {
+                        uint32_t b = 0;
+                        float t = 0.f;
+                        res = fast_ray(C, P, a.guards, z.x, z.y, b, t);
+                        if (res == RAY_HIT) {
+                            bin = b;
+                            tf = t_fixed(t);
+                        }
+                    }
+                    if (res == RAY_FLAG) {
+                        const uint2 r = kExact ? trace_df_exact_packed(D, E, z.x, z.y)
+                                               : trace_df_exact_call(D, E, z.x, z.y);
+                        bin = r.x;
+                        tf = r.y;
+                        used_df = true;
+                    }
+                }
+            }
+            rs.bin[warp][lane] = bin;
+            rs.tf[warp][lane] = tf;
+            const uint32_t dfb = __ballot_sync(0xffffffffu, used_df);
+            if (lane == 0) rs.df[warp] = dfb;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t flag = 0u;
+            for (uint32_t w = 0; w < KW; w++) {
+                const uint32_t r0 = g0 + w * kRoundRays;
+                if (r0 >= R) break;
+                const uint32_t nr = min(kRoundRays, R - r0);
+                const uint32_t bin = rs.bin[w][lane], tf = rs.tf[w][lane];
+                const bool hit = bin != 0xffffffffu;
+                const uint32_t hm = __ballot_sync(0xffffffffu, hit);
+                count += nr;
+                hits += __popc(hm);
+                ndf += __popc(rs.df[w]);
+                if (!hm) continue;  // no hit: a certain "go on"
+                const uint32_t grp = __match_any_sync(0xffffffffu, bin);
+                if (hit) {
+                    const uint32_t q = tf >> kTqShift;  // <= 2^20
+                    atomicAdd(st.s1 + bin, (unsigned long long)tf);
+                    atomicAdd(st.q1 + bin, (unsigned long long)q);
+                    atomicAdd(st.q2 + bin, (unsigned long long)q * q);
+                }
+                __syncwarp();
+                int verdict = SEM_PASS;
+                if (hit && (grp & lt_mask) == 0u) {  // the lowest lane of each bin's group
+                    const uint32_t n = st.n[bin] + nr, h = st.h[bin] + (uint32_t)__popc(grp);
+                    st.n[bin] = n;
+                    st.h[bin] = h;
+                    verdict = sem_test(n, h, st.q1[bin], st.q2[bin], kExact ? 0u : kTqDelta);
+                }
+                const bool fail = __any_sync(0xffffffffu, verdict == SEM_FAIL);
+                const bool unsure = __any_sync(0xffffffffu, verdict == SEM_UNSURE);
+                __syncwarp();
+                if (fail) continue;
+                flag = (!kExact && unsure) ? 2u : 1u;
+                break;
+            }
+            if (!flag && g0 + KW * kRoundRays >= R) flag = 1u;  // out of rays
+            if (lane == 0) {
+                rs.flag = flag;
+                rs.count = count;
+            }
+        }
+        __syncthreads();
+        if (rs.flag) break;
+    }
+    if (warp == 0 && rs.flag == 2u) {
+        if (lane == 0) {
+            const unsigned long long pos = atomicAdd(&a.ctl->queue_count, 1ull);
+            if (pos < a.qcap) a.queue[pos] = QEntry{d, k, 0u, 0u};
+            else atomicOr(&a.ctl->overflow, 1u);
+        }
+    } else if (warp == 0) {
+        unsigned long long *hrow = a.hist + J.hist_off + (uint64_t)k * B;
+        for (uint32_t b = lane; b < B; b += 32u) {
+            const unsigned long long s1 = st.s1[b];
+            if (s1) hrow[b] = rescale_cell(s1, R, count);
+        }
+        if (lane == 0) {
+            const uint32_t sp = (uint32_t)(row % (uint64_t)kSpread);
+            atomicAdd(&a.acc[d].fast[sp], (unsigned long long)count);
+            if (hits) atomicAdd(&a.acc[d].hits[sp], (unsigned long long)hits);
+            if (ndf) atomicAdd(&a.acc[d].retraced[sp], (unsigned long long)ndf);
+        }
+    }
+    __syncthreads();  // every warp: st and rs are reused by the block's next row
+}
+
+#ifndef CPD_ADAPT_MIN_BLOCKS
+#define CPD_ADAPT_MIN_BLOCKS 8  // 64 registers: more resident rows, which the one-warp rows need
+#endif
+// One row per block of KW = blockDim.x / 32 warps: rows differ widely in length (a single
+// round to all R / 32), and one row per block lets the block scheduler balance them.
+__global__ void __launch_bounds__(32 * kMaxAdaptWarps, CPD_ADAPT_MIN_BLOCKS) adaptive_kernel(const LaunchArgs a)
+{
+    extern __shared__ __align__(16) unsigned long long adapt_smem[];
+    __shared__ RoundSlots rs;
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();  // the setup's LamParams and LamDF
+    adaptive_row<false>(a, blockIdx.x, adapt_smem, rs, blockDim.x >> 5,
+                        threadIdx.x >> 5, threadIdx.x & 31u);
+}
+
+// The queued rows: the float-float path from the first round on, one warp per block.
+__global__ void __launch_bounds__(32) adaptive_exact_kernel(const LaunchArgs a)
+{
+    extern __shared__ __align__(16) unsigned long long adapt_smem[];
+    __shared__ RoundSlots rs;
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();  // the adaptive kernel's queue
+    const unsigned long long qn = a.ctl->queue_count;
+    const uint64_t n = qn < a.qcap ? qn : a.qcap;
+    for (uint64_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const QEntry e = a.queue[i];
+        adaptive_row<true>(a, a.jobs[e.design].row_off + e.k, adapt_smem, rs, 1u, 0u,
+                           threadIdx.x);
     }
 }
 
@@ -551,6 +762,21 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         launch_k(setup_kernel, blocks, 32, 2 * kStageRays * sizeof(float), stream, false, a);
         launches++;
     }
+    if (a.adaptive) {
+        const size_t smem = bin_state_bytes(a.max_B ? a.max_B : 1u);
+        if (ev) cudaEventRecord(ev[1], stream);
+        if (a.total_rows) {
+            // enough rows to fill the GPU: one warp per row; fewer: up to kMaxAdaptWarps
+            // warps per row trace that many rounds at once
+            const uint64_t per_sm = a.total_rows / (uint64_t)num_sms;
+            const uint32_t kw = per_sm >= 8 ? 1u : per_sm >= 2 ? 2u : kMaxAdaptWarps;
+            launch_k(adaptive_kernel, (unsigned)a.total_rows, 32 * kw, smem, stream, pdl, a);
+            launches++;
+        }
+        if (ev) cudaEventRecord(ev[2], stream);
+        launch_k(adaptive_exact_kernel, (unsigned)(num_sms * 8), 32, smem, stream, pdl, a);
+        launches++;
+    } else {
     if (ev) cudaEventRecord(ev[1], stream);
     if (a.mode != CPD_TRACE_FP64 && a.total_items) {
         int per_sm = 0;
@@ -567,6 +793,7 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     launch_k(a.mode == CPD_TRACE_FP64 ? retrace_exact_kernel : retrace_kernel, (unsigned)(num_sms * 8), 32, 0, stream,
              pdl, a);
     launches++;
+    }
     if (ev) cudaEventRecord(ev[3], stream);
     if (a.total_tiles) {
         // one warp per tile, as many blocks as are resident at once

@@ -418,6 +418,58 @@ CPD_HD Guards no_guards() { return Guards{0.f, 0.f, 0.f, 0.f, 0.f}; }
 // Relative guard of the y-interval ends: both sides are f64, so a few ulps suffice.
 constexpr double kYGuardRel = 1e-11;
 
+// ----------------------------------------------------------------- adaptive sampling
+//
+// The stop rule of the reference GPU kernel (src/spectrometer/kernel.rs:127-178): the
+// rays of one wavelength are taken in index order, 32 per round. After each round, every
+// bin that the round's rays hit merges the round into its Welford state (32 samples: the
+// hits' t and zeros for the round's other rays), and the wavelength stops when the round
+// hit some bin and every bin it hit passes the SEM test (welford.rs:80-84,
+// SEM^2 <= (5e-3)^2). p(d|lambda) is then the bin's sum of t over all rays consumed.
+//
+// Here the Welford states are exact integer sums, so the test is exact arithmetic on
+// quantized transmittances, the same on the host and the device:
+//   t_q = t_fixed >> 11 (t in 2^-20 units), N = samples (32 per round in which the bin was
+//   hit), q1 = sum t_q, q2 = sum t_q^2 over its h hits,
+//   M2 = (q2 - q1^2 / N) 2^-40 < (5e-3)^2 N (N - 1)
+//   <=>  40000 (N q2 - q1^2) < N^2 (N - 1) 2^40.
+// N <= 2^22 rays keeps every term below 2^107 (unsigned 128-bit arithmetic).
+constexpr uint32_t kRoundRays = 32;
+constexpr int kTqShift = 11;
+// Bound on |t_q(FP32 fast path) - t_q(exact)| for a fast-path hit: it holds while the
+// fast path's transmittance error stays below 2^-19 (~1.9e-6; measured: below 3e-7).
+constexpr uint32_t kTqDelta = 2;
+
+enum : int { SEM_FAIL = 0, SEM_PASS = 1, SEM_UNSURE = 2 };
+
+// The SEM test of one bin. With delta > 0 the sums are those of FP32 transmittances,
+// each t_q within delta of its exact value: the test is SEM_UNSURE when those errors
+// could change its outcome, i.e. when |40000 (N q2 - q1^2) - N^2 (N - 1) 2^40| is within
+// 40000 (N h delta (2^21 + delta) + h delta (2 q1 + h delta)).
+CPD_HD int sem_test(uint64_t N, uint64_t h, uint64_t q1, uint64_t q2, uint32_t delta)
+{
+    typedef unsigned __int128 u128;
+    // N q2 >= q1^2: Cauchy-Schwarz over the N samples (hits and zeros)
+    const u128 lhs = (u128)40000u * ((u128)N * q2 - (u128)q1 * q1);
+    const u128 rhs = ((u128)N * N * (N - 1u)) << 40;
+    if (delta == 0u) return lhs < rhs ? SEM_PASS : SEM_FAIL;
+    const u128 hd = (u128)h * delta;
+    const u128 err =
+        (u128)40000u * ((u128)N * h * ((u128)delta * ((1u << 21) + delta)) + hd * (2u * (u128)q1 + hd));
+    if (lhs + err < rhs) return SEM_PASS;
+    if (lhs >= rhs + err) return SEM_FAIL;
+    return SEM_UNSURE;
+}
+
+// A cell's sum of t over `count` rays rescaled to the pass's common divisor R:
+// round(s1 R / count), so that p = cell 2^-31 / R everywhere downstream.
+CPD_HD uint64_t rescale_cell(uint64_t s1, uint32_t R, uint32_t count)
+{
+    if (count == R || s1 == 0u) return s1;
+    typedef unsigned __int128 u128;
+    return (uint64_t)(((u128)s1 * R + count / 2u) / count);
+}
+
 // Splits an f64 into f32 hi + lo parts (hi + lo == v to about 2^-48 relative).
 CPD_HD void split_f32(double v, float &hi, float &lo)
 {

@@ -87,8 +87,12 @@ struct RayKey {
 struct RayTable {
     std::vector<double> z64;
     std::vector<float> z32;
+    std::vector<uint32_t> rank;  // ray index -> sorted position (adaptive sampling)
 };
 using RayTablePtr = std::shared_ptr<const RayTable>;
+
+// The sampling flags a trace mode may carry.
+constexpr uint32_t kSamplingBits = CPD_SAMPLING_ADAPTIVE | CPD_SAMPLING_EXACT;
 
 // Everything one pass needs on the device, plus its staging and its captured graph.
 // A context owns one slot (the synchronous calls); a server owns several, so that
@@ -184,7 +188,7 @@ RayTablePtr ray_table_cached(cpd_context *ctx, double seed, uint32_t R)
     std::vector<double> u(R);
     seed_points(seed, 1, R, u.data());
     auto t = std::make_shared<RayTable>();
-    ray_table(u.data(), R, t->z64, t->z32);
+    ray_table(u.data(), R, t->z64, t->z32, &t->rank);
     std::lock_guard<std::mutex> lk(ctx->cache_mu);
     if (ctx->ray_cache.size() > 256) ctx->ray_cache.clear();
     return ctx->ray_cache.emplace(key, t).first->second;
@@ -239,10 +243,14 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
                double *p_out_host, bool use_graph, bool profile)
 {
     const uint32_t n = (uint32_t)ds.size();
+    const bool adaptive = (mode & CPD_SAMPLING_ADAPTIVE) != 0u;
+    const bool all_exact = adaptive && (mode & CPD_SAMPLING_EXACT) != 0u;
+    mode &= ~kSamplingBits;
     std::vector<DesignJob> jobs(n);
     std::vector<uint8_t> owns_rays(n, 1);  // designs that share a ray table share its copy
-    std::map<const RayTable *, uint64_t> ray_offs;
-    uint64_t rows = 0, hist = 0, lam = 0, ray = 0, accc = 0, items = 0, tiles = 0;
+    std::map<const RayTable *, std::pair<uint64_t, uint64_t>> ray_offs;
+    uint64_t rows = 0, hist = 0, lam = 0, ray = 0, rnk = 0, accc = 0, items = 0, tiles = 0;
+    uint32_t max_B = 0;
     for (uint32_t i = 0; i < n; i++) {
         const PassDesign &p = ds[i];
         DesignJob &J = jobs[i];
@@ -254,9 +262,11 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         J.row_off = rows;
         J.hist_off = hist;
         J.lam_off = lam;
-        auto ro = ray_offs.emplace(p.rays, ray);
-        J.ray_off = ro.first->second;
+        auto ro = ray_offs.emplace(p.rays, std::make_pair(ray, rnk));
+        J.ray_off = ro.first->second.first;
+        J.rank_off = ro.first->second.second;
         owns_rays[i] = ro.second;
+        max_B = std::max(max_B, J.B);
         J.acc_off = accc;
         J.item_off = items;
         J.tile_off = tiles;
@@ -268,18 +278,23 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         rows += J.W;
         hist += (uint64_t)J.W * J.B;
         lam += J.W;
-        if (owns_rays[i]) ray += (J.Rz + 1u) & ~1u;  // even: every table starts 16-byte aligned
+        if (owns_rays[i]) {
+            ray += (J.Rz + 1u) & ~1u;  // even: every table starts 16-byte aligned
+            if (adaptive) rnk += J.R;
+        }
         accc += J.B;
         items += (uint64_t)((J.W + 31) / 32) * J.nchunk;
         tiles += J.ntiles;
     }
-    // one input arena: designs | jobs | wavelength points | z64 | z32 (256-byte sections)
+    // one input arena: designs | jobs | wavelength points | z64 | z32 | ranks (256-byte
+    // sections; the ranks only under adaptive sampling)
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t o_job = al(sizeof(DevDesign) * n);
     const size_t o_lam = o_job + al(sizeof(DesignJob) * n);
     const size_t o_z64 = o_lam + al(sizeof(double) * lam);
     const size_t o_z32 = o_z64 + al(sizeof(double) * ray);
-    const size_t in_bytes = o_z32 + al(2 * sizeof(float) * ray);
+    const size_t o_rank = o_z32 + al(2 * sizeof(float) * ray);
+    const size_t in_bytes = o_rank + al(sizeof(uint32_t) * rnk);
     const size_t ctl_off = al(sizeof(DesignOut) * n);
     const size_t out_bytes = ctl_off + sizeof(Control);
     CPD_TRY(S.h_in.ensure(in_bytes));
@@ -294,6 +309,9 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
                     sizeof(double) * jobs[i].Rz);
         std::memcpy(reinterpret_cast<float *>(hin + o_z32) + 2 * jobs[i].ray_off, ds[i].rays->z32.data(),
                     2 * sizeof(float) * jobs[i].Rz);
+        if (adaptive)
+            std::memcpy(reinterpret_cast<uint32_t *>(hin + o_rank) + jobs[i].rank_off, ds[i].rays->rank.data(),
+                        sizeof(uint32_t) * jobs[i].R);
     }
     // device buffers
     const size_t hist_bytes = sizeof(unsigned long long) * std::max<uint64_t>(hist, 1);
@@ -331,6 +349,9 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     a.lam_u = reinterpret_cast<const double *>(din + o_lam);
     a.z64 = reinterpret_cast<const double *>(din + o_z64);
     a.z32 = reinterpret_cast<const float *>(din + o_z32);
+    a.rank = adaptive ? reinterpret_cast<const uint32_t *>(din + o_rank) : nullptr;
+    a.adaptive = adaptive ? (all_exact ? 2u : 1u) : 0u;
+    a.max_B = max_B;
     a.lp = S.lp.as<LamParams>();
     a.lx = S.lx.as<LamDF>();
     a.hist = S.hist.as<unsigned long long>();
@@ -426,7 +447,10 @@ int pass_finish(PassSlot &S, PassResult &res)
     return CPD_OK;
 }
 
-void fill_fitness(const cpd_design &d, const DesignOut &o, uint64_t rays, cpd_fitness &f, bool need_conv)
+// rays: the fixed-N estimator's ray count; under adaptive sampling the rays actually
+// consumed (counted on the device) replace it.
+void fill_fitness(const cpd_design &d, const DesignOut &o, uint64_t rays, cpd_fitness &f, bool need_conv,
+                  bool adaptive = false)
 {
     std::memset(&f, 0, sizeof(f));
     f.size = d.size;
@@ -435,10 +459,10 @@ void fill_fitness(const cpd_design &d, const DesignOut &o, uint64_t rays, cpd_fi
     f.h_cond = o.h_cond;
     f.h_det = o.h_det;
     f.max_sem = o.max_sem;
-    f.rays = rays;
+    f.rays = adaptive ? o.fast : rays;
     f.hits = o.hits;
     f.retraced = o.retraced;
-    f.fast_rays = o.fast;
+    f.fast_rays = adaptive ? o.fast - std::min(o.fast, o.retraced) : o.fast;
     f.wavelengths = (uint32_t)o.rows;
     f.status = (need_conv && !o.converged) ? CPD_NOT_CONVERGED : CPD_OK;
 }
@@ -447,6 +471,17 @@ bool valid_design(const cpd_design *d)
 {
     return d && d->nglass >= 1 && d->nglass <= CPD_MAX_GLASS && d->bin_count >= 1 && d->bin_count <= CPD_MAX_BINS;
 }
+
+// A CPD_TRACE_* value, optionally with CPD_SAMPLING_ADAPTIVE (hybrid trace only) and
+// then CPD_SAMPLING_EXACT.
+bool valid_mode(uint32_t m)
+{
+    const uint32_t t = m & ~kSamplingBits, smp = m & kSamplingBits;
+    if (t > CPD_TRACE_FP64) return false;
+    return smp == 0u || (t == CPD_TRACE_HYBRID && (smp & CPD_SAMPLING_ADAPTIVE));
+}
+
+bool is_adaptive(uint32_t m) { return (m & CPD_SAMPLING_ADAPTIVE) != 0u; }
 
 bool valid_item(const cpd_batch_item &it)
 {
@@ -633,7 +668,7 @@ void srv_complete(cpd_server *sv, size_t i)
         if (e) r.status = e;
         else fill_fitness(r.designs[work[k].idx], res.outs[k],
                           (uint64_t)r.items[work[k].idx].max_n * r.items[work[k].idx].max_eval, r.outs[work[k].idx],
-                          true);
+                          true, is_adaptive(r.mode));
         if (--r.remaining == 0) {
             r.done = true;
             r.t_done = std::chrono::steady_clock::now();
@@ -847,29 +882,38 @@ int cpd_fitness_gpu_points(cpd_context *ctx, const cpd_design *d, const double *
                            const double *ray_u, uint32_t R, uint32_t trace_mode, cpd_fitness *out, double *p_out)
 {
     if (!ctx || !valid_design(d) || !lam_u || !ray_u || !out) return CPD_INVALID_ARGUMENT;
-    if (W == 0 || W > CPD_MAX_WAVELENGTHS || R == 0 || R > CPD_MAX_RAYS || trace_mode > CPD_TRACE_FP64)
+    if (W == 0 || W > CPD_MAX_WAVELENGTHS || R == 0 || R > CPD_MAX_RAYS || !valid_mode(trace_mode))
         return CPD_INVALID_ARGUMENT;
     CPD_SYNC_ENTRY(ctx);
     DevDesign D;
     design_to_dev(*d, D);
     RayTable rt;
-    ray_table(ray_u, R, rt.z64, rt.z32);
+    ray_table(ray_u, R, rt.z64, rt.z32, &rt.rank);
     std::vector<PassDesign> ds{PassDesign{&D, W, R, lam_u, &rt}};
     PassResult res;
     int e = run_pass_checked(ctx, ctx->main, ds, trace_mode, true, p_out, res, ctx->use_graphs);
     if (e) return e;
-    fill_fitness(*d, res.outs[0], (uint64_t)W * R, *out, false);
+    fill_fitness(*d, res.outs[0], (uint64_t)W * R, *out, false, is_adaptive(trace_mode));
     return CPD_OK;
 }
 
 int cpd_fitness_gpu(cpd_context *ctx, const cpd_design *d, const double *seeds, uint32_t nseeds, uint32_t max_n,
                     uint32_t nwarp, uint32_t max_eval, cpd_fitness *out)
 {
+    return cpd_fitness_gpu_ex(ctx, d, seeds, nseeds, max_n, nwarp, max_eval, 0u, out);
+}
+
+int cpd_fitness_gpu_ex(cpd_context *ctx, const cpd_design *d, const double *seeds, uint32_t nseeds, uint32_t max_n,
+                       uint32_t nwarp, uint32_t max_eval, uint32_t sampling, cpd_fitness *out)
+{
     if (!ctx || !valid_design(d) || !seeds || !out || nseeds == 0) return CPD_INVALID_ARGUMENT;
     if (max_n == 0 || max_eval == 0 || max_eval > CPD_MAX_RAYS) return CPD_INVALID_ARGUMENT;
     if ((uint64_t)max_n * nseeds > CPD_MAX_WAVELENGTHS) return CPD_INVALID_ARGUMENT;
+    const uint32_t mode = CPD_TRACE_HYBRID | sampling;
+    if ((sampling & ~kSamplingBits) || !valid_mode(mode)) return CPD_INVALID_ARGUMENT;
     CPD_SYNC_ENTRY(ctx);
-    const bool tune = ctx->autotune && !ctx->profiling;
+    // the adaptive kernels have no launch shape to tune
+    const bool tune = ctx->autotune && !ctx->profiling && !is_adaptive(mode);
     if (!tune && nwarp >= 1 && nwarp <= 8) ctx->warps_per_cta = nwarp;
     DevDesign D;
     design_to_dev(*d, D);
@@ -881,28 +925,28 @@ int cpd_fitness_gpu(cpd_context *ctx, const cpd_design *d, const double *seeds, 
         std::vector<PassDesign> ds{PassDesign{&D, max_n, max_eval, lam->data(), rt.get()}};
         if (tune && s == 0) {
             // the autotuner replaces the reference's nwarp hint
-            auto it = ctx->tune_cache.find(tune_class(ds, CPD_TRACE_HYBRID));
+            auto it = ctx->tune_cache.find(tune_class(ds, mode));
             if (it != ctx->tune_cache.end()) {
                 ctx->ray_tile = it->second.first;
                 ctx->warps_per_cta = it->second.second;
             } else {
-                const int te = tune_pass(ctx, ds, CPD_TRACE_HYBRID, nullptr);
+                const int te = tune_pass(ctx, ds, mode, nullptr);
                 if (te) return te;
             }
         }
-        int e = run_pass_checked(ctx, ctx->main, ds, CPD_TRACE_HYBRID, s == 0, nullptr, res, ctx->use_graphs);
+        int e = run_pass_checked(ctx, ctx->main, ds, mode, s == 0, nullptr, res, ctx->use_graphs);
         if (e) return e;
         rays += (uint64_t)max_n * max_eval;
         if (res.outs[0].converged) break;
     }
-    fill_fitness(*d, res.outs[0], rays, *out, true);
+    fill_fitness(*d, res.outs[0], rays, *out, true, is_adaptive(mode));
     return out->status;
 }
 
 int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items, uint32_t n,
                           uint32_t trace_mode, cpd_fitness *outs)
 {
-    if (!ctx || !designs || !items || !outs || n == 0 || trace_mode > CPD_TRACE_FP64) return CPD_INVALID_ARGUMENT;
+    if (!ctx || !designs || !items || !outs || n == 0 || !valid_mode(trace_mode)) return CPD_INVALID_ARGUMENT;
     for (uint32_t i = 0; i < n; i++)
         if (!valid_design(&designs[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
     CPD_SYNC_ENTRY(ctx);
@@ -911,7 +955,7 @@ int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd
     std::vector<RayTablePtr> rts;
     std::vector<PassDesign> ds;
     batch_inputs(ctx, designs, items, n, devs, lams, rts, ds);
-    if (ctx->autotune && !ctx->profiling) {
+    if (ctx->autotune && !ctx->profiling && !is_adaptive(trace_mode)) {
         auto it = ctx->tune_cache.find(tune_class(ds, trace_mode));
         if (it != ctx->tune_cache.end()) {
             ctx->ray_tile = it->second.first;
@@ -925,14 +969,15 @@ int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd
     int e = run_pass_checked(ctx, ctx->main, ds, trace_mode, true, nullptr, res, ctx->use_graphs);
     if (e) return e;
     for (uint32_t i = 0; i < n; i++)
-        fill_fitness(designs[i], res.outs[i], (uint64_t)items[i].max_n * items[i].max_eval, outs[i], true);
+        fill_fitness(designs[i], res.outs[i], (uint64_t)items[i].max_n * items[i].max_eval, outs[i], true,
+                     is_adaptive(trace_mode));
     return CPD_OK;
 }
 
 int cpd_autotune_batch(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items, uint32_t n,
                        uint32_t trace_mode, uint32_t *ray_tile, uint32_t *warps_per_cta, double *best_ms)
 {
-    if (!ctx || !designs || !items || n == 0 || trace_mode > CPD_TRACE_FP64) return CPD_INVALID_ARGUMENT;
+    if (!ctx || !designs || !items || n == 0 || trace_mode > CPD_TRACE_FP64) return CPD_INVALID_ARGUMENT;  // fixed-N only
     for (uint32_t i = 0; i < n; i++)
         if (!valid_design(&designs[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
     CPD_SYNC_ENTRY(ctx);
@@ -1069,7 +1114,7 @@ int cpd_server_create(cpd_context *ctx, uint64_t mem_budget_bytes, uint32_t slot
 int cpd_server_submit(cpd_server *sv, const cpd_design *designs, const cpd_batch_item *items, uint32_t n,
                       uint32_t trace_mode, uint64_t *request_id)
 {
-    if (!sv || !designs || !items || !request_id || n == 0 || trace_mode > CPD_TRACE_FP64) return CPD_INVALID_ARGUMENT;
+    if (!sv || !designs || !items || !request_id || n == 0 || !valid_mode(trace_mode)) return CPD_INVALID_ARGUMENT;
     for (uint32_t i = 0; i < n; i++)
         if (!valid_design(&designs[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(sv->mu);

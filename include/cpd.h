@@ -107,6 +107,21 @@ enum {
     CPD_TRACE_FP64 = 2      /* every ray in exact f64 (precision study reference) */
 };
 
+/* Sampling flag, OR-ed into a trace mode (CPD_TRACE_HYBRID only) or passed as
+ * cpd_fitness_gpu_ex's `sampling`: the per-wavelength SEM stop of the reference GPU
+ * kernel (src/spectrometer/kernel.rs:127-178). Each wavelength takes its rays in index
+ * order, 32 per round, and stops after the first round that hit some bin and after which
+ * every bin it hit has SEM <= 5e-3 (welford.rs:80-84); p(d|lambda) is the bin's sum of t
+ * over the rays consumed. The Welford state of each bin is kept as exact integer sums
+ * (t quantized to 2^-20 for the test), so the decisions are those of exact arithmetic
+ * and the same on every launch shape. Without the flag every wavelength uses all rays
+ * (fixed N). cpd_fitness.rays then counts the rays consumed. */
+#define CPD_SAMPLING_ADAPTIVE 0x10u
+/* With CPD_SAMPLING_ADAPTIVE: every wavelength on the exact path (float-float trace and
+ * transmittances, exact test) instead of the FP32 fast path with the exact path as
+ * fallback. For verification: the stop rounds are those of CPD_SAMPLING_ADAPTIVE. */
+#define CPD_SAMPLING_EXACT 0x20u
+
 typedef struct cpd_context cpd_context;
 
 /* ---------------------------------------------------------------- host side */
@@ -178,11 +193,19 @@ void cpd_context_destroy(cpd_context *ctx);
 int cpd_fitness_gpu(cpd_context *ctx, const cpd_design *d, const double *seeds, uint32_t nseeds,
                     uint32_t max_n, uint32_t nwarp, uint32_t max_eval, cpd_fitness *out);
 
+/* cpd_fitness_gpu with a sampling choice: 0 (fixed N, what cpd_fitness_gpu does) or
+ * CPD_SAMPLING_ADAPTIVE, the reference kernel's per-wavelength SEM stop
+ * (src/spectrometer/kernel.rs:127-178) inside the same seed loop. */
+int cpd_fitness_gpu_ex(cpd_context *ctx, const cpd_design *d, const double *seeds, uint32_t nseeds,
+                       uint32_t max_n, uint32_t nwarp, uint32_t max_eval, uint32_t sampling,
+                       cpd_fitness *out);
+
 /* Fixed-N estimator on explicit point sets (the parity entry point): W wavelength
  * u-points and R ray u-points, every wavelength traced with all R rays
  * (prob_dets_given_wavelengths, src/spectrometer/kernel.rs:89-193, on given
  * points). p_out (optional, W*B, row-major) receives p(d|lambda). trace_mode is a
- * CPD_TRACE_* value. */
+ * CPD_TRACE_* value, optionally with CPD_SAMPLING_ADAPTIVE (then R is the ray budget
+ * and the rays are taken in the given order). */
 int cpd_fitness_gpu_points(cpd_context *ctx, const cpd_design *d, const double *lam_u, uint32_t W,
                            const double *ray_u, uint32_t R, uint32_t trace_mode, cpd_fitness *out,
                            double *p_out);
@@ -227,7 +250,9 @@ typedef struct cpd_batch_item {
 
 /* Batched form (no reference counterpart; the reference evaluates one design per
  * call, designer.py:267-300): n designs of mixed G, B, W, R in one captured
- * launch sequence. outs[i].status is CPD_OK or CPD_NOT_CONVERGED per design. */
+ * launch sequence. outs[i].status is CPD_OK or CPD_NOT_CONVERGED per design. trace_mode
+ * may carry CPD_SAMPLING_ADAPTIVE (then the autotuner is not used: the adaptive kernels
+ * have no launch shape). */
 int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items,
                           uint32_t n, uint32_t trace_mode, cpd_fitness *outs);
 
@@ -242,7 +267,8 @@ int cpd_get_launch_shape(cpd_context *ctx, uint32_t *ray_tile, uint32_t *warps_p
  * the resident warps, and warps per CTA in {2, 4, 8} (captured graph, minimum of two
  * timed passes each), sets the fastest on the context and remembers it for the batch's
  * class: trace mode and the binary orders of magnitude of its design count, wavelength
- * rows, rays and widest detector. Results do not depend on the shape. */
+ * rows, rays and widest detector. Results do not depend on the shape. Fixed-N passes
+ * only (a trace mode without CPD_SAMPLING_ADAPTIVE). */
 int cpd_autotune_batch(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items,
                        uint32_t n, uint32_t trace_mode, uint32_t *ray_tile, uint32_t *warps_per_cta,
                        double *best_ms);
@@ -283,7 +309,9 @@ int cpd_measure_fp32_peak(cpd_context *ctx, uint32_t iters, double *tflops);
 typedef struct cpd_server cpd_server;
 int cpd_server_create(cpd_context *ctx, uint64_t mem_budget_bytes, uint32_t slots,
                       uint32_t max_designs_per_pass, cpd_server **out);
-/* Queues n designs (one trace mode per request); returns a request id at once. */
+/* Queues n designs (one trace mode per request, optionally with
+ * CPD_SAMPLING_ADAPTIVE; a pass holds requests of one mode); returns a request id at
+ * once. */
 int cpd_server_submit(cpd_server *sv, const cpd_design *designs, const cpd_batch_item *items,
                       uint32_t n, uint32_t trace_mode, uint64_t *request_id);
 /* Waits up to timeout_ms for a request. On completion writes its n results, the time

@@ -656,13 +656,101 @@ typedef struct {
     double *p;          /* W*B */
     uint64_t hits;
     size_t k0, k1;
+    int adaptive;
+    uint32_t *counts;   /* W (adaptive): rays consumed per wavelength */
 } fixed_job;
+
+/* ------------------------------------ adaptive sampling on explicit point sets
+ *
+ * The per-wavelength stop of the reference GPU kernel (src/spectrometer/kernel.rs:
+ * 127-178): rays in the given order, 32 per round (the last round may be shorter; the
+ * reference rounds max_evals down to a multiple of 32, kernel.rs:137). After a round,
+ * each bin the round hit merges a Welford state of the round's samples (its hits' t, zeros
+ * for the other rays; kernel.rs:147-170, welford.rs:59-91); the wavelength stops after
+ * a round that hit some bin and after which every bin it hit passes
+ * sem_le_error_threshold with (5e-3)^2 (welford.rs:80-84, kernel.rs:170-178), and
+ * p(d|lambda) is the bin's mean over every ray consumed (Welford::skip, kernel.rs:181-189).
+ *
+ * The merges are done in exact arithmetic, on t quantized as the GPU quantizes it:
+ * t_fixed = round(2^31 t), t_q = t_fixed >> 11, so that M2 N = N sum t_q^2 - (sum t_q)^2
+ * and the test 40000 (N q2 - q1^2) < N^2 (N - 1) 2^40 are exact integers (the reference's
+ * f32 merges round; parity with that rounding is unpinned). */
+typedef unsigned __int128 orc_u128;
+
+static uint32_t orc_t_fixed(double t) { return (uint32_t)(t * 2147483648.0 + 0.5); }
+
+static int orc_sem_pass(uint64_t n, uint64_t q1, uint64_t q2)
+{
+    orc_u128 lhs = (orc_u128)40000u * ((orc_u128)n * q2 - (orc_u128)q1 * q1);
+    orc_u128 rhs = ((orc_u128)n * n * (n - 1u)) << 40;
+    return lhs < rhs;
+}
+
+typedef struct {
+    uint64_t s1, q1, q2, n;
+    size_t stamp;       /* last round that merged this bin, plus one */
+} orc_bin;
+
+static uint32_t adaptive_wavelength(const spectrometer *sp, double w, const double *ys, size_t R, orc_bin *st,
+                                    double *row, uint64_t *hits)
+{
+    uint32_t B = sp->det.bin_count;
+    for (uint32_t b = 0; b < B; b++) st[b].s1 = st[b].q1 = st[b].q2 = st[b].n = st[b].stamp = 0;
+    size_t count = 0;
+    size_t round = 0;
+    for (size_t r0 = 0; r0 < R; r0 += 32, round++) {
+        size_t nr = R - r0 < 32 ? R - r0 : 32;
+        uint32_t bins[32], tf[32];
+        int hit[32], any = 0;
+        count += nr;
+        for (size_t l = 0; l < nr; l++) {
+            double t;
+            hit[l] = spec_propagate(sp, ys[r0 + l], w, &bins[l], &t) == ORC_OK;
+            if (hit[l]) {
+                tf[l] = orc_t_fixed(t);
+                any = 1;
+                (*hits)++;
+            }
+        }
+        if (!any) continue;
+        /* every bin the round hit: merge, then test */
+        for (size_t l = 0; l < nr; l++)
+            if (hit[l]) {
+                orc_bin *bs = &st[bins[l]];
+                if (bs->stamp != round + 1) {
+                    bs->stamp = round + 1;
+                    bs->n += nr;
+                }
+                uint64_t q = tf[l] >> 11;
+                bs->s1 += tf[l];
+                bs->q1 += q;
+                bs->q2 += q * q;
+            }
+        int finished = 1;
+        for (size_t l = 0; l < nr; l++)
+            if (hit[l] && !orc_sem_pass(st[bins[l]].n, st[bins[l]].q1, st[bins[l]].q2)) finished = 0;
+        if (finished) break;
+    }
+    for (uint32_t b = 0; b < B; b++) row[b] = (double)st[b].s1 / ((double)count * 2147483648.0);
+    return (uint32_t)count;
+}
 
 static void *fixed_worker(void *arg)
 {
     fixed_job *j = (fixed_job *)arg;
     uint32_t B = j->sp->det.bin_count;
     uint64_t hits = 0;
+    if (j->adaptive) {
+        orc_bin *st = calloc(B, sizeof(orc_bin));
+        for (size_t k = j->k0; k < j->k1; k++) {
+            double w = sample_wavelength(j->sp, j->lam_u[k]);
+            uint32_t c = adaptive_wavelength(j->sp, w, j->ys, j->R, st, j->p + k * B, &hits);
+            if (j->counts) j->counts[k] = c;
+        }
+        free(st);
+        j->hits = hits;
+        return NULL;
+    }
     for (size_t k = j->k0; k < j->k1; k++) {
         double w = sample_wavelength(j->sp, j->lam_u[k]);
         double *row = j->p + k * B;
@@ -681,8 +769,26 @@ static void *fixed_worker(void *arg)
     return NULL;
 }
 
+static int fitness_points_impl(const orc_spec *s, const double *lam_u, size_t W, const double *ray_u, size_t R,
+                               int nthreads, double *p_out, double stats[4], uint64_t *hits_out, int adaptive,
+                               uint32_t *counts_out);
+
 int orc_fitness_points(const orc_spec *s, const double *lam_u, size_t W, const double *ray_u,
                        size_t R, int nthreads, double *p_out, double stats[4], uint64_t *hits_out)
+{
+    return fitness_points_impl(s, lam_u, W, ray_u, R, nthreads, p_out, stats, hits_out, 0, NULL);
+}
+
+int orc_fitness_adaptive_points(const orc_spec *s, const double *lam_u, size_t W, const double *ray_u, size_t R,
+                                int nthreads, double *p_out, double stats[4], uint64_t *hits_out,
+                                uint32_t *counts_out)
+{
+    return fitness_points_impl(s, lam_u, W, ray_u, R, nthreads, p_out, stats, hits_out, 1, counts_out);
+}
+
+static int fitness_points_impl(const orc_spec *s, const double *lam_u, size_t W, const double *ray_u, size_t R,
+                               int nthreads, double *p_out, double stats[4], uint64_t *hits_out, int adaptive,
+                               uint32_t *counts_out)
 {
     spectrometer sp;
     int e = build_spectrometer(s, &sp);
@@ -710,6 +816,8 @@ int orc_fitness_points(const orc_spec *s, const double *lam_u, size_t W, const d
         jobs[i].p = p;
         jobs[i].k0 = W * (size_t)i / (size_t)nthreads;
         jobs[i].k1 = W * (size_t)(i + 1) / (size_t)nthreads;
+        jobs[i].adaptive = adaptive;
+        jobs[i].counts = counts_out;
     }
     for (int i = 1; i < nthreads; i++) pthread_create(&th[i], NULL, fixed_worker, &jobs[i]);
     fixed_worker(&jobs[0]);

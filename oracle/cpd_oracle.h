@@ -104,6 +104,16 @@ int orc_p_dets_l_wavelength(const orc_spec *s, double wavelength, size_t max_m, 
 int orc_fitness_points(const orc_spec *s, const double *lam_u, size_t W, const double *ray_u,
                        size_t R, int nthreads, double *p_out, double stats[4], uint64_t *hits_out);
 
+/* Adaptive sampling on explicit point sets: the per-wavelength SEM stop of the
+ * reference GPU kernel (src/spectrometer/kernel.rs:127-178) with exact Welford merges on
+ * t_q = round(2^31 t) >> 11 (cpd_oracle.c states the rule). Rays are taken in the given
+ * order, 32 per round; p(d|lambda) = sum of t over the rays consumed / their number.
+ * counts_out (optional, W): rays consumed per wavelength. Other arguments as
+ * orc_fitness_points. */
+int orc_fitness_adaptive_points(const orc_spec *s, const double *lam_u, size_t W, const double *ray_u,
+                                size_t R, int nthreads, double *p_out, double stats[4], uint64_t *hits_out,
+                                uint32_t *counts_out);
+
 /* Per-ray twin of propagation_test_kernel (src/spectrometer/kernel.rs:195-224) in f64:
  * lambda = wmin + (wmax-wmin)*lam_u[i]; bin_count marks a lost ray. */
 int orc_trace_pairs(const orc_spec *s, const double *lam_u, const double *ray_u, size_t n,

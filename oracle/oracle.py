@@ -78,6 +78,8 @@ def lib():
         L.orc_p_dets_l_wavelength.argtypes = [sp, C.c_double, C.c_size_t, dp]
         L.orc_fitness_points.argtypes = [sp, dp, C.c_size_t, dp, C.c_size_t, C.c_int, dp, dp,
                                          C.POINTER(C.c_uint64)]
+        L.orc_fitness_adaptive_points.argtypes = [sp, dp, C.c_size_t, dp, C.c_size_t, C.c_int, dp, dp,
+                                                  C.POINTER(C.c_uint64), up]
         L.orc_trace_pairs.argtypes = [sp, dp, dp, C.c_size_t, up, dp]
         _lib = L
     return _lib
@@ -193,6 +195,24 @@ def fitness_points(d: dict, lam_u, ray_u, nthreads: int = 1, want_p: bool = True
     assert e == OK, e
     return p, {"info": float(st[0]), "h_cond": float(st[1]), "h_det": float(st[2]),
                "size": float(st[3]), "hits": int(hits.value)}
+
+
+def fitness_adaptive_points(d: dict, lam_u, ray_u, nthreads: int = 1):
+    """Adaptive sampling on explicit points (rays in the given order, 32 per round).
+    Returns (p[W,B], stats dict, counts[W] = rays consumed per wavelength)."""
+    s = make_spec(d)
+    lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
+    ray_u = np.ascontiguousarray(ray_u, dtype=np.float64)
+    W, R, B = lam_u.size, ray_u.size, int(d["bin_count"])
+    p = np.zeros((W, B))
+    st = np.zeros(4)
+    hits = C.c_uint64(0)
+    counts = np.zeros(W, dtype=np.uint32)
+    e = lib().orc_fitness_adaptive_points(C.byref(s), _dp(lam_u), W, _dp(ray_u), R, int(nthreads), _dp(p),
+                                          _dp(st), C.byref(hits), counts.ctypes.data_as(C.POINTER(C.c_uint32)))
+    assert e == OK, e
+    return p, {"info": float(st[0]), "h_cond": float(st[1]), "h_det": float(st[2]),
+               "size": float(st[3]), "hits": int(hits.value)}, counts
 
 
 def trace_pairs(d: dict, lam_u, ray_u):

@@ -10,6 +10,8 @@
 //
 // usage: fastpath_check design.bin W R lam_u.bin ray_u.bin
 // prints: rays <n> mismatches <m> flagged <f> outside_band_hits <h> df_mismatches <d>
+//         fast_t_relerr_e9 <e> (largest relative t error of a fast-path hit, x 1e9, rounded up)
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -41,6 +43,7 @@ int main(int argc, char **argv)
     std::vector<float> z32;
     ray_table(ru.data(), R, z64, z32);
     long n = 0, mism = 0, flag = 0, outside = 0, dfmism = 0;
+    double terr = 0.0;  // largest |t_fast - t| / t over fast-path hits
     for (int k = 0; k < W; k++) {
         const double lam = x::wavelength(D, lu[k]);
         LamParams P;
@@ -70,9 +73,10 @@ int main(int argc, char **argv)
                 continue;
             }
             if ((r == RAY_HIT) != (e == 0) || (r == RAY_HIT && bf != b)) mism++;
+            if (r == RAY_HIT && e == 0) terr = std::fmax(terr, std::fabs((double)tf - t) / t);
         }
     }
-    std::printf("rays %ld mismatches %ld flagged %ld outside_band_hits %ld df_mismatches %ld\n", n, mism, flag, outside,
-                dfmism);
+    std::printf("rays %ld mismatches %ld flagged %ld outside_band_hits %ld df_mismatches %ld fast_t_relerr_e9 %ld\n", n,
+                mism, flag, outside, dfmism, (long)std::ceil(terr * 1e9));
     return 0;
 }
