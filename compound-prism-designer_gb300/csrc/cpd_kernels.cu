@@ -437,91 +437,131 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 
 constexpr int kEntropyThreads = 256;
 
-// Per-design finalize by one warp: H(D) from the
-// per-bin sums, MI, and the SEM stop of cuda_fitness (src/cuda_fitness.rs:392-422).
-// f64 costs ~64 cycles per warp instruction here, so pbar log2 pbar is formed in
-// float-float on the FP32 pipe: pbar = S1 / (n R 2^31) and log2 pbar = log2 S1 -
-// log2(n R) - 31, both logs of integers (ff::log2_u64, absolute error < 1e-12). Only the
-// Welford M2 of each bin and the final SEM square root are f64.
+// Per-design finalize by one warp: H(D) from the per-bin sums, MI, and the SEM stop of
+// cuda_fitness (src/cuda_fitness.rs:392-422). f64 costs ~64 cycles per warp instruction
+// here (a division or square root ~700 cycles of latency), and this warp is the tail of
+// the plain call, so everything is float-float on the FP32 pipe: pbar = S1 / (n R 2^31),
+// log2 pbar = log2 S1 - log2(n R) - 31 (logs of integers, ff::log2_u64, absolute error
+// < 1e-12), and the Welford M2 of each bin, S2 - S1^2 / n, against (5e-3)^2 n (n - 1).
+// Only the conversion of the three results to double is f64.
 __device__ void finalize_warp(const LaunchArgs &a, uint32_t d, const DesignJob &J, uint32_t lane, const float *tab)
 {
-    {
-        const unsigned long long rows = __ldcg(&a.acc[d].rows) + J.W;
-        const double n = (double)rows;
-        const double inv_n = 1.0 / n;
-        const double p_unit = kTScaleInv / (double)J.R;  // p per count unit
-        const double thr = 5e-3 * 5e-3 * (n * (n - 1.0));
-        // 1 / (n R 2^31) and log2(n R) + 31 as float-float
-        const unsigned long long nR = rows * (unsigned long long)J.R;
-        float ih, il;
-        {
-            const double inr = p_unit * inv_n;
-            ih = (float)inr;
-            il = (float)(inr - (double)ih);
+    using ff::F2;
+    const unsigned long long rows = __ldcg(&a.acc[d].rows) + J.W;
+    const F2 n = ff::from_u64(rows);
+    const F2 inv_n = df::rcp(n);
+    const F2 unit{J.unit_hi, J.unit_lo};  // p per count unit, 2^-31 / R
+    const F2 inv_nr = ff::mul(unit, inv_n);
+    const unsigned long long nR = rows * (unsigned long long)J.R;
+    const F2 lnr = ff::add_f(ff::log2_u64(nR, tab), 31.f);
+    const F2 thr = df::div(ff::mul(n, ff::from_u64(rows - 1ull)), df::c(40000.f));  // (5e-3)^2 n (n - 1)
+    const F2 s2unit{(float)kPScaleInv, 0.f};
+    F2 hdet{0.f, 0.f};
+    float m2max = 0.f;
+    int conv = 1;
+    for (uint32_t b = lane; b < J.B; b += 32u) {
+        const unsigned long long c1 = __ldcg(&a.S1[J.acc_off + b]);
+        const F2 sc1 = ff::from_u64(c1);
+        if (c1) {
+            const F2 pbar = ff::mul(sc1, inv_nr);
+            const F2 lg = ff::add(ff::log2_u64(c1, tab), F2{-lnr.hi, -lnr.lo});
+            hdet = ff::add(hdet, ff::mul(pbar, lg));
         }
-        const ff::F2 inv_nr{ih, il};
-        const ff::F2 lnr = ff::add_f(ff::log2_u64(nR, tab), 31.f);
-        ff::F2 hdet{0.f, 0.f};
-        double m2max = 0.0;
-        int conv = 1;
-        for (uint32_t b = lane; b < J.B; b += 32u) {
-            const unsigned long long c1 = __ldcg(&a.S1[J.acc_off + b]);
-            if (c1) {
-                const ff::F2 pbar = ff::mul(ff::from_u64(c1), inv_nr);
-                const ff::F2 lg = ff::add(ff::log2_u64(c1, tab), ff::F2{-lnr.hi, -lnr.lo});
-                hdet = ff::add(hdet, ff::mul(pbar, lg));
-            }
-            // Welford M2 of the per-wavelength p(d|lambda) (welford.rs:26-57)
-            const double s1 = (double)c1 * p_unit;  // sum over rows of p
-            const double s2 = (double)__ldcg(&a.S2[J.acc_off + b]) * kPScaleInv;
-            double m2 = s2 - s1 * s1 * inv_n;
-            if (m2 < 0.0) m2 = 0.0;
-            conv &= (m2 < thr) ? 1 : 0;
-            m2max = fmax(m2max, m2);
-        }
+        // Welford M2 of the per-wavelength p(d|lambda) (welford.rs:26-57)
+        const F2 s1 = ff::mul(sc1, unit);  // sum over rows of p
+        const F2 s2 = ff::mul(ff::from_u64(__ldcg(&a.S2[J.acc_off + b])), s2unit);
+        F2 m2 = df::sub(s2, ff::mul(ff::mul(s1, s1), inv_n));
+        if (df::neg_(m2)) m2 = F2{0.f, 0.f};
+        conv &= df::lt(m2, thr) ? 1 : 0;
+        m2max = fmaxf(m2max, m2.hi);
+    }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const ff::F2 other{__shfl_xor_sync(0xffffffffu, hdet.hi, o), __shfl_xor_sync(0xffffffffu, hdet.lo, o)};
-            // the same pairs are added in the same order on every lane: a fixed tree
-            hdet = (lane & (uint32_t)o) ? ff::add(other, hdet) : ff::add(hdet, other);
-            m2max = fmax(m2max, __shfl_xor_sync(0xffffffffu, m2max, o));
-        }
-        conv = __all_sync(0xffffffffu, conv);
-        const bool cp = lane < (uint32_t)kSpread;
-        const unsigned long long hits = warp_sum_u64(cp ? __ldcg(&a.acc[d].hits[lane]) : 0ull);
-        const unsigned long long retraced = warp_sum_u64(cp ? __ldcg(&a.acc[d].retraced[lane]) : 0ull);
-        const unsigned long long fast = warp_sum_u64(cp ? __ldcg(&a.acc[d].fast[lane]) : 0ull);
-        if (lane == 0) {
-            const double H = (double)__ldcg(&a.acc[d].H) * kHScaleInv;
-            const double h_cond = -H * inv_n;
-            const double h_det = (double)hdet.hi + (double)hdet.lo;
-            DesignOut o;
-            o.h_cond = h_cond;
-            o.h_det = h_det;
-            o.info = h_cond - h_det;
-            o.max_sem = n > 1.0 ? sqrt(m2max / (n - 1.0) * inv_n) : INFINITY;
-            o.hits = hits;
-            o.retraced = retraced;
-            o.rows = rows;
-            o.fast = fast;
-            o.converged = conv;
-            o.pad = 0;
-            a.out[d] = o;
-            a.acc[d].rows = rows;
-        }
+    for (int o = 16; o > 0; o >>= 1) {
+        const F2 other{__shfl_xor_sync(0xffffffffu, hdet.hi, o), __shfl_xor_sync(0xffffffffu, hdet.lo, o)};
+        // the same pairs are added in the same order on every lane: a fixed tree
+        hdet = (lane & (uint32_t)o) ? ff::add(other, hdet) : ff::add(hdet, other);
+        m2max = fmaxf(m2max, __shfl_xor_sync(0xffffffffu, m2max, o));
+    }
+    conv = __all_sync(0xffffffffu, conv);
+    const bool cp = lane < (uint32_t)kSpread;
+    const unsigned long long hits = warp_sum_u64(cp ? __ldcg(&a.acc[d].hits[lane]) : 0ull);
+    const unsigned long long retraced = warp_sum_u64(cp ? __ldcg(&a.acc[d].retraced[lane]) : 0ull);
+    const unsigned long long fast = warp_sum_u64(cp ? __ldcg(&a.acc[d].fast[lane]) : 0ull);
+    if (lane == 0) {
+        const F2 H = ff::mul(ff::from_u64(__ldcg(&a.acc[d].H)), F2{(float)kHScaleInv, 0.f});
+        const F2 hc = ff::mul(H, inv_n);
+        const F2 h_cond{-hc.hi, -hc.lo};
+        const F2 info = df::sub(h_cond, hdet);
+        DesignOut o;
+        o.h_cond = (double)h_cond.hi + (double)h_cond.lo;
+        o.h_det = (double)hdet.hi + (double)hdet.lo;
+        o.info = (double)info.hi + (double)info.lo;
+        const float fn = (float)rows;
+        o.max_sem = rows > 1ull ? (double)sqrtf(m2max / (fn - 1.f) / fn) : (double)INFINITY;
+        o.hits = hits;
+        o.retraced = retraced;
+        o.rows = rows;
+        o.fast = fast;
+        o.converged = conv;
+        o.pad = 0;
+        a.out[d] = o;
+        a.acc[d].rows = rows;
     }
 }
 
-// Entropy sums of the rows [r0, r1) of one design by one warp. Lane -> (bin, row phase):
-// for B <= 32 the lanes split into 32/B row phases of one bin each; for wider detectors
-// a lane owns bins lane, lane+32, ... of every row, NB of them per sweep. Every partial
-// sum is therefore fixed by B and the tile alone, whatever else shares the launch, and
-// is converted to fixed point before it is added across lanes, tiles and designs. Each
-// step reads 8/NB rows x NB bins, so eight loads per lane are in flight; each nonzero
-// cell is zeroed after it is read, which leaves the histogram clear for the next pass.
+// A non-negative float-float value in fixed point with `scale` units, its hi and lo
+// words rounded separately: one rounding per cell, so that the sums over cells are integer
+// sums whose value does not depend on how the cells are grouped.
+// The conversions are 32-bit or exact bit arithmetic: 64-bit float-to-integer conversions
+// issue to the FP64 unit, ~64 cycles per warp instruction on this GPU.
+__device__ __forceinline__ unsigned long long df_to_fixed(ff::F2 v, float scale)
+{
+    const float x = v.hi * scale;  // >= 0, below 2^47
+    unsigned long long q;
+    if (x < 2147483648.0f) {
+        q = __float2uint_rn(x);
+    } else {
+        // at or above 2^31 a float is an integer: its significand shifted by its exponent
+        const uint32_t bits = __float_as_uint(x);
+        q = (unsigned long long)((bits & 0x7fffffu) | 0x800000u) << (((bits >> 23) & 0xffu) - 150u);
+    }
+    // |lo| is below half an ulp of hi: |lo scale| < 2^23
+    const long long r = (long long)q + __float2int_rn(v.lo * scale);
+    return r > 0 ? (unsigned long long)r : 0ull;
+}
+
+// One nonzero cell of the histogram: -p log2 p (2^-40 units) and p^2 (2^-46 units) in
+// fixed point, p = c 2^-31 / R in float-float on the FP32 pipe.
+__device__ __forceinline__ void entropy_cell(unsigned long long cv, ff::F2 unit, ff::F2 lu, const float *tab,
+                                             unsigned long long &hq, unsigned long long &pq)
+{
+    const ff::F2 p = ff::mul(ff::from_u64(cv), unit);
+    const ff::F2 lp = ff::add(ff::log2_u64(cv, tab), lu);
+    const ff::F2 plp = ff::mul(p, lp);  // p log2 p <= 0
+    hq = df_to_fixed(ff::F2{-plp.hi, -plp.lo}, (float)kHScale);
+    pq = df_to_fixed(ff::mul(p, p), (float)kPScale);
+}
+
+// The finalize of a single-design pass, folded into the entropy kernel: the warp that
+// accounts the design's last tile runs it (after the fences that publish every tile's sums).
+__device__ __forceinline__ bool last_tile_of_design(const LaunchArgs &a, const DesignJob &J, uint32_t lane)
+{
+    __threadfence();
+    unsigned last = 0;
+    if (lane == 0) last = atomicAdd(&a.ctl->tiles_done, 1u) == J.ntiles - 1u ? 1u : 0u;
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (last) __threadfence();
+    return last != 0u;
+}
+
+// Entropy sums of the rows [r0, r1) of one design by one warp (the form for passes with
+// many tiles: no block-level synchronization). Lane -> (bin, row phase): for B <= 32 the
+// lanes split into 32/B row phases of one bin each; for wider detectors a lane owns bins
+// lane, lane+32, ... of every row, NB of them per sweep. Each step reads 8/NB rows x NB
+// bins, so eight loads per lane are in flight.
 template <int NB>
 __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJob &J, uint32_t r0, uint32_t r1,
-                                             uint32_t lane, const float *tab, ff::F2 &h)
+                                             uint32_t lane, const float *tab, unsigned long long &hl)
 {
     constexpr uint32_t RS = 8u / NB;
     const uint32_t B = J.B;
@@ -529,17 +569,12 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
     const uint32_t grp = B <= 32u ? lane / B : 0u;
     const uint32_t bin0 = B <= 32u ? lane % B : lane;
     const bool active = grp < groups;
-    const double p_unit = kTScaleInv / (double)J.R;
     const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
     unsigned long long *base = a.hist + J.hist_off;
     for (uint32_t bg = 0; bg < B; bg += 32u * NB) {
-        unsigned long long c1[NB];
-        ff::F2 q2[NB];
+        unsigned long long c1[NB], q2[NB];
 #pragma unroll
-        for (int i = 0; i < NB; i++) {
-            c1[i] = 0ull;
-            q2[i] = ff::F2{0.f, 0.f};
-        }
+        for (int i = 0; i < NB; i++) c1[i] = q2[i] = 0ull;
         for (uint32_t row = r0 + grp; row < r1; row += RS * groups) {
             unsigned long long c[RS * NB];
 #pragma unroll
@@ -551,8 +586,7 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
                     c[rr * NB + i] = (active && rw < r1 && b < B) ? base[(uint64_t)rw * B + b] : 0ull;
                 }
             }
-            // one copy of the cell code, not RS x NB: the plain call runs each tile once,
-            // so instruction fetch is what an unrolled body would cost
+            // one copy of the cell code, not RS x NB (instruction fetch)
 #pragma unroll 1
             for (uint32_t q = 0; q < RS * NB; q++) {
                 const uint32_t rw = row + (q / NB) * groups;
@@ -561,19 +595,18 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
                 const unsigned long long cv = c[q];
                 if (cv) {
                     base[(uint64_t)rw * B + b] = 0ull;
-                    // p = c unit and p log2 p in float-float (FP32 pipe)
-                    const ff::F2 p = ff::mul(ff::from_u64(cv), unit);
-                    const ff::F2 lp = ff::add(ff::log2_u64(cv, tab), lu);
-                    h = ff::add(h, ff::mul(p, lp));
-                    const ff::F2 pp = ff::mul(p, p);
+                    unsigned long long hq, pq;
+                    entropy_cell(cv, unit, lu, tab, hq, pq);
+                    hl += hq;
 #pragma unroll
                     for (int ii = 0; ii < NB; ii++)
                         if (ii == (int)i) {
-                            q2[ii] = ff::add(q2[ii], pp);
+                            q2[ii] += pq;
                             c1[ii] += cv;
                         }
                 }
-                if (a.p_out && active && rw < r1 && b < B) a.p_out[(uint64_t)rw * B + b] = (double)cv * p_unit;
+                if (a.p_out && active && rw < r1 && b < B)
+                    a.p_out[(uint64_t)rw * B + b] = (double)cv * (kTScaleInv / (double)J.R);
             }
         }
 #pragma unroll
@@ -581,15 +614,14 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
             const uint32_t b = bg + bin0 + 32u * (uint32_t)i;
             if (c1[i]) {
                 atomicAdd(&a.S1[J.acc_off + b], c1[i]);
-                atomicAdd(&a.S2[J.acc_off + b], __double2ull_rn(((double)q2[i].hi + (double)q2[i].lo) * kPScale));
+                atomicAdd(&a.S2[J.acc_off + b], q2[i]);
             }
         }
     }
 }
 
-// One warp per entropy tile: kTileCells cells of one design (tile_rows = kTileCells / B
-// rows, at least one).
-__global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const LaunchArgs a)
+// One warp per tile.
+__global__ void __launch_bounds__(kEntropyThreads, 2) entropy_warp_kernel(const LaunchArgs a)
 {
     __shared__ float tab[4 * ff::kLogTable];
     cudaTriggerProgrammaticLaunchCompletion();
@@ -607,24 +639,98 @@ __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_kernel(const Launc
         const uint32_t r0 = (uint32_t)(tile - J.tile_off) * J.tile_rows;
         const uint32_t r1 = min(r0 + J.tile_rows, J.W);
         const uint32_t nb = (J.B + 31u) / 32u;  // bins per lane
-        ff::F2 h{0.f, 0.f};
-        if (nb >= 3u) entropy_tile<4>(a, J, r0, r1, lane, tab, h);
-        else if (nb == 2u) entropy_tile<2>(a, J, r0, r1, lane, tab, h);
-        else entropy_tile<1>(a, J, r0, r1, lane, tab, h);
-        const unsigned long long hl = warp_sum_u64(__double2ull_rn(-((double)h.hi + (double)h.lo) * kHScale));
+        unsigned long long hl = 0ull;
+        if (nb >= 3u) entropy_tile<4>(a, J, r0, r1, lane, tab, hl);
+        else if (nb == 2u) entropy_tile<2>(a, J, r0, r1, lane, tab, hl);
+        else entropy_tile<1>(a, J, r0, r1, lane, tab, hl);
+        hl = warp_sum_u64(hl);
         if (lane == 0 && hl) atomicAdd(&a.acc[d].H, hl);
+        if (a.njobs == 1 && last_tile_of_design(a, J, lane)) finalize_warp(a, d, J, lane, tab);
+    }
+}
+
+// One block per entropy tile (tile_rows rows of one design, at most kTileCells cells),
+// the form for passes with few tiles (the plain call), where one warp per tile would
+// leave most SMs idle: thread t takes cells t, t + 256, ... of the tile in row-major order,
+// and the tile's per-bin sums meet in shared memory, then one global atomic per bin and
+// sum. In both forms each cell's terms are rounded to fixed point once (entropy_cell), so
+// every sum is independent of the grouping of cells into threads, tiles and launches,
+// and each nonzero cell is zeroed after it is read, which leaves the histogram clear for
+// the next pass.
+__global__ void __launch_bounds__(kEntropyThreads, 4) entropy_block_kernel(const LaunchArgs a)
+{
+    __shared__ float tab[4 * ff::kLogTable];
+    extern __shared__ __align__(16) unsigned long long ent_smem[];  // per-bin s1, s2 (max_B each)
+    __shared__ unsigned long long hsum;
+    __shared__ unsigned last_tile;
+    cudaTriggerProgrammaticLaunchCompletion();
+    for (uint32_t i = threadIdx.x; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
+    __syncthreads();
+    cudaGridDependencySynchronize();  // the histogram of the trace and re-trace kernels
+    // A pass whose re-trace queue overflowed is re-run by the host: leave every
+    // accumulator untouched.
+    if (a.ctl->overflow || a.ctl->queue_count > a.qcap) return;
+    const uint32_t t = threadIdx.x, lane = t & 31u;
+    for (uint64_t tile = blockIdx.x; tile < a.total_tiles; tile += gridDim.x) {
+        const uint32_t d = find_job<F_TILE>(a.jobs, a.njobs, tile);
+        const DesignJob J = a.jobs[d];
+        const uint32_t B = J.B;
+        const uint32_t r0 = (uint32_t)(tile - J.tile_off) * J.tile_rows;
+        const uint32_t r1 = min(r0 + J.tile_rows, J.W);
+        unsigned long long *s1 = ent_smem, *s2 = ent_smem + B;
+        for (uint32_t b = t; b < B; b += kEntropyThreads) s1[b] = s2[b] = 0ull;
+        if (t == 0) hsum = 0ull;
+        __syncthreads();
+        const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
+        unsigned long long *base = a.hist + J.hist_off;
+        const uint32_t cells = (r1 - r0) * B;
+        const uint32_t db = (uint32_t)kEntropyThreads % B, dr = (uint32_t)kEntropyThreads / B;
+        uint32_t b = t % B, row = r0 + t / B;
+        unsigned long long hl = 0ull;
+        for (uint32_t i = t; i < cells; i += kEntropyThreads) {
+            const uint64_t idx = (uint64_t)row * B + b;
+            const unsigned long long cv = base[idx];
+            if (cv) {
+                base[idx] = 0ull;
+                unsigned long long hq, pq;
+                entropy_cell(cv, unit, lu, tab, hq, pq);
+                hl += hq;
+                atomicAdd(s1 + b, cv);
+                atomicAdd(s2 + b, pq);
+            }
+            if (a.p_out) a.p_out[idx] = (double)cv * (kTScaleInv / (double)J.R);
+            b += db;
+            row += dr;
+            if (b >= B) {
+                b -= B;
+                row++;
+            }
+        }
+        hl = warp_sum_u64(hl);
+        if (lane == 0 && hl) atomicAdd(&hsum, hl);
+        __syncthreads();
+        for (uint32_t bb = t; bb < B; bb += kEntropyThreads) {
+            const unsigned long long v1 = s1[bb];
+            if (v1) {
+                atomicAdd(&a.S1[J.acc_off + bb], v1);
+                atomicAdd(&a.S2[J.acc_off + bb], s2[bb]);
+            }
+        }
+        if (t == 0 && hsum) atomicAdd(&a.acc[d].H, hsum);
         if (a.njobs == 1) {
-            // a single design (the plain call): the warp that finishes its last tile runs
+            // a single design (the plain call): the block that finishes the last tile runs
             // the finalize, which saves a launch; with many designs the per-tile fences
             // would cost more than the separate finalize kernel
             __threadfence();
-            unsigned last = 0;
-            if (lane == 0) last = atomicAdd(&a.ctl->tiles_done, 1u) == J.ntiles - 1u ? 1u : 0u;
-            if (__shfl_sync(0xffffffffu, last, 0)) {
+            __syncthreads();
+            if (t == 0) last_tile = atomicAdd(&a.ctl->tiles_done, 1u) == J.ntiles - 1u ? 1u : 0u;
+            __syncthreads();
+            if (last_tile && t < 32u) {
                 __threadfence();
                 finalize_warp(a, d, J, lane, tab);
             }
         }
+        __syncthreads();  // the shared sums are reused by the block's next tile
     }
 }
 
@@ -763,7 +869,7 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         launches++;
     }
     if (a.adaptive) {
-        const size_t smem = bin_state_bytes(a.max_B ? a.max_B : 1u);
+        const size_t smem = bin_state_bytes(a.max_B ? a.max_B : (uint32_t)CPD_MAX_BINS);
         if (ev) cudaEventRecord(ev[1], stream);
         if (a.total_rows) {
             // enough rows to fill the GPU: one warp per row; fewer: up to kMaxAdaptWarps
@@ -796,14 +902,25 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     }
     if (ev) cudaEventRecord(ev[3], stream);
     if (a.total_tiles) {
-        // one warp per tile, as many blocks as are resident at once
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, entropy_kernel, kEntropyThreads, 0);
-        if (per_sm < 1) per_sm = 1;
         const uint64_t wpb = (uint64_t)kEntropyThreads / 32u;
-        uint64_t grid = (a.total_tiles + wpb - 1) / wpb;
-        if (grid > (uint64_t)num_sms * per_sm) grid = (uint64_t)num_sms * per_sm;
-        launch_k(entropy_kernel, (unsigned)grid, kEntropyThreads, 0, stream, pdl, a);
+        if (a.total_tiles <= (uint64_t)num_sms * wpb) {
+            // few tiles: one block per tile
+            const size_t smem = 2u * sizeof(unsigned long long) * (a.max_B ? a.max_B : (uint32_t)CPD_MAX_BINS);
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, entropy_block_kernel, kEntropyThreads, smem);
+            if (per_sm < 1) per_sm = 1;
+            uint64_t grid = a.total_tiles;
+            if (grid > (uint64_t)num_sms * per_sm) grid = (uint64_t)num_sms * per_sm;
+            launch_k(entropy_block_kernel, (unsigned)grid, kEntropyThreads, smem, stream, pdl, a);
+        } else {
+            // one warp per tile, as many blocks as are resident at once
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, entropy_warp_kernel, kEntropyThreads, 0);
+            if (per_sm < 1) per_sm = 1;
+            uint64_t grid = (a.total_tiles + wpb - 1) / wpb;
+            if (grid > (uint64_t)num_sms * per_sm) grid = (uint64_t)num_sms * per_sm;
+            launch_k(entropy_warp_kernel, (unsigned)grid, kEntropyThreads, 0, stream, pdl, a);
+        }
         launches++;
     }
     if (a.njobs > 1 || !a.total_tiles) {

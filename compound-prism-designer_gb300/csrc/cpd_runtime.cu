@@ -109,6 +109,13 @@ struct PassSlot {
     bool hist_dirty = true;
     uint32_t qcap = 1u << 18;
     std::vector<uint8_t> graph_key;
+    // The wavelength-point and ray tables (the arena after the designs and jobs) of the
+    // last pass, when they came from the context's caches: identity of each table in
+    // upload order, and references that keep those tables (and so their addresses)
+    // alive. A pass with the same key leaves them in place and uploads the designs and
+    // jobs only.
+    std::vector<const void *> tables_key;
+    std::vector<std::shared_ptr<const void>> tables_refs;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_launches = 0;
     // the pass in flight / last finished
@@ -195,11 +202,18 @@ RayTablePtr ray_table_cached(cpd_context *ctx, double seed, uint32_t R)
 }
 
 // The wavelength u-points of the GPU seed policy, u_i = fract(fma(i, 1/phi, seed)),
-// cached per (seed, W) like the ray tables (an optimizer reuses its seeds).
-std::shared_ptr<const std::vector<double>> lam_points_cached(cpd_context *ctx, double seed, uint32_t W)
+// cached per seed like the ray tables (an optimizer reuses its seeds). The points of W
+// wavelengths are the first W of any longer table of the same seed, so one table of
+// max(1024, W rounded up to a power of two) points serves every W up to its length:
+// the designs of a batch with mixed W share a few tables.
+using LamPtr = std::shared_ptr<const std::vector<double>>;
+LamPtr lam_points_cached(cpd_context *ctx, double seed, uint32_t W)
 {
     uint64_t bits;
     std::memcpy(&bits, &seed, 8);
+    uint32_t L = 1024;
+    while (L < W) L <<= 1;
+    W = L;
     RayKey key{bits, W};
     {
         std::lock_guard<std::mutex> lk(ctx->cache_mu);
@@ -213,12 +227,15 @@ std::shared_ptr<const std::vector<double>> lam_points_cached(cpd_context *ctx, d
     return ctx->lam_cache.emplace(key, v).first->second;
 }
 
-// One design's sampling inputs for a pass.
+// One design's sampling inputs for a pass. lam_keep / rays_keep: set when lam_u / rays are
+// immutable tables of the context's caches (their device copies may then stay resident).
 struct PassDesign {
     const DevDesign *dev;      // host copy
     uint32_t W, R;
-    const double *lam_u;       // W wavelength u-points (host)
+    const double *lam_u;       // W wavelength u-points (host), the first W of lam_len
     const RayTable *rays;
+    std::shared_ptr<const void> lam_keep = nullptr, rays_keep = nullptr;
+    uint32_t lam_len = 0;      // length of the lam_u table (0: W)
 };
 
 struct PassResult {
@@ -248,7 +265,12 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     mode &= ~kSamplingBits;
     std::vector<DesignJob> jobs(n);
     std::vector<uint8_t> owns_rays(n, 1);  // designs that share a ray table share its copy
+    std::vector<uint8_t> owns_lam(n, 1);   // likewise for wavelength-point tables
     std::map<const RayTable *, std::pair<uint64_t, uint64_t>> ray_offs;
+    std::map<std::pair<const double *, uint32_t>, uint64_t> lam_offs;
+    // identity of the tables in upload order (null entries: not from a cache)
+    std::vector<const void *> tables_key;
+    bool cacheable = true;
     uint64_t rows = 0, hist = 0, lam = 0, ray = 0, rnk = 0, accc = 0, items = 0, tiles = 0;
     uint32_t max_B = 0;
     for (uint32_t i = 0; i < n; i++) {
@@ -261,11 +283,23 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         J.B = p.dev->B;
         J.row_off = rows;
         J.hist_off = hist;
-        J.lam_off = lam;
+        const uint32_t lam_len = std::max(p.lam_len, p.W);
+        auto lo = lam_offs.emplace(std::make_pair(p.lam_u, lam_len), lam);
+        J.lam_off = lo.first->second;
+        owns_lam[i] = lo.second;
+        if (owns_lam[i]) {
+            lam += lam_len;
+            tables_key.push_back(p.lam_u);
+            cacheable = cacheable && p.lam_keep;
+        }
         auto ro = ray_offs.emplace(p.rays, std::make_pair(ray, rnk));
         J.ray_off = ro.first->second.first;
         J.rank_off = ro.first->second.second;
         owns_rays[i] = ro.second;
+        if (owns_rays[i]) {
+            tables_key.push_back(p.rays);
+            cacheable = cacheable && p.rays_keep;
+        }
         max_B = std::max(max_B, J.B);
         J.acc_off = accc;
         J.item_off = items;
@@ -277,7 +311,6 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         ff::split(-31.0 - std::log2((double)J.R), J.lu_hi, J.lu_lo);
         rows += J.W;
         hist += (uint64_t)J.W * J.B;
-        lam += J.W;
         if (owns_rays[i]) {
             ray += (J.Rz + 1u) & ~1u;  // even: every table starts 16-byte aligned
             if (adaptive) rnk += J.R;
@@ -286,24 +319,37 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         items += (uint64_t)((J.W + 31) / 32) * J.nchunk;
         tiles += J.ntiles;
     }
-    // one input arena: designs | jobs | wavelength points | z64 | z32 | ranks (256-byte
-    // sections; the ranks only under adaptive sampling)
+    // one input arena: wavelength points | z64 | z32 | ranks | designs | jobs (256-byte
+    // sections; the ranks only under adaptive sampling). The tables come first, so their
+    // offsets depend on the tables alone and a pass that finds them resident uploads the
+    // tail from the designs on.
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t o_job = al(sizeof(DevDesign) * n);
-    const size_t o_lam = o_job + al(sizeof(DesignJob) * n);
+    const size_t o_lam = 0;
     const size_t o_z64 = o_lam + al(sizeof(double) * lam);
     const size_t o_z32 = o_z64 + al(sizeof(double) * ray);
     const size_t o_rank = o_z32 + al(2 * sizeof(float) * ray);
-    const size_t in_bytes = o_rank + al(sizeof(uint32_t) * rnk);
+    const size_t o_des = o_rank + al(sizeof(uint32_t) * rnk);
+    const size_t o_job = o_des + al(sizeof(DevDesign) * n);
+    const size_t in_bytes = o_job + al(sizeof(DesignJob) * n);
     const size_t ctl_off = al(sizeof(DesignOut) * n);
     const size_t out_bytes = ctl_off + sizeof(Control);
     CPD_TRY(S.h_in.ensure(in_bytes));
     CPD_TRY(S.h_outs.ensure(out_bytes));
+    const void *in_before = S.in.p;
+    CPD_TRY(S.in.ensure(in_bytes));
+    // the tables already on the device from the previous pass of this slot
+    tables_key.push_back(adaptive ? &kSamplingBits : nullptr);  // the rank section
+    tables_key.push_back(S.in.p);
+    const bool resident = cacheable && S.in.p == in_before && tables_key == S.tables_key;
+    const size_t up_off = resident ? o_des : 0, up_bytes = in_bytes - up_off;
     char *hin = S.h_in.as<char>();
     for (uint32_t i = 0; i < n; i++) {
-        reinterpret_cast<DevDesign *>(hin)[i] = *ds[i].dev;
+        reinterpret_cast<DevDesign *>(hin + o_des)[i] = *ds[i].dev;
         reinterpret_cast<DesignJob *>(hin + o_job)[i] = jobs[i];
-        std::memcpy(reinterpret_cast<double *>(hin + o_lam) + jobs[i].lam_off, ds[i].lam_u, sizeof(double) * ds[i].W);
+        if (resident) continue;
+        if (owns_lam[i])
+            std::memcpy(reinterpret_cast<double *>(hin + o_lam) + jobs[i].lam_off, ds[i].lam_u,
+                        sizeof(double) * std::max(ds[i].lam_len, ds[i].W));
         if (!owns_rays[i]) continue;
         std::memcpy(reinterpret_cast<double *>(hin + o_z64) + jobs[i].ray_off, ds[i].rays->z64.data(),
                     sizeof(double) * jobs[i].Rz);
@@ -313,10 +359,20 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
             std::memcpy(reinterpret_cast<uint32_t *>(hin + o_rank) + jobs[i].rank_off, ds[i].rays->rank.data(),
                         sizeof(uint32_t) * jobs[i].R);
     }
+    if (cacheable) {
+        S.tables_key = tables_key;
+        S.tables_refs.clear();
+        for (const PassDesign &p : ds) {
+            S.tables_refs.push_back(p.lam_keep);
+            S.tables_refs.push_back(p.rays_keep);
+        }
+    } else {
+        S.tables_key.clear();
+        S.tables_refs.clear();
+    }
     // device buffers
     const size_t hist_bytes = sizeof(unsigned long long) * std::max<uint64_t>(hist, 1);
     const size_t old_hist = S.hist.cap;
-    CPD_TRY(S.in.ensure(in_bytes));
     CPD_TRY(S.lp.ensure(sizeof(LamParams) * std::max<uint64_t>(rows, 1)));
     CPD_TRY(S.lx.ensure(sizeof(LamDF) * std::max<uint64_t>(rows, 1)));
     CPD_TRY(S.hist.ensure(hist_bytes));
@@ -334,13 +390,13 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         CPD_TRY(cudaMemsetAsync(S.hist.p, 0, S.hist.cap, s));
         S.hist_dirty = false;
     }
-    S.h2d += in_bytes;
+    S.h2d += up_bytes;
     S.d2h += out_bytes + (p_out_host ? sizeof(double) * hist : 0);
     char *din = S.in.as<char>();
 
     LaunchArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.designs = reinterpret_cast<const DevDesign *>(din);
+    a.designs = reinterpret_cast<const DevDesign *>(din + o_des);
     a.jobs = reinterpret_cast<const DesignJob *>(din + o_job);
     a.njobs = n;
     a.total_rows = rows;
@@ -379,12 +435,12 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     // timing events around the kernels -- is one graph, captured once per signature.
     std::vector<uint8_t> key(sizeof(a) + 6 * sizeof(uint64_t));
     std::memcpy(key.data(), &a, sizeof(a));
-    const uint64_t extra[6] = {n, ctx->warps_per_cta, (uint64_t)ctx->num_sms, in_bytes, out_bytes,
-                               fresh ? accc + 1 : 0};
+    const uint64_t extra[6] = {n, ctx->warps_per_cta, (uint64_t)ctx->num_sms, (in_bytes << 1) | (resident ? 1u : 0u),
+                               out_bytes, fresh ? accc + 1 : 0};
     std::memcpy(key.data() + sizeof(a), extra, sizeof(extra));
     auto record = [&](cudaStream_t st, bool capturing) -> int {
         const unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-        cudaMemcpyAsync(S.in.p, S.h_in.p, in_bytes, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(S.in.as<char>() + up_off, S.h_in.as<char>() + up_off, up_bytes, cudaMemcpyHostToDevice, st);
         if (fresh) {
             cudaMemsetAsync(S.S1.p, 0, sizeof(unsigned long long) * accc, st);
             cudaMemsetAsync(S.S2.p, 0, sizeof(unsigned long long) * accc, st);
@@ -584,7 +640,7 @@ int tune_pass(cpd_context *ctx, const std::vector<PassDesign> &ds, uint32_t mode
 
 // Builds the pass inputs of a batch (host copies kept alive by the caller's vectors).
 void batch_inputs(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items, uint32_t n,
-                  std::vector<DevDesign> &devs, std::vector<std::vector<double>> &lams, std::vector<RayTablePtr> &rts,
+                  std::vector<DevDesign> &devs, std::vector<LamPtr> &lams, std::vector<RayTablePtr> &rts,
                   std::vector<PassDesign> &ds)
 {
     devs.resize(n);
@@ -593,10 +649,10 @@ void batch_inputs(cpd_context *ctx, const cpd_design *designs, const cpd_batch_i
     ds.resize(n);
     for (uint32_t i = 0; i < n; i++) {
         design_to_dev(designs[i], devs[i]);
-        lams[i].resize(items[i].max_n);
-        seed_points(items[i].seed, 0, items[i].max_n, lams[i].data());
+        lams[i] = lam_points_cached(ctx, items[i].seed, items[i].max_n);
         rts[i] = ray_table_cached(ctx, items[i].seed, items[i].max_eval);
-        ds[i] = PassDesign{&devs[i], items[i].max_n, items[i].max_eval, lams[i].data(), rts[i].get()};
+        ds[i] = PassDesign{&devs[i], items[i].max_n, items[i].max_eval, lams[i]->data(), rts[i].get(), lams[i], rts[i],
+                           (uint32_t)lams[i]->size()};
     }
 }
 
@@ -704,7 +760,7 @@ void srv_loop(cpd_server *sv)
         for (size_t i = 0; i < sv->slots.size(); i++) {
             std::vector<SrvWork> take;
             std::vector<DevDesign> devs;
-            std::vector<std::vector<double>> lams;
+            std::vector<LamPtr> lams;
             std::vector<RayTablePtr> rays;
             uint32_t mode = 0;
             {
@@ -741,10 +797,10 @@ void srv_loop(cpd_server *sv)
                 }
                 const cpd_batch_item &it = r->items[take[k].idx];
                 design_to_dev(r->designs[take[k].idx], devs[k]);
-                lams[k].resize(it.max_n);
-                seed_points(it.seed, 0, it.max_n, lams[k].data());
+                lams[k] = lam_points_cached(sv->ctx, it.seed, it.max_n);
                 rays[k] = ray_table_cached(sv->ctx, it.seed, it.max_eval);
-                ds[k] = PassDesign{&devs[k], it.max_n, it.max_eval, lams[k].data(), rays[k].get()};
+                ds[k] = PassDesign{&devs[k], it.max_n, it.max_eval, lams[k]->data(), rays[k].get(), lams[k], rays[k],
+                                   (uint32_t)lams[k]->size()};
             }
             int e = pass_issue(sv->ctx, *sv->slots[i], ds, mode, true, nullptr, false, false);
             if (e) {
@@ -922,7 +978,8 @@ int cpd_fitness_gpu_ex(cpd_context *ctx, const cpd_design *d, const double *seed
     for (uint32_t s = 0; s < nseeds; s++) {
         const auto lam = lam_points_cached(ctx, seeds[s], max_n);
         RayTablePtr rt = ray_table_cached(ctx, seeds[s], max_eval);
-        std::vector<PassDesign> ds{PassDesign{&D, max_n, max_eval, lam->data(), rt.get()}};
+        std::vector<PassDesign> ds{
+            PassDesign{&D, max_n, max_eval, lam->data(), rt.get(), lam, rt, (uint32_t)lam->size()}};
         if (tune && s == 0) {
             // the autotuner replaces the reference's nwarp hint
             auto it = ctx->tune_cache.find(tune_class(ds, mode));
@@ -951,7 +1008,7 @@ int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd
         if (!valid_design(&designs[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
     CPD_SYNC_ENTRY(ctx);
     std::vector<DevDesign> devs;
-    std::vector<std::vector<double>> lams;
+    std::vector<LamPtr> lams;
     std::vector<RayTablePtr> rts;
     std::vector<PassDesign> ds;
     batch_inputs(ctx, designs, items, n, devs, lams, rts, ds);
@@ -982,7 +1039,7 @@ int cpd_autotune_batch(cpd_context *ctx, const cpd_design *designs, const cpd_ba
         if (!valid_design(&designs[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
     CPD_SYNC_ENTRY(ctx);
     std::vector<DevDesign> devs;
-    std::vector<std::vector<double>> lams;
+    std::vector<LamPtr> lams;
     std::vector<RayTablePtr> rts;
     std::vector<PassDesign> ds;
     batch_inputs(ctx, designs, items, n, devs, lams, rts, ds);

@@ -173,6 +173,7 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     a.qcap = kStaticQueue;
     a.ray_tile = ray_tile;
     a.mode = trace_mode;
+    a.max_B = J.B;
     if (trace_mode == CPD_TRACE_FP32) {
         a.guards = no_guards();
         a.yguard_rel = 0.0;
