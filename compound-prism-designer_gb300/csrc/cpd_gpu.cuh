@@ -45,6 +45,14 @@ struct Control {
     unsigned int tiles_done;  // entropy tiles finished (single-design passes)
 };
 
+// What the host reads of a pass's Control words, written by the re-trace kernel (the
+// last kernel to change them) into mapped host memory.
+struct HostStatus {
+    unsigned long long queue_count;
+    unsigned int overflow;
+    unsigned int pad;
+};
+
 // Copies of each per-design ray counter: thousands of warps add to the counters of one
 // design, and same-address atomics serialize in L2, so each warp adds to one of
 // kSpread copies and the finalize sums them.
@@ -87,8 +95,11 @@ struct LaunchArgs {
     unsigned long long *S1;
     unsigned long long *S2;
     DesignAcc *acc;
-    DesignOut *out;
+    DesignOut *out;       // results (mapped host memory in the context's passes)
     Control *ctl;
+    HostStatus *status;   // optional (mapped host memory)
+    uint32_t clear_acc;   // the setup kernel zeroes S1, S2 (acc_cells) and acc (njobs) first
+    uint64_t acc_cells;
     QEntry *queue;
     uint32_t qcap;
     uint32_t ray_tile;

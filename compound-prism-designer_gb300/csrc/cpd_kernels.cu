@@ -71,6 +71,16 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     // lets the trace kernel's blocks become resident now; they wait for this grid's
     // results in cudaGridDependencySynchronize
     cudaTriggerProgrammaticLaunchCompletion();
+    if (a.clear_acc) {
+        // a fresh pass: zero the per-bin and per-design accumulators (the kernels that add
+        // to them wait for this grid to complete)
+        const uint64_t gt = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+        const uint64_t nt = (uint64_t)gridDim.x * blockDim.x;
+        for (uint64_t i = gt; i < a.acc_cells; i += nt) a.S1[i] = a.S2[i] = 0ull;
+        unsigned long long *acc = reinterpret_cast<unsigned long long *>(a.acc);
+        const uint64_t words = (uint64_t)a.njobs * (sizeof(DesignAcc) / sizeof(unsigned long long));
+        for (uint64_t i = gt; i < words; i += nt) acc[i] = 0ull;
+    }
     __shared__ __align__(16) DevDesign sD;
     extern __shared__ __align__(16) float sz[];  // 2 kStageRays floats
     const uint64_t row0 = blockIdx.x * (uint64_t)blockDim.x;
@@ -173,10 +183,21 @@ __global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
 }
 
 // The queued rays, hybrid mode: the float-float re-trace.
+// The pass's final queue state for the host (no later kernel changes it).
+__device__ __forceinline__ void publish_status(const LaunchArgs &a)
+{
+    if (a.status && blockIdx.x == 0 && threadIdx.x == 0) {
+        a.status->queue_count = a.ctl->queue_count;
+        a.status->overflow = a.ctl->overflow;
+        a.status->pad = 0u;
+    }
+}
+
 __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
 {
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();  // the queue of the setup and trace kernels
+    publish_status(a);
     const unsigned long long qn = a.ctl->queue_count;
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -201,6 +222,7 @@ __global__ void __launch_bounds__(32) retrace_exact_kernel(const LaunchArgs a)
 {
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();  // the queue of the setup and trace kernels
+    publish_status(a);
     const unsigned long long qn = a.ctl->queue_count;
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -419,6 +441,7 @@ __global__ void __launch_bounds__(32) adaptive_exact_kernel(const LaunchArgs a)
     __shared__ RoundSlots rs;
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();  // the adaptive kernel's queue
+    publish_status(a);
     const unsigned long long qn = a.ctl->queue_count;
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
     for (uint64_t i = blockIdx.x; i < n; i += gridDim.x) {

@@ -52,16 +52,20 @@ struct DevBuf {
 
 struct HostBuf {
     void *p = nullptr;
+    void *dev = nullptr;  // the device's address of a mapped buffer
     size_t cap = 0;
-    cudaError_t ensure(size_t bytes)
+    // mapped: the GPU reads and writes the buffer in place (over NVLink-C2C on this
+    // machine), so a kernel can deliver results without a copy
+    cudaError_t ensure(size_t bytes, bool mapped = false)
     {
         if (bytes <= cap) return cudaSuccess;
         if (p) cudaFreeHost(p);
-        p = nullptr;
+        p = dev = nullptr;
         cap = 0;
         size_t want = std::max<size_t>(bytes, 256);
         want = want + want / 4;
-        cudaError_t e = cudaMallocHost(&p, want);
+        cudaError_t e = cudaHostAlloc(&p, want, mapped ? cudaHostAllocMapped : cudaHostAllocDefault);
+        if (e == cudaSuccess && mapped) e = cudaHostGetDevicePointer(&dev, p, 0);
         if (e == cudaSuccess) cap = want;
         return e;
     }
@@ -101,8 +105,9 @@ struct PassSlot {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
     cudaEvent_t kev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    // inputs (designs, jobs, wavelength points, ray tables) in one arena, uploaded with one
-    // copy; outputs (DesignOut[n] then Control) in one buffer, read back with one copy
+    // inputs (tables, designs, jobs) in one arena, uploaded with one copy; results
+    // (DesignOut[n] then HostStatus) written by the kernels into mapped host memory;
+    // `outs` holds the device-side Control words
     DevBuf in, lp, lx, hist, S1, S2, acc, outs, queue, pout;
     HostBuf h_in, h_outs;
     size_t ctl_off = 0;
@@ -332,9 +337,9 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     const size_t o_job = o_des + al(sizeof(DevDesign) * n);
     const size_t in_bytes = o_job + al(sizeof(DesignJob) * n);
     const size_t ctl_off = al(sizeof(DesignOut) * n);
-    const size_t out_bytes = ctl_off + sizeof(Control);
+    const size_t out_bytes = ctl_off + sizeof(HostStatus);
     CPD_TRY(S.h_in.ensure(in_bytes));
-    CPD_TRY(S.h_outs.ensure(out_bytes));
+    CPD_TRY(S.h_outs.ensure(out_bytes, true));
     const void *in_before = S.in.p;
     CPD_TRY(S.in.ensure(in_bytes));
     // the tables already on the device from the previous pass of this slot
@@ -380,7 +385,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     CPD_TRY(S.S1.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
     CPD_TRY(S.S2.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
     CPD_TRY(S.acc.ensure(sizeof(DesignAcc) * n));
-    CPD_TRY(S.outs.ensure(out_bytes));
+    CPD_TRY(S.outs.ensure(sizeof(Control)));
     CPD_TRY(S.queue.ensure(sizeof(QEntry) * S.qcap));
     if (p_out_host) CPD_TRY(S.pout.ensure(hist_bytes));
     S.ctl_off = ctl_off;
@@ -414,8 +419,11 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     a.S1 = S.S1.as<unsigned long long>();
     a.S2 = S.S2.as<unsigned long long>();
     a.acc = S.acc.as<DesignAcc>();
-    a.out = S.outs.as<DesignOut>();
-    a.ctl = reinterpret_cast<Control *>(S.outs.as<char>() + ctl_off);
+    a.out = reinterpret_cast<DesignOut *>(S.h_outs.dev);
+    a.status = reinterpret_cast<HostStatus *>(reinterpret_cast<char *>(S.h_outs.dev) + ctl_off);
+    a.ctl = S.outs.as<Control>();
+    a.clear_acc = fresh ? 1u : 0u;
+    a.acc_cells = accc;
     a.queue = S.queue.as<QEntry>();
     a.qcap = S.qcap;
     a.ray_tile = ctx->ray_tile;
@@ -441,17 +449,13 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     auto record = [&](cudaStream_t st, bool capturing) -> int {
         const unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
         cudaMemcpyAsync(S.in.as<char>() + up_off, S.h_in.as<char>() + up_off, up_bytes, cudaMemcpyHostToDevice, st);
-        if (fresh) {
-            cudaMemsetAsync(S.S1.p, 0, sizeof(unsigned long long) * accc, st);
-            cudaMemsetAsync(S.S2.p, 0, sizeof(unsigned long long) * accc, st);
-            cudaMemsetAsync(S.acc.p, 0, sizeof(DesignAcc) * n, st);
-        }
+        // the per-design accumulators are cleared by the setup kernel (clear_acc), the
+        // results arrive in mapped host memory: one copy and one memset around the kernels
         cudaMemsetAsync(a.ctl, 0, sizeof(Control), st);
         // External: under stream capture these become event-record nodes of the graph
         cudaEventRecordWithFlags(S.ev0, st, evf);
         const int l = launch_pass(a, ctx->num_sms, ctx->warps_per_cta, st, profile ? S.kev : nullptr, true);
         cudaEventRecordWithFlags(S.ev1, st, evf);
-        cudaMemcpyAsync(S.h_outs.p, S.outs.p, out_bytes, cudaMemcpyDeviceToHost, st);
         return l;
     };
     if (use_graph && !profile) {
@@ -496,7 +500,7 @@ int pass_finish(PassSlot &S, PassResult &res)
             cudaEventElapsedTime(&km, S.kev[i], S.kev[i + 1]);
             S.kernel_ms[i] = km;
         }
-    const Control *c = reinterpret_cast<const Control *>(S.h_outs.as<char>() + S.ctl_off);
+    const HostStatus *c = reinterpret_cast<const HostStatus *>(S.h_outs.as<char>() + S.ctl_off);
     res.overflow = c->overflow != 0 || c->queue_count > S.qcap;
     if (res.overflow) S.hist_dirty = true;
     res.outs.assign(S.h_outs.as<DesignOut>(), S.h_outs.as<DesignOut>() + S.n);
