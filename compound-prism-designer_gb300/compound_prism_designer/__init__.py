@@ -25,7 +25,7 @@ __all__ = [
     "RayTraceError", "CudaError", "Glass", "DesignFitness", "Vector2D", "UnitVector2D",
     "UniformWavelengthDistribution", "GaussianBeam", "FiberBeam", "CompoundPrism",
     "position_detector_array", "DetectorArray", "Spectrometer", "Context", "default_context",
-    "fitness_batch", "autotune_batch", "build_designs", "Server", "TRACE_HYBRID", "TRACE_FP32", "TRACE_FP64",
+    "fitness_batch", "fitness_batch_params", "autotune_batch", "build_designs", "Server", "TRACE_HYBRID", "TRACE_FP32", "TRACE_FP64",
     "SAMPLING_ADAPTIVE", "SAMPLING_EXACT",
 ]
 
@@ -571,19 +571,51 @@ def autotune_batch(spectrometers: Sequence[Spectrometer], *, seeds=None, max_n=2
     return rt.value, w.value, ms.value
 
 
-def build_designs(params: np.ndarray, acceptance: float = 0.0):
+def build_designs(params: np.ndarray, acceptance: float = 0.0, *, device: bool = False,
+                  context: Optional[Context] = None):
     """Builds a whole generation of designs from an array of N.PARAMS_DTYPE records (no
     reference counterpart; the reference builds one Spectrometer per call,
     designer.py:203-265). With acceptance in (0, 1] each detector is placed by
-    position_detector_array first. Returns (designs, status): an N.DESIGN_DTYPE array and
-    the per-design status codes (0 = built)."""
+    position_detector_array first. device=True builds them on the GPU
+    (cpd_design_build_device). Returns (designs, status): an N.DESIGN_DTYPE array and the
+    per-design status codes (0 = built)."""
     params = np.ascontiguousarray(params, dtype=N.PARAMS_DTYPE)
     n = params.size
     designs = np.zeros(n, dtype=N.DESIGN_DTYPE)
     status = np.zeros(n, dtype=np.int32)
-    _check(N.lib.cpd_design_build_batch(params.ctypes.data, n, float(acceptance), designs.ctypes.data,
-                                        status.ctypes.data_as(C.POINTER(C.c_int32))), "build_designs")
+    if device:
+        ctx = context or default_context()
+        _check(N.lib.cpd_design_build_device(ctx.handle, params.ctypes.data, n, float(acceptance),
+                                             designs.ctypes.data, status.ctypes.data_as(C.POINTER(C.c_int32))),
+               "build_designs")
+    else:
+        _check(N.lib.cpd_design_build_batch(params.ctypes.data, n, float(acceptance), designs.ctypes.data,
+                                            status.ctypes.data_as(C.POINTER(C.c_int32))), "build_designs")
     return designs, status
+
+
+def _items(n, seeds, max_n, max_eval):
+    items = np.zeros(n, dtype=N.BATCH_ITEM_DTYPE)
+    items["seed"] = np.broadcast_to(np.asarray(seeds, dtype=np.float64), (n,))
+    items["max_n"] = np.broadcast_to(np.asarray(max_n), (n,))
+    items["max_eval"] = np.broadcast_to(np.asarray(max_eval), (n,))
+    return items
+
+
+def fitness_batch_params(params: np.ndarray, *, acceptance: float = 0.0, seeds=0.5, max_n=256, max_eval=16_384,
+                         mode: int = TRACE_HYBRID, context: Optional[Context] = None) -> np.ndarray:
+    """The batched fitness of designs built on the device from N.PARAMS_DTYPE records
+    (cpd_fitness_gpu_batch_params). Returns an N.FITNESS_DTYPE array; status holds a
+    design's build error (a RayTraceError code) where it could not be built."""
+    params = np.ascontiguousarray(params, dtype=N.PARAMS_DTYPE)
+    n = params.size
+    items = _items(n, seeds, max_n, max_eval)
+    outs = np.zeros(n, dtype=N.FITNESS_DTYPE)
+    ctx = context or default_context()
+    _check(N.lib.cpd_fitness_gpu_batch_params(ctx.handle, params.ctypes.data, items.ctypes.data, n,
+                                              float(acceptance), int(mode), outs.ctypes.data),
+           "fitness_batch_params")
+    return outs
 
 
 def _design_array(designs) -> np.ndarray:
@@ -626,6 +658,20 @@ class Server:
         rid = C.c_uint64(0)
         _check(N.lib.cpd_server_submit(self._h, d.ctypes.data, items.ctypes.data, n, int(mode), C.byref(rid)),
                "cpd_server_submit")
+        with self._lock:
+            self._sizes[rid.value] = n
+        return rid.value
+
+    def submit_params(self, params, *, acceptance: float = 0.0, seeds=0.5, max_n=128, max_eval=8192,
+                      mode: int = TRACE_HYBRID) -> int:
+        """Queues N.PARAMS_DTYPE records; the designs are built on the device inside their
+        pass (cpd_server_submit_params). Returns the request id at once."""
+        p = np.ascontiguousarray(params, dtype=N.PARAMS_DTYPE)
+        n = p.size
+        items = _items(n, seeds, max_n, max_eval)
+        rid = C.c_uint64(0)
+        _check(N.lib.cpd_server_submit_params(self._h, p.ctypes.data, items.ctypes.data, n, float(acceptance),
+                                              int(mode), C.byref(rid)), "cpd_server_submit_params")
         with self._lock:
             self._sizes[rid.value] = n
         return rid.value

@@ -150,6 +150,10 @@ SIGNATURES = [
                                  C.POINTER(C.c_uint8)]),
     ("cpd_fitness_gpu_batch", C.c_int, [_ctxp, C.POINTER(Design), C.POINTER(BatchItem), C.c_uint32, C.c_uint32,
                                         C.POINTER(Fitness)]),
+    ("cpd_fitness_gpu_batch_params", C.c_int, [_ctxp, C.c_void_p, C.c_void_p, C.c_uint32, C.c_double, C.c_uint32,
+                                               C.c_void_p]),
+    ("cpd_design_build_device", C.c_int, [_ctxp, C.c_void_p, C.c_uint32, C.c_double, C.c_void_p,
+                                          C.POINTER(C.c_int32)]),
     ("cpd_autotune_batch", C.c_int, [_ctxp, C.POINTER(Design), C.POINTER(BatchItem), C.c_uint32, C.c_uint32, _up,
                                      _up, _dp]),
     ("cpd_set_autotune", C.c_int, [_ctxp, C.c_int]),
@@ -163,6 +167,8 @@ SIGNATURES = [
     ("cpd_server_create", C.c_int, [_ctxp, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(C.c_void_p)]),
     ("cpd_server_submit", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                     C.POINTER(C.c_uint64)]),
+    ("cpd_server_submit_params", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_double, C.c_uint32,
+                                           C.POINTER(C.c_uint64)]),
     ("cpd_server_wait", C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_double, _dp]),
     ("cpd_server_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                    C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),

@@ -154,7 +154,8 @@ def survive(pop: Population, info: np.ndarray, mu: int) -> Population:
 
 
 def serve(server, *, generations: int = 200, sizes=(64, 2048), mean_interarrival_s: float = 0.0, mu: int = 512,
-          max_n: int = 128, max_eval: int = 8192, seed: int = 0, mode: int = 0, catalog_size: int = 64):
+          max_n: int = 128, max_eval: int = 8192, seed: int = 0, mode: int = 0, catalog_size: int = 64,
+          device_build: bool = False):
     """Drives `server` (a compound_prism_designer.Server) with `generations` batches.
 
     Batch sizes are uniform in [sizes[0], sizes[1]]; batches arrive as a Poisson process
@@ -166,6 +167,8 @@ def serve(server, *, generations: int = 200, sizes=(64, 2048), mean_interarrival
     requests in order, records each request's latency (submit to completion, measured
     by the server) and updates the population by (mu + lambda) survival on mutual
     information (a design that did not reach the SEM stop or failed counts as -inf).
+    device_build: submit the offspring's parameter records and let the server build the
+    designs on the device (Server.submit_params) instead of building them here.
 
     Returns a dict: designs, generations, seconds (first submit to last completion),
     designs_per_s, latency_ms list, p50_ms, p99_ms, mean_batch, best_info."""
@@ -217,10 +220,18 @@ def serve(server, *, generations: int = 200, sizes=(64, 2048), mean_interarrival
         with lock:
             parents = state["pop"]
         off = perturb(rng, parents, n, len(catalog))
-        designs, ok = build(off, catalog)
-        keep = np.nonzero(ok)[0]
-        off = off.take(keep)
-        rid = server.submit(designs[keep], seeds=float(rng.uniform()), max_n=max_n, max_eval=max_eval, mode=mode)
+        if device_build:
+            # every offspring goes to the device; the ones that fail to build come back
+            # with their ray-trace status and lose the survival
+            keep = np.arange(len(off))
+            rid = server.submit_params(to_params(off, catalog), acceptance=1.0, seeds=float(rng.uniform()),
+                                       max_n=max_n, max_eval=max_eval, mode=mode)
+        else:
+            designs, ok = build(off, catalog)
+            keep = np.nonzero(ok)[0]
+            off = off.take(keep)
+            rid = server.submit(designs[keep], seeds=float(rng.uniform()), max_n=max_n, max_eval=max_eval,
+                                mode=mode)
         if first_submit is None:
             first_submit = time.perf_counter()
         n_designs += keep.size

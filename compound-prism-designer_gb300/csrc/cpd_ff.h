@@ -131,7 +131,7 @@ CPD_FF_HD float ldexp_f(float v, int e)
 constexpr int kLogTable = 256;
 
 // Splits an f64 into a float-float pair.
-inline void split(double v, float &hi, float &lo)
+CPD_FF_HD void split(double v, float &hi, float &lo)
 {
     hi = (float)v;
     lo = (float)(v - (double)hi);

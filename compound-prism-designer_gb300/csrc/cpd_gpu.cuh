@@ -70,9 +70,10 @@ struct DesignAcc {
 // Per-design result of the fused finalize (cumulative over passes).
 struct DesignOut {
     double info, h_cond, h_det, max_sem;
+    double size, deviation;  // from the design record (built on the host or the device)
     unsigned long long hits, retraced, rows, fast;
     int32_t converged;
-    int32_t pad;
+    int32_t status;          // the design record's status (a device build's error)
 };
 
 // Cells per entropy tile (one warp): a design's tile is max(1, kTileCells / B) rows.
@@ -109,6 +110,10 @@ struct LaunchArgs {
     Guards guards;
     double yguard_rel;
     double *p_out;        // optional W x B for the single design of the launch
+    // designs built on the device (CPD_BUILD_ON_DEVICE): parameter records, written into
+    // the design records by the build kernel before the setup
+    const cpd_spectrometer_params *params;
+    double build_acceptance;
     const float *logtab;  // float-float log2 table (cpd_ff.h), 4 x 256 floats
 };
 
@@ -147,6 +152,10 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
 
 // Warps of the trace kernel resident at once with this block shape.
 uint64_t trace_resident_warps(int num_sms, uint32_t warps_per_cta);
+
+// cpd_design records built on the device from n parameter records (one thread each).
+void launch_build_records(const cpd_spectrometer_params *p, uint32_t n, double acceptance, cpd_design *out,
+                          int32_t *status, cudaStream_t stream);
 
 // One thread per (lam_u[i], z[i]) pair: the twin of propagation_test_kernel.
 void launch_trace_pairs(const DevDesign *d, const double *lam_u, const double *z64, uint32_t n, uint32_t mode,

@@ -7,187 +7,15 @@
 #include <cstring>
 #include <vector>
 
+#include "cpd_build.h"
 #include "cpd_ff.h"
 #include "cpd_host.h"
 #include "cpd_model.h"
 
 namespace cpd {
 
-namespace {
-struct V2 {
-    double x, y;
-};
-V2 angled(double th) { return V2{std::cos(th), std::sin(th)}; }  // Vector::angled_xy (vector.rs:336-343)
-V2 rot180(V2 a) { return V2{-a.x, -a.y}; }
-V2 rot90(V2 a) { return V2{-a.y, a.x}; }
-V2 rot90ccw(V2 a) { return V2{a.y, -a.x}; }
-V2 vfma(V2 a, double b, V2 c) { return V2{std::fma(a.x, b, c.x), std::fma(a.y, b, c.y)}; }
-}  // namespace
-
-// create_joined_trapezoids (geometry.rs:430-489) and CurvedPlane::from_hyperplane
-// (geometry.rs:283-314), into the cpd_design tables.
-int build_prism(const cpd_spectrometer_params &p, cpd_design &d)
-{
-    const int G = p.nglass;
-    if (G < 1 || G > CPD_MAX_GLASS) return CPD_INVALID_ARGUMENT;
-    if (!(p.height > 0.0) || !(std::fabs(p.curvature) > 0.0) || !(std::fabs(p.curvature) <= 1.0))
-        return CPD_INVALID_ARGUMENT;
-    d.nglass = G;
-    d.ar_coated = p.ar_coated ? 1 : 0;
-    std::memcpy(d.glass, p.glass, sizeof(d.glass));
-    d.height = p.height;
-    const double h2 = p.height * 0.5;
-    V2 n0 = rot180(angled(p.angles[0]));
-    V2 pt0{std::fabs(n0.y / n0.x) * h2, h2};
-    d.face_point[0][0] = pt0.x;
-    d.face_point[0][1] = pt0.y;
-    d.face_normal[0][0] = n0.x;
-    d.face_normal[0][1] = n0.y;
-    bool prev_sign = !std::signbit(n0.y);
-    double d1 = pt0.x, mx = pt0.x;
-    V2 last_pt{0, 0}, last_n{0, 0};
-    // array_prepend (utils.rs:5-12): face k (1..G-1) uses lengths[k-1], the exit face lengths[G-1]
-    for (int k = 1; k <= G; k++) {
-        V2 n = rot180(angled(p.angles[k]));
-        bool sign = !std::signbit(n.y);
-        double d2 = std::fabs(n.y / n.x) * h2;
-        double sep = p.lengths[k - 1] + (prev_sign != sign ? d1 + d2 : std::fabs(d1 - d2));
-        prev_sign = sign;
-        d1 = d2;
-        mx += sep;
-        if (k < G) {
-            d.face_point[k][0] = mx;
-            d.face_point[k][1] = h2;
-            d.face_normal[k][0] = n.x;
-            d.face_normal[k][1] = n.y;
-        } else {
-            last_pt = V2{mx, h2};
-            last_n = n;
-        }
-    }
-    const double kc = p.curvature;
-    const double chord = std::fabs(p.height / last_n.x);
-    const double radius = chord * 0.5 / std::fabs(kc);
-    const double apothem = std::sqrt(radius * radius - chord * chord * 0.25);
-    const double sagitta = radius - apothem;
-    V2 c = vfma(last_n, std::copysign(apothem, kc), last_pt);
-    V2 m = vfma(last_n, -std::copysign(sagitta, kc), last_pt);
-    d.exit_center[0] = c.x;
-    d.exit_center[1] = c.y;
-    d.exit_radius = radius;
-    d.exit_bound_center[0] = m.x;
-    d.exit_bound_center[1] = m.y;
-    d.exit_bound_r2 = sagitta * sagitta + chord * chord * 0.25;
-    for (int k = 0; k < G; k++)
-        if (!std::isfinite(d.face_point[k][0]) || !std::isfinite(d.face_normal[k][0])) return CPD_INVALID_ARGUMENT;
-    if (!std::isfinite(radius) || !std::isfinite(apothem)) return CPD_INVALID_ARGUMENT;
-    return CPD_OK;
-}
-
-void fill_source(const cpd_spectrometer_params &p, cpd_design &d)
-{
-    d.wavelength_bounds[0] = p.wavelength_bounds[0];
-    d.wavelength_bounds[1] = p.wavelength_bounds[1];
-    d.beam_width = p.beam_width;
-    d.beam_y_mean = p.beam_y_mean;
-}
-
-// f64 tables -> device record (exact part copied, FP32 fast-path constants derived in f64).
-void design_to_dev(const cpd_design &d, DevDesign &D)
-{
-    std::memset(&D, 0, sizeof(D));
-    D.G = d.nglass;
-    D.B = d.bin_count;
-    D.ar = d.ar_coated;
-    std::memcpy(D.glass, d.glass, sizeof(D.glass));
-    for (int k = 0; k < CPD_MAX_GLASS; k++) {
-        D.ppx[k] = d.face_point[k][0];
-        D.ppy[k] = d.face_point[k][1];
-        D.pnx[k] = d.face_normal[k][0];
-        D.pny[k] = d.face_normal[k][1];
-    }
-    D.height = d.height;
-    D.ccx = d.exit_center[0];
-    D.ccy = d.exit_center[1];
-    D.crad = d.exit_radius;
-    D.cbx = d.exit_bound_center[0];
-    D.cby = d.exit_bound_center[1];
-    D.cbr2 = d.exit_bound_r2;
-    D.bin_size = d.bin_size;
-    D.slope = d.linear_slope;
-    D.intercept = d.linear_intercept;
-    D.min_ci = d.min_ci;
-    D.L = d.det_length;
-    D.dnx = d.det_normal[0];
-    D.dny = d.det_normal[1];
-    D.dpx = d.det_position[0];
-    D.dpy = d.det_position[1];
-    D.dux = d.det_direction[0];
-    D.duy = d.det_direction[1];
-    D.wmin = d.wavelength_bounds[0];
-    D.wmax = d.wavelength_bounds[1];
-    D.bw = d.beam_width;
-    D.bym = d.beam_y_mean;
-    FastConst &f = D.fc;
-    f.inv_rc = (float)(1.0 / D.crad);
-    f.rho = (float)std::sqrt(D.cbr2);
-    f.rho2 = (float)D.cbr2;
-    f.dnfx = (float)D.dnx;
-    f.dnfy = (float)D.dny;
-    f.dufx = (float)D.dux;
-    f.dufy = (float)D.duy;
-    f.min_ci = (float)D.min_ci;
-    f.L = (float)D.L;
-    f.c0 = (float)D.intercept;
-    f.slope = (float)D.slope;
-    f.inv_slope = (float)(1.0 / D.slope);
-    f.bin_size = (float)D.bin_size;
-    f.bw = (float)D.bw;
-    f.hL = (float)(0.5 * D.L);
-    f.ar = D.ar;
-    f.B = D.B;
-    DFConst &c = D.dc;
-    auto sp = [](double v) {
-        ff::F2 r;
-        ff::split(v, r.hi, r.lo);
-        return r;
-    };
-    for (int k = 0; k < CPD_MAX_GLASS; k++) {
-        for (int i = 0; i < 6; i++) c.glass[k][i] = sp(D.glass[k][i]);
-        c.ppx[k] = sp(D.ppx[k]);
-        c.ppy[k] = sp(D.ppy[k]);
-        c.pnx[k] = sp(D.pnx[k]);
-        c.pny[k] = sp(D.pny[k]);
-    }
-    c.height = sp(D.height);
-    c.ccx = sp(D.ccx);
-    c.ccy = sp(D.ccy);
-    c.rc2 = sp(D.crad * D.crad);
-    c.irc = sp(1.0 / D.crad);
-    c.cbx = sp(D.cbx);
-    c.cby = sp(D.cby);
-    c.cbr2 = sp(D.cbr2);
-    c.vx = sp(D.cbx - D.ccx);
-    c.vy = sp(D.cby - D.ccy);
-    c.bin_size = sp(D.bin_size);
-    c.slope = sp(D.slope);
-    c.islope = sp(1.0 / D.slope);
-    c.intercept = sp(D.intercept);
-    c.min_ci = sp(D.min_ci);
-    c.L = sp(D.L);
-    c.dnx = sp(D.dnx);
-    c.dny = sp(D.dny);
-    c.dpx = sp(D.dpx);
-    c.dpy = sp(D.dpy);
-    c.dux = sp(D.dux);
-    c.duy = sp(D.duy);
-    c.qx = sp(D.dpx - D.cbx);
-    c.qy = sp(D.dpy - D.cby);
-    c.wmin = sp(D.wmin);
-    c.wspan = sp(D.wmax - D.wmin);
-    c.bw = sp(D.bw);
-    c.bym = sp(D.bym);
-}
+// f64 tables -> device record (cpd_build.h).
+void design_to_dev(const cpd_design &d, DevDesign &D) { build::to_dev(d, D); }
 
 // Shaw's inverse normal CDF (erf.rs:27-73), host-side: the ray tables are built here
 // so that the device never evaluates a logarithm on the exact path.
@@ -289,79 +117,15 @@ int cpd_position_detector_array(const cpd_spectrometer_params *p, double accepta
                                 int32_t *flipped_out)
 {
     if (!p || !position_out || !flipped_out) return CPD_INVALID_ARGUMENT;
-    if (!(acceptance > 0.0) || !(acceptance <= 1.0)) return CPD_INVALID_ARGUMENT;
-    cpd_design d;
-    std::memset(&d, 0, sizeof(d));
-    int e = build_prism(*p, d);
-    if (e) return e;
-    fill_source(*p, d);
-    DevDesign D;
-    design_to_dev(d, D);
-    // detector_array_positioning (spectrometer.rs:322-364)
-    const double uh = std::max(1.0 - acceptance, 0.0) * 0.5;
-    const double wmin = x::wavelength(D, uh);
-    const double wmax = x::wavelength(D, 1.0 - uh);
-    x::Ray lo{0.0, D.bym, 1.0, 0.0, 1.0, 1.0}, up = lo;
-    e = x::prism(D, wmin, lo);
-    if (e) return e;
-    e = x::prism(D, wmax, up);
-    if (e) return e;
-    if ((lo.ts + lo.tp) * 0.5 <= 1e-3 || (up.ts + up.tp) * 0.5 <= 1e-3) return CPD_RAYTRACE_ANGULAR_RESPONSE_TOO_WEAK;
-    // fit_ray_difference_surface (geometry.rs:495-542)
-    V2 spec_dir = rot90(angled(p->det_angle));
-    V2 spec{spec_dir.x * p->det_length, spec_dir.y * p->det_length};
-    const double a = up.dx, b = -lo.dx, c = up.dy, dd = -lo.dy;
-    const double det = a * dd - b * c;
-    if (det == 0.0) return CPD_RAYTRACE_NO_SURFACE_INTERSECTION;
-    const double i10 = -c / det, i11 = a / det;
-    double tx = (spec.x - up.ox) + lo.ox, ty = (spec.y - up.oy) + lo.oy;
-    double d2 = i10 * tx + i11 * ty;
-    int32_t flipped = 0;
-    if (!(d2 > 0.0)) {
-        tx = (-spec.x - up.ox) + lo.ox;
-        ty = (-spec.y - up.oy) + lo.oy;
-        d2 = i10 * tx + i11 * ty;
-        if (d2 < 0.0) return CPD_RAYTRACE_NO_SURFACE_INTERSECTION;
-        flipped = 1;
-    }
-    position_out[0] = std::fma(lo.dx, d2, lo.ox);
-    position_out[1] = std::fma(lo.dy, d2, lo.oy);
-    *flipped_out = flipped;
-    return CPD_OK;
+    return build::position(*p, acceptance, position_out, *flipped_out);
 }
 
 int cpd_design_build(const cpd_spectrometer_params *p, cpd_design *out)
 {
     if (!p || !out) return CPD_INVALID_ARGUMENT;
-    if (p->bin_count == 0 || p->bin_count > CPD_MAX_BINS) return CPD_INVALID_ARGUMENT;
-    if (!(p->linear_slope > 0.0) || !(p->bin_size > 0.0) || !(p->det_length > 0.0)) return CPD_INVALID_ARGUMENT;
-    if (!(p->wavelength_bounds[1] >= p->wavelength_bounds[0])) return CPD_INVALID_ARGUMENT;
     cpd_design d;
-    std::memset(&d, 0, sizeof(d));
-    int e = build_prism(*p, d);
+    const int e = build::design(*p, d);
     if (e) return e;
-    fill_source(*p, d);
-    // LinearDetectorArray::new (spectrometer.rs:183-219), min_ci = cos (src/pylib.rs:886)
-    d.bin_count = p->bin_count;
-    d.bin_size = p->bin_size;
-    d.linear_slope = p->linear_slope;
-    d.linear_intercept = p->linear_intercept;
-    d.min_ci = std::cos(p->max_incident_angle);
-    d.det_length = p->det_length;
-    V2 n = rot180(angled(p->det_angle));
-    V2 u = p->det_flipped ? rot90(n) : rot90ccw(n);
-    d.det_normal[0] = n.x;
-    d.det_normal[1] = n.y;
-    d.det_direction[0] = u.x;
-    d.det_direction[1] = u.y;
-    d.det_position[0] = p->det_position[0];
-    d.det_position[1] = p->det_position[1];
-    // size_and_deviation + mid_pt (spectrometer.rs:429-437, 305-308)
-    V2 mid = vfma(u, p->det_length * 0.5, V2{d.det_position[0], d.det_position[1]});
-    const double dx = mid.x, dy = mid.y - p->beam_y_mean;
-    const double size = std::sqrt(dx * dx + dy * dy);
-    d.size = size;
-    d.deviation = std::fabs(dy / size);
     *out = d;
     return CPD_OK;
 }
@@ -371,14 +135,7 @@ int cpd_design_build_batch(const cpd_spectrometer_params *p, uint32_t n, double 
 {
     if ((!p || !out || !status) && n) return CPD_INVALID_ARGUMENT;
     if (acceptance != 0.0 && !(acceptance > 0.0 && acceptance <= 1.0)) return CPD_INVALID_ARGUMENT;
-    for (uint32_t i = 0; i < n; i++) {
-        cpd_spectrometer_params q = p[i];
-        int e = CPD_OK;
-        if (acceptance > 0.0) e = cpd_position_detector_array(&q, acceptance, q.det_position, &q.det_flipped);
-        if (!e) e = cpd_design_build(&q, &out[i]);
-        if (e) std::memset(&out[i], 0, sizeof(cpd_design));
-        status[i] = e;
-    }
+    for (uint32_t i = 0; i < n; i++) status[i] = build::design_positioned(p[i], acceptance, out[i]);
     return CPD_OK;
 }
 

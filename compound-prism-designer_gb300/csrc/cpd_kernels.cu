@@ -16,6 +16,7 @@
 //   finalize one warp per design: H(D), MI, SEM convergence.
 #include <cuda_runtime.h>
 
+#include "cpd_build.h"
 #include "cpd_df.h"
 #include "cpd_gpu.cuh"
 
@@ -49,6 +50,34 @@ __device__ __forceinline__ void push_ray(const LaunchArgs &a, uint32_t d, uint32
     unsigned long long pos = atomicAdd(&a.ctl->queue_count, 1ull);
     if (pos < a.qcap) a.queue[pos] = QEntry{d, k, j, 0u};
     else atomicOr(&a.ctl->overflow, 1u);
+}
+
+// Designs built on the device from parameter records (CPD_BUILD_ON_DEVICE): one thread
+// per design, the f64 construction of cpd_build.h (positioning first when the pass's
+// acceptance is positive), written straight into the pass's design records. A design whose
+// construction fails keeps its status in the record; the setup then loses all its rays.
+__global__ void __launch_bounds__(32) build_kernel(const LaunchArgs a)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.njobs) return;
+    cpd_design d;
+    const int e = build::design_positioned(a.params[i], a.build_acceptance, d);
+    DevDesign D;
+    build::to_dev(d, D);
+    D.status = e;
+    if (e) D.B = a.jobs[i].B;
+    const_cast<DevDesign *>(a.designs)[i] = D;
+}
+
+// cpd_design records from parameter records, for the host (cpd_design_build_device).
+__global__ void __launch_bounds__(32) build_records_kernel(const cpd_spectrometer_params *p, uint32_t n,
+                                                           double acceptance, cpd_design *out, int32_t *status)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    cpd_design d;
+    status[i] = build::design_positioned(p[i], acceptance, d);
+    out[i] = d;
 }
 
 // Sorted-ray tables up to this many rays are staged in shared memory by the setup.
@@ -109,6 +138,16 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     const DevDesign &D = staged ? sD : a.designs[d];
     const float *z32 = staged && stage_z ? sz : a.z32 + 2 * J.ray_off;
     LamParams P;
+    if (D.status) {
+        // a design whose device build failed: every ray of it is lost
+        uint32_t *w = reinterpret_cast<uint32_t *>(&P);
+        for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
+        LamDF *E = a.lx + row;
+        memset(E, 0, sizeof(LamDF));
+        E->lost = 1u;
+        a.lp[row] = P;
+        return;
+    }
     lambda_setup_df(D, a.lam_u[J.lam_off + k], z32, J.Rz, P, a.yguard_rel, a.lx + row, a.adaptive != 0);
     if (a.adaptive) {
         // the adaptive rounds trace every ray of the band themselves
@@ -125,7 +164,10 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     a.lp[row] = P;
 }
 
-__global__ void __launch_bounds__(256, 3) trace_kernel(const LaunchArgs a)
+#ifndef CPD_TRACE_MIN_BLOCKS
+#define CPD_TRACE_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(256, CPD_TRACE_MIN_BLOCKS) trace_kernel(const LaunchArgs a)
 {
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();  // setup's LamParams and queue
@@ -521,12 +563,15 @@ __device__ void finalize_warp(const LaunchArgs &a, uint32_t d, const DesignJob &
         o.info = (double)info.hi + (double)info.lo;
         const float fn = (float)rows;
         o.max_sem = rows > 1ull ? (double)sqrtf(m2max / (fn - 1.f) / fn) : (double)INFINITY;
+        const DevDesign &D = a.designs[d];
+        o.size = D.size;
+        o.deviation = D.deviation;
         o.hits = hits;
         o.retraced = retraced;
         o.rows = rows;
         o.fast = fast;
         o.converged = conv;
-        o.pad = 0;
+        o.status = D.status;
         a.out[d] = o;
         a.acc[d].rows = rows;
     }
@@ -885,6 +930,10 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     pdl = pdl && ev == nullptr;
     int launches = 0;
     if (ev) cudaEventRecord(ev[0], stream);
+    if (a.params) {
+        launch_k(build_kernel, (a.njobs + 31u) / 32u, 32, 0, stream, false, a);
+        launches++;
+    }
     if (a.total_rows) {
         // one warp per block: f64-pipe bound, so spreading rows over every SM matters
         const uint32_t blocks = (uint32_t)((a.total_rows + 31) / 32);
@@ -960,6 +1009,13 @@ uint64_t trace_resident_warps(int num_sms, uint32_t warps_per_cta)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel, (int)warps_per_cta * 32, 0);
     if (per_sm < 1) per_sm = 1;
     return (uint64_t)num_sms * (uint64_t)per_sm * warps_per_cta;
+}
+
+void launch_build_records(const cpd_spectrometer_params *p, uint32_t n, double acceptance, cpd_design *out,
+                          int32_t *status, cudaStream_t stream)
+{
+    if (!n) return;
+    build_records_kernel<<<(n + 31) / 32, 32, 0, stream>>>(p, n, acceptance, out, status);
 }
 
 void launch_trace_pairs(const DevDesign *d, const double *lam_u, const double *z64, uint32_t n, uint32_t mode,

@@ -105,7 +105,7 @@ struct alignas(16) DevDesign {
     int32_t G;
     uint32_t B;
     int32_t ar;
-    int32_t pad0;
+    int32_t status;  // 0, or the error of a design built on the device (its rays are all lost)
     double glass[CPD_MAX_GLASS][6];
     double ppx[CPD_MAX_GLASS], ppy[CPD_MAX_GLASS], pnx[CPD_MAX_GLASS], pny[CPD_MAX_GLASS];
     double height;
@@ -113,6 +113,7 @@ struct alignas(16) DevDesign {
     double bin_size, slope, intercept, min_ci, L;
     double dnx, dny, dpx, dpy, dux, duy;
     double wmin, wmax, bw, bym;
+    double size, deviation;  // size_and_deviation (spectrometer.rs:429-437)
     FastConst fc;
     DFConst dc;
 };

@@ -168,6 +168,7 @@ struct cpd_context {
     std::mutex cache_mu;  // ray-table cache
     PassSlot main;
     DevBuf pair_design, pair_lam, pair_z, pair_bins, pair_ts, pair_flags, peak, logtab;
+    DevBuf bld_params, bld_out, bld_status;  // cpd_design_build_device
     uint32_t ray_tile = 32;
     uint32_t warps_per_cta = 8;
     bool profiling = false;
@@ -241,6 +242,10 @@ struct PassDesign {
     const RayTable *rays;
     std::shared_ptr<const void> lam_keep = nullptr, rays_keep = nullptr;
     uint32_t lam_len = 0;      // length of the lam_u table (0: W)
+    // set instead of dev: the design is built on the device from this record (detector
+    // positioned first when acceptance > 0; the same acceptance for every design of a pass)
+    const cpd_spectrometer_params *params = nullptr;
+    double acceptance = 0.0;
 };
 
 struct PassResult {
@@ -267,6 +272,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     const uint32_t n = (uint32_t)ds.size();
     const bool adaptive = (mode & CPD_SAMPLING_ADAPTIVE) != 0u;
     const bool all_exact = adaptive && (mode & CPD_SAMPLING_EXACT) != 0u;
+    const bool on_device = n > 0 && ds[0].params != nullptr;  // every design of the pass, or none
     mode &= ~kSamplingBits;
     std::vector<DesignJob> jobs(n);
     std::vector<uint8_t> owns_rays(n, 1);  // designs that share a ray table share its copy
@@ -285,7 +291,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         J.W = p.W;
         J.R = p.R;
         J.Rz = (uint32_t)p.rays->z64.size();
-        J.B = p.dev->B;
+        J.B = on_device ? p.params->bin_count : p.dev->B;
         J.row_off = rows;
         J.hist_off = hist;
         const uint32_t lam_len = std::max(p.lam_len, p.W);
@@ -335,7 +341,8 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     const size_t o_rank = o_z32 + al(2 * sizeof(float) * ray);
     const size_t o_des = o_rank + al(sizeof(uint32_t) * rnk);
     const size_t o_job = o_des + al(sizeof(DevDesign) * n);
-    const size_t in_bytes = o_job + al(sizeof(DesignJob) * n);
+    const size_t o_par = o_job + al(sizeof(DesignJob) * n);  // parameter records (device builds)
+    const size_t in_bytes = o_par + (on_device ? al(sizeof(cpd_spectrometer_params) * n) : 0);
     const size_t ctl_off = al(sizeof(DesignOut) * n);
     const size_t out_bytes = ctl_off + sizeof(HostStatus);
     CPD_TRY(S.h_in.ensure(in_bytes));
@@ -346,10 +353,12 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     tables_key.push_back(adaptive ? &kSamplingBits : nullptr);  // the rank section
     tables_key.push_back(S.in.p);
     const bool resident = cacheable && S.in.p == in_before && tables_key == S.tables_key;
-    const size_t up_off = resident ? o_des : 0, up_bytes = in_bytes - up_off;
+    // a device build writes the design records itself: they are not uploaded
+    const size_t up_off = resident ? (on_device ? o_job : o_des) : 0, up_bytes = in_bytes - up_off;
     char *hin = S.h_in.as<char>();
     for (uint32_t i = 0; i < n; i++) {
-        reinterpret_cast<DevDesign *>(hin + o_des)[i] = *ds[i].dev;
+        if (on_device) reinterpret_cast<cpd_spectrometer_params *>(hin + o_par)[i] = *ds[i].params;
+        else reinterpret_cast<DevDesign *>(hin + o_des)[i] = *ds[i].dev;
         reinterpret_cast<DesignJob *>(hin + o_job)[i] = jobs[i];
         if (resident) continue;
         if (owns_lam[i])
@@ -437,6 +446,10 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     }
     a.p_out = p_out_host ? S.pout.as<double>() : nullptr;
     a.logtab = ctx->logtab.as<float>();
+    if (on_device) {
+        a.params = reinterpret_cast<const cpd_spectrometer_params *>(din + o_par);
+        a.build_acceptance = ds[0].acceptance;
+    }
 
     // The device work of a pass, captured once per signature and replayed.
     // The whole pass -- input upload, accumulator clears, kernels, read-back, and the two
@@ -509,12 +522,11 @@ int pass_finish(PassSlot &S, PassResult &res)
 
 // rays: the fixed-N estimator's ray count; under adaptive sampling the rays actually
 // consumed (counted on the device) replace it.
-void fill_fitness(const cpd_design &d, const DesignOut &o, uint64_t rays, cpd_fitness &f, bool need_conv,
-                  bool adaptive = false)
+void fill_fitness(const DesignOut &o, uint64_t rays, cpd_fitness &f, bool need_conv, bool adaptive = false)
 {
     std::memset(&f, 0, sizeof(f));
-    f.size = d.size;
-    f.deviation = d.deviation;
+    f.size = o.size;  // from the design record (built on the host or on the device)
+    f.deviation = o.deviation;
     f.info = o.info;
     f.h_cond = o.h_cond;
     f.h_det = o.h_det;
@@ -524,7 +536,7 @@ void fill_fitness(const cpd_design &d, const DesignOut &o, uint64_t rays, cpd_fi
     f.retraced = o.retraced;
     f.fast_rays = adaptive ? o.fast - std::min(o.fast, o.retraced) : o.fast;
     f.wavelengths = (uint32_t)o.rows;
-    f.status = (need_conv && !o.converged) ? CPD_NOT_CONVERGED : CPD_OK;
+    f.status = o.status ? o.status : (need_conv && !o.converged) ? CPD_NOT_CONVERGED : CPD_OK;
 }
 
 bool valid_design(const cpd_design *d)
@@ -542,6 +554,13 @@ bool valid_mode(uint32_t m)
 }
 
 bool is_adaptive(uint32_t m) { return (m & CPD_SAMPLING_ADAPTIVE) != 0u; }
+
+// What the pass needs of a parameter record before the device builds it (the build
+// checks the rest and reports failures per design).
+bool valid_params(const cpd_spectrometer_params &p)
+{
+    return p.nglass >= 1 && p.nglass <= CPD_MAX_GLASS && p.bin_count >= 1 && p.bin_count <= CPD_MAX_BINS;
+}
 
 bool valid_item(const cpd_batch_item &it)
 {
@@ -575,7 +594,7 @@ std::array<uint64_t, 5> tune_class(const std::vector<PassDesign> &ds, uint32_t m
     for (const PassDesign &p : ds) {
         rows += p.W;
         rays += (uint64_t)p.W * p.R;
-        maxB = std::max<uint64_t>(maxB, p.dev->B);
+        maxB = std::max<uint64_t>(maxB, p.params ? p.params->bin_count : p.dev->B);
     }
     auto lg = [](uint64_t v) {
         uint64_t b = 0;
@@ -667,6 +686,8 @@ void batch_inputs(cpd_context *ctx, const cpd_design *designs, const cpd_batch_i
 namespace {
 struct SrvRequest {
     std::vector<cpd_design> designs;
+    std::vector<cpd_spectrometer_params> params;  // instead of designs: built on the device
+    double acceptance = 0.0;
     std::vector<cpd_batch_item> items;
     std::vector<cpd_fitness> outs;
     uint32_t remaining = 0;
@@ -726,9 +747,8 @@ void srv_complete(cpd_server *sv, size_t i)
         if (rit == sv->reqs.end()) continue;
         SrvRequest &r = rit->second;
         if (e) r.status = e;
-        else fill_fitness(r.designs[work[k].idx], res.outs[k],
-                          (uint64_t)r.items[work[k].idx].max_n * r.items[work[k].idx].max_eval, r.outs[work[k].idx],
-                          true, is_adaptive(r.mode));
+        else fill_fitness(res.outs[k], (uint64_t)r.items[work[k].idx].max_n * r.items[work[k].idx].max_eval,
+                          r.outs[work[k].idx], true, is_adaptive(r.mode));
         if (--r.remaining == 0) {
             r.done = true;
             r.t_done = std::chrono::steady_clock::now();
@@ -772,10 +792,16 @@ void srv_loop(cpd_server *sv)
                 if (sv->busy[i] || sv->pending.empty()) continue;
                 bool others = false;
                 for (size_t j = 0; j < sv->slots.size(); j++) others |= sv->busy[j];
-                mode = sv->reqs[sv->pending.front().req].mode;
+                const SrvRequest &r0 = sv->reqs[sv->pending.front().req];
+                mode = r0.mode;
+                const bool dev0 = !r0.params.empty();
+                const double acc0 = r0.acceptance;
                 while (!sv->pending.empty() && take.size() < sv->max_designs_per_pass) {
                     const SrvWork &w = sv->pending.front();
-                    if (sv->reqs[w.req].mode != mode) break;
+                    // a pass holds designs of one trace mode and one kind (built on the host,
+                    // or on the device with one acceptance)
+                    const SrvRequest &rw = sv->reqs[w.req];
+                    if (rw.mode != mode || rw.params.empty() != !dev0 || rw.acceptance != acc0) break;
                     if (sv->in_use + w.bytes > sv->budget && (others || !take.empty())) break;
                     sv->in_use += w.bytes;
                     take.push_back(w);
@@ -800,11 +826,16 @@ void srv_loop(cpd_server *sv)
                     r = &sv->reqs[take[k].req];
                 }
                 const cpd_batch_item &it = r->items[take[k].idx];
-                design_to_dev(r->designs[take[k].idx], devs[k]);
+                if (r->params.empty()) design_to_dev(r->designs[take[k].idx], devs[k]);
                 lams[k] = lam_points_cached(sv->ctx, it.seed, it.max_n);
                 rays[k] = ray_table_cached(sv->ctx, it.seed, it.max_eval);
                 ds[k] = PassDesign{&devs[k], it.max_n, it.max_eval, lams[k]->data(), rays[k].get(), lams[k], rays[k],
                                    (uint32_t)lams[k]->size()};
+                if (!r->params.empty()) {
+                    ds[k].dev = nullptr;
+                    ds[k].params = &r->params[take[k].idx];
+                    ds[k].acceptance = r->acceptance;
+                }
             }
             int e = pass_issue(sv->ctx, *sv->slots[i], ds, mode, true, nullptr, false, false);
             if (e) {
@@ -876,7 +907,8 @@ void cpd_context_destroy(cpd_context *ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     ctx->main.destroy();
-    for (DevBuf *b : {&ctx->pair_design, &ctx->pair_lam, &ctx->pair_z, &ctx->pair_bins, &ctx->pair_ts,
+    for (DevBuf *b : {&ctx->bld_params, &ctx->bld_out, &ctx->bld_status, &ctx->pair_design, &ctx->pair_lam,
+                      &ctx->pair_z, &ctx->pair_bins, &ctx->pair_ts,
                       &ctx->pair_flags, &ctx->peak, &ctx->logtab})
         b->release();
     delete ctx;
@@ -953,7 +985,7 @@ int cpd_fitness_gpu_points(cpd_context *ctx, const cpd_design *d, const double *
     PassResult res;
     int e = run_pass_checked(ctx, ctx->main, ds, trace_mode, true, p_out, res, ctx->use_graphs);
     if (e) return e;
-    fill_fitness(*d, res.outs[0], (uint64_t)W * R, *out, false, is_adaptive(trace_mode));
+    fill_fitness(res.outs[0], (uint64_t)W * R, *out, false, is_adaptive(trace_mode));
     return CPD_OK;
 }
 
@@ -1000,7 +1032,7 @@ int cpd_fitness_gpu_ex(cpd_context *ctx, const cpd_design *d, const double *seed
         rays += (uint64_t)max_n * max_eval;
         if (res.outs[0].converged) break;
     }
-    fill_fitness(*d, res.outs[0], rays, *out, true, is_adaptive(mode));
+    fill_fitness(res.outs[0], rays, *out, true, is_adaptive(mode));
     return out->status;
 }
 
@@ -1030,8 +1062,68 @@ int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd
     int e = run_pass_checked(ctx, ctx->main, ds, trace_mode, true, nullptr, res, ctx->use_graphs);
     if (e) return e;
     for (uint32_t i = 0; i < n; i++)
-        fill_fitness(designs[i], res.outs[i], (uint64_t)items[i].max_n * items[i].max_eval, outs[i], true,
+        fill_fitness(res.outs[i], (uint64_t)items[i].max_n * items[i].max_eval, outs[i], true,
                      is_adaptive(trace_mode));
+    return CPD_OK;
+}
+
+int cpd_fitness_gpu_batch_params(cpd_context *ctx, const cpd_spectrometer_params *params,
+                                 const cpd_batch_item *items, uint32_t n, double acceptance, uint32_t trace_mode,
+                                 cpd_fitness *outs)
+{
+    if (!ctx || !params || !items || !outs || n == 0 || !valid_mode(trace_mode)) return CPD_INVALID_ARGUMENT;
+    if (acceptance != 0.0 && !(acceptance > 0.0 && acceptance <= 1.0)) return CPD_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < n; i++)
+        if (!valid_params(params[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
+    CPD_SYNC_ENTRY(ctx);
+    std::vector<LamPtr> lams(n);
+    std::vector<RayTablePtr> rts(n);
+    std::vector<PassDesign> ds(n);
+    for (uint32_t i = 0; i < n; i++) {
+        lams[i] = lam_points_cached(ctx, items[i].seed, items[i].max_n);
+        rts[i] = ray_table_cached(ctx, items[i].seed, items[i].max_eval);
+        ds[i] = PassDesign{nullptr, items[i].max_n, items[i].max_eval, lams[i]->data(), rts[i].get(), lams[i], rts[i],
+                           (uint32_t)lams[i]->size(), &params[i], acceptance};
+    }
+    if (ctx->autotune && !ctx->profiling && !is_adaptive(trace_mode)) {
+        auto it = ctx->tune_cache.find(tune_class(ds, trace_mode));
+        if (it != ctx->tune_cache.end()) {
+            ctx->ray_tile = it->second.first;
+            ctx->warps_per_cta = it->second.second;
+        } else {
+            const int te = tune_pass(ctx, ds, trace_mode, nullptr);
+            if (te) return te;
+        }
+    }
+    PassResult res;
+    int e = run_pass_checked(ctx, ctx->main, ds, trace_mode, true, nullptr, res, ctx->use_graphs);
+    if (e) return e;
+    for (uint32_t i = 0; i < n; i++)
+        fill_fitness(res.outs[i], (uint64_t)items[i].max_n * items[i].max_eval, outs[i], true,
+                     is_adaptive(trace_mode));
+    return CPD_OK;
+}
+
+int cpd_design_build_device(cpd_context *ctx, const cpd_spectrometer_params *params, uint32_t n, double acceptance,
+                            cpd_design *out, int32_t *status)
+{
+    if (!ctx || ((!params || !out || !status) && n)) return CPD_INVALID_ARGUMENT;
+    if (acceptance != 0.0 && !(acceptance > 0.0 && acceptance <= 1.0)) return CPD_INVALID_ARGUMENT;
+    if (n == 0) return CPD_OK;
+    CPD_SYNC_ENTRY(ctx);
+    cudaStream_t s = ctx->main.stream;
+    CPD_TRY(ctx->bld_params.ensure(sizeof(cpd_spectrometer_params) * n));
+    CPD_TRY(ctx->bld_out.ensure(sizeof(cpd_design) * n));
+    CPD_TRY(ctx->bld_status.ensure(sizeof(int32_t) * n));
+    CPD_TRY(cudaMemcpyAsync(ctx->bld_params.p, params, sizeof(cpd_spectrometer_params) * n, cudaMemcpyHostToDevice, s));
+    launch_build_records(ctx->bld_params.as<cpd_spectrometer_params>(), n, acceptance, ctx->bld_out.as<cpd_design>(),
+                         ctx->bld_status.as<int32_t>(), s);
+    CPD_TRY(cudaGetLastError());
+    CPD_TRY(cudaMemcpyAsync(out, ctx->bld_out.p, sizeof(cpd_design) * n, cudaMemcpyDeviceToHost, s));
+    CPD_TRY(cudaMemcpyAsync(status, ctx->bld_status.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+    CPD_TRY(cudaStreamSynchronize(s));
+    ctx->main.h2d += sizeof(cpd_spectrometer_params) * n;
+    ctx->main.d2h += (sizeof(cpd_design) + sizeof(int32_t)) * n;
     return CPD_OK;
 }
 
@@ -1191,6 +1283,32 @@ int cpd_server_submit(cpd_server *sv, const cpd_design *designs, const cpd_batch
     for (uint32_t i = 0; i < n; i++)
         sv->pending.push_back(
             SrvWork{id, i, design_bytes(items[i].max_n, items[i].max_eval, designs[i].bin_count)});
+    *request_id = id;
+    sv->cv_work.notify_one();
+    return CPD_OK;
+}
+
+int cpd_server_submit_params(cpd_server *sv, const cpd_spectrometer_params *params, const cpd_batch_item *items,
+                             uint32_t n, double acceptance, uint32_t trace_mode, uint64_t *request_id)
+{
+    if (!sv || !params || !items || !request_id || n == 0 || !valid_mode(trace_mode)) return CPD_INVALID_ARGUMENT;
+    if (acceptance != 0.0 && !(acceptance > 0.0 && acceptance <= 1.0)) return CPD_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < n; i++)
+        if (!valid_params(params[i]) || !valid_item(items[i])) return CPD_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->stop) return CPD_INVALID_ARGUMENT;
+    const uint64_t id = sv->next_id++;
+    SrvRequest &r = sv->reqs[id];
+    r.params.assign(params, params + n);
+    r.acceptance = acceptance;
+    r.items.assign(items, items + n);
+    r.outs.resize(n);
+    r.remaining = n;
+    r.mode = trace_mode;
+    r.t_submit = std::chrono::steady_clock::now();
+    for (uint32_t i = 0; i < n; i++)
+        sv->pending.push_back(
+            SrvWork{id, i, design_bytes(items[i].max_n, items[i].max_eval, params[i].bin_count)});
     *request_id = id;
     sv->cv_work.notify_one();
     return CPD_OK;

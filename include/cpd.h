@@ -256,6 +256,25 @@ typedef struct cpd_batch_item {
 int cpd_fitness_gpu_batch(cpd_context *ctx, const cpd_design *designs, const cpd_batch_item *items,
                           uint32_t n, uint32_t trace_mode, cpd_fitness *outs);
 
+/* Design construction on the device (no reference counterpart; the reference builds each
+ * Spectrometer on the host, src/pylib.rs:690-1170). The batched form with parameter records
+ * instead of built designs: the pass's first kernel builds each design on the GPU (the
+ * f64 construction of cpd_design_build, the detector positioned first by
+ * cpd_position_detector_array when acceptance is in (0, 1]; acceptance 0 takes
+ * det_position/det_flipped as given) and the fitness follows in the same launch sequence.
+ * The construction's sin/cos are CUDA's f64 functions, so a design may differ from the
+ * host-built one in the last bit of its tables. outs[i].status is the build error of a
+ * design that could not be built (a CPD_RAYTRACE_* or CPD_INVALID_ARGUMENT value; its
+ * other fields are zero), else CPD_OK or CPD_NOT_CONVERGED. */
+int cpd_fitness_gpu_batch_params(cpd_context *ctx, const cpd_spectrometer_params *params,
+                                 const cpd_batch_item *items, uint32_t n, double acceptance,
+                                 uint32_t trace_mode, cpd_fitness *outs);
+
+/* cpd_design_build_batch on the GPU: the same records and status codes (up to the last-bit
+ * differences of CUDA's sin/cos), one thread per design. */
+int cpd_design_build_device(cpd_context *ctx, const cpd_spectrometer_params *params, uint32_t n,
+                            double acceptance, cpd_design *out, int32_t *status);
+
 /* Launch-shape tuning of the batched/plain kernels (ray tile = rays per lane per
  * work item, warps per CTA). 0 leaves a value unchanged. */
 int cpd_set_launch_shape(cpd_context *ctx, uint32_t ray_tile, uint32_t warps_per_cta);
@@ -314,6 +333,13 @@ int cpd_server_create(cpd_context *ctx, uint64_t mem_budget_bytes, uint32_t slot
  * once. */
 int cpd_server_submit(cpd_server *sv, const cpd_design *designs, const cpd_batch_item *items,
                       uint32_t n, uint32_t trace_mode, uint64_t *request_id);
+/* cpd_server_submit with parameter records: the designs are built on the device inside
+ * their pass (as cpd_fitness_gpu_batch_params), so an optimizer that produces parameters
+ * needs no host build step. A pass holds requests of one trace mode, one kind (designs or
+ * parameter records) and one acceptance. */
+int cpd_server_submit_params(cpd_server *sv, const cpd_spectrometer_params *params,
+                             const cpd_batch_item *items, uint32_t n, double acceptance,
+                             uint32_t trace_mode, uint64_t *request_id);
 /* Waits up to timeout_ms for a request. On completion writes its n results, the time
  * from submit to completion (latency_ms, optional), forgets the request and returns
  * CPD_OK (or the error a pass met); on timeout returns CPD_TIMEOUT and the request
