@@ -299,10 +299,14 @@ def serving_form(ctx, generations=200):
         cap = sat["designs_per_s"]
         mean_gap = sat["mean_batch"] / (0.7 * cap)
         poi = gen.serve(sv, generations=generations, seed=3, mean_interarrival_s=mean_gap)
+        # the same back-to-back load with the designs built on the device (parameter
+        # records submitted; no host build step)
+        dev = gen.serve(sv, generations=generations, seed=2, device_build=True)
         st = sv.stats()
-    for r in (sat, poi):
+    for r in (sat, poi, dev):
         r.pop("latency_ms")
     out["back_to_back"] = sat
+    out["back_to_back_device_build"] = dev
     out["poisson_70pct"] = dict(poi, mean_interarrival_ms=1e3 * mean_gap)
     out["designs_per_s"] = cap
     out["server_only_designs_per_s"] = cap_pre

@@ -6,8 +6,9 @@
 //    with every rounding step made explicit. On the device the arithmetic uses
 //    the _rn intrinsics (no contraction); on the host this header is compiled with
 //    -ffp-contract=off. Both therefore give the reference's own f64 results bit
-//    for bit, given the same tables. Transcendentals (log in the inverse normal
-//    CDF, sin/cos in design construction) are evaluated on the host only.
+//    for bit, given the same tables. The log of the inverse normal CDF is evaluated
+//    on the host only; the sin/cos of design construction on the host, or with CUDA's
+//    f64 functions when the device builds the design (cpd_build.h).
 //  * Per-wavelength setup (lambda_setup_df, cpd_df.h): all rays of one wavelength
 //    leave the Gaussian beam with direction (1,0) (Ray::new_from_start,
 //    ray.rs:277-279), and every face before the curved exit face is flat, so the
