@@ -212,3 +212,18 @@ def test_repeat_calls_identical(designs):
     a = s.gpu_fitness_full([0.6], max_n=128, max_eval=2048)
     b = s.gpu_fitness_full([0.6], max_n=128, max_eval=2048)
     assert a.as_dict() == b.as_dict()
+
+
+@pytest.mark.parametrize("B", [1, 1024])
+def test_detector_size_extremes(B):
+    """One bin, and the largest detector the ABI accepts (CPD_MAX_BINS = 1024 bins, the
+    widest per-bin state of the entropy and adaptive kernels), fixed N and adaptive."""
+    rng = np.random.default_rng(4242 + B)
+    s, d, _ = synth.random_design(rng, 4, B)
+    err_p, mi_rel, f = _check_fitness(s, d, 64, 1024)
+    assert f.hits > 0
+    lam_u, ray_u = O.qrng_points(0.5, 48), O.qrng_points(0.25, 4096)
+    fa, p = s.gpu_fitness_points(lam_u, ray_u, mode=cpd.TRACE_HYBRID | cpd.SAMPLING_ADAPTIVE, want_p=True)
+    po, st, counts = O.fitness_adaptive_points(d, lam_u, ray_u, nthreads=NTHREADS)
+    assert fa.rays == int(counts.sum()) and fa.hits == st["hits"]
+    assert np.abs(p - po).max() <= 1e-6
