@@ -502,81 +502,6 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 
 constexpr int kEntropyThreads = 256;
 
-// Per-design finalize by one warp: H(D) from the per-bin sums, MI, and the SEM stop of
-// cuda_fitness (src/cuda_fitness.rs:392-422). f64 costs ~64 cycles per warp instruction
-// here (a division or square root ~700 cycles of latency), and this warp is the tail of
-// the plain call, so everything is float-float on the FP32 pipe: pbar = S1 / (n R 2^31),
-// log2 pbar = log2 S1 - log2(n R) - 31 (logs of integers, ff::log2_u64, absolute error
-// < 1e-12), and the Welford M2 of each bin, S2 - S1^2 / n, against (5e-3)^2 n (n - 1).
-// Only the conversion of the three results to double is f64.
-__device__ void finalize_warp(const LaunchArgs &a, uint32_t d, const DesignJob &J, uint32_t lane, const float *tab)
-{
-    using ff::F2;
-    const unsigned long long rows = __ldcg(&a.acc[d].rows) + J.W;
-    const F2 n = ff::from_u64(rows);
-    const F2 inv_n = df::rcp(n);
-    const F2 unit{J.unit_hi, J.unit_lo};  // p per count unit, 2^-31 / R
-    const F2 inv_nr = ff::mul(unit, inv_n);
-    const unsigned long long nR = rows * (unsigned long long)J.R;
-    const F2 lnr = ff::add_f(ff::log2_u64(nR, tab), 31.f);
-    const F2 thr = df::div(ff::mul(n, ff::from_u64(rows - 1ull)), df::c(40000.f));  // (5e-3)^2 n (n - 1)
-    const F2 s2unit{(float)kPScaleInv, 0.f};
-    F2 hdet{0.f, 0.f};
-    float m2max = 0.f;
-    int conv = 1;
-    for (uint32_t b = lane; b < J.B; b += 32u) {
-        const unsigned long long c1 = __ldcg(&a.S1[J.acc_off + b]);
-        const F2 sc1 = ff::from_u64(c1);
-        if (c1) {
-            const F2 pbar = ff::mul(sc1, inv_nr);
-            const F2 lg = ff::add(ff::log2_u64(c1, tab), F2{-lnr.hi, -lnr.lo});
-            hdet = ff::add(hdet, ff::mul(pbar, lg));
-        }
-        // Welford M2 of the per-wavelength p(d|lambda) (welford.rs:26-57)
-        const F2 s1 = ff::mul(sc1, unit);  // sum over rows of p
-        const F2 s2 = ff::mul(ff::from_u64(__ldcg(&a.S2[J.acc_off + b])), s2unit);
-        F2 m2 = df::sub(s2, ff::mul(ff::mul(s1, s1), inv_n));
-        if (df::neg_(m2)) m2 = F2{0.f, 0.f};
-        conv &= df::lt(m2, thr) ? 1 : 0;
-        m2max = fmaxf(m2max, m2.hi);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const F2 other{__shfl_xor_sync(0xffffffffu, hdet.hi, o), __shfl_xor_sync(0xffffffffu, hdet.lo, o)};
-        // the same pairs are added in the same order on every lane: a fixed tree
-        hdet = (lane & (uint32_t)o) ? ff::add(other, hdet) : ff::add(hdet, other);
-        m2max = fmaxf(m2max, __shfl_xor_sync(0xffffffffu, m2max, o));
-    }
-    conv = __all_sync(0xffffffffu, conv);
-    const bool cp = lane < (uint32_t)kSpread;
-    const unsigned long long hits = warp_sum_u64(cp ? __ldcg(&a.acc[d].hits[lane]) : 0ull);
-    const unsigned long long retraced = warp_sum_u64(cp ? __ldcg(&a.acc[d].retraced[lane]) : 0ull);
-    const unsigned long long fast = warp_sum_u64(cp ? __ldcg(&a.acc[d].fast[lane]) : 0ull);
-    if (lane == 0) {
-        const F2 H = ff::mul(ff::from_u64(__ldcg(&a.acc[d].H)), F2{(float)kHScaleInv, 0.f});
-        const F2 hc = ff::mul(H, inv_n);
-        const F2 h_cond{-hc.hi, -hc.lo};
-        const F2 info = df::sub(h_cond, hdet);
-        DesignOut o;
-        o.h_cond = (double)h_cond.hi + (double)h_cond.lo;
-        o.h_det = (double)hdet.hi + (double)hdet.lo;
-        o.info = (double)info.hi + (double)info.lo;
-        const float fn = (float)rows;
-        o.max_sem = rows > 1ull ? (double)sqrtf(m2max / (fn - 1.f) / fn) : (double)INFINITY;
-        const DevDesign &D = a.designs[d];
-        o.size = D.size;
-        o.deviation = D.deviation;
-        o.hits = hits;
-        o.retraced = retraced;
-        o.rows = rows;
-        o.fast = fast;
-        o.converged = conv;
-        o.status = D.status;
-        a.out[d] = o;
-        a.acc[d].rows = rows;
-    }
-}
-
 // A non-negative float-float value in fixed point with `scale` units, its hi and lo
 // words rounded separately: one rounding per cell, so that the sums over cells are integer
 // sums whose value does not depend on how the cells are grouped.
@@ -596,6 +521,107 @@ __device__ __forceinline__ unsigned long long df_to_fixed(ff::F2 v, float scale)
     // |lo| is below half an ulp of hi: |lo scale| < 2^23
     const long long r = (long long)q + __float2int_rn(v.lo * scale);
     return r > 0 ? (unsigned long long)r : 0ull;
+}
+
+// Per-design finalize: H(D) from the per-bin sums, MI, and the SEM stop of cuda_fitness
+// (src/cuda_fitness.rs:392-422), by nthr threads (one warp, or the 256 threads of an entropy
+// block; red: nthr / 32 scratch records in shared memory when nthr > 32). f64 costs ~64
+// cycles per warp instruction here (a division or square root ~700 cycles of latency), and
+// this runs on the tail of the plain call, so everything is float-float on the FP32 pipe:
+// pbar = S1 / (n R 2^31), log2 pbar = log2 S1 - log2(n R) - 31 (logs of integers,
+// ff::log2_u64, absolute error < 1e-12), each bin's pbar log2 pbar rounded once to 2^-50
+// fixed point (so the sum over bins is the same integer for any number of threads), and
+// each bin's Welford M2, S2 - S1^2 / n, against (5e-3)^2 n (n - 1). Only the conversion of
+// the three results to double is f64.
+struct FinalizeRed {
+    long long hdet;
+    float m2max;
+    int conv;
+};
+constexpr float kHdetScale = 1125899906842624.0f;  // 2^50
+
+__device__ void finalize_design(const LaunchArgs &a, uint32_t d, const DesignJob &J, uint32_t tid, uint32_t nthr,
+                                const float *tab, FinalizeRed *red)
+{
+    using ff::F2;
+    const uint32_t lane = tid & 31u;
+    const unsigned long long rows = __ldcg(&a.acc[d].rows) + J.W;
+    const F2 n = ff::from_u64(rows);
+    const F2 inv_n = df::rcp(n);
+    const F2 unit{J.unit_hi, J.unit_lo};  // p per count unit, 2^-31 / R
+    const F2 inv_nr = ff::mul(unit, inv_n);
+    const unsigned long long nR = rows * (unsigned long long)J.R;
+    const F2 lnr = ff::add_f(ff::log2_u64(nR, tab), 31.f);
+    const F2 thr = df::div(ff::mul(n, ff::from_u64(rows - 1ull)), df::c(40000.f));  // (5e-3)^2 n (n - 1)
+    const F2 s2unit{(float)kPScaleInv, 0.f};
+    long long hdet = 0;  // sum of pbar log2 pbar (<= 0), 2^-50 units
+    float m2max = 0.f;
+    int conv = 1;
+    for (uint32_t b = tid; b < J.B; b += nthr) {
+        const unsigned long long c1 = __ldcg(&a.S1[J.acc_off + b]);
+        const F2 sc1 = ff::from_u64(c1);
+        if (c1) {
+            const F2 pbar = ff::mul(sc1, inv_nr);
+            const F2 lg = ff::add(ff::log2_u64(c1, tab), F2{-lnr.hi, -lnr.lo});
+            const F2 pl = ff::mul(pbar, lg);
+            hdet -= (long long)df_to_fixed(F2{-pl.hi, -pl.lo}, kHdetScale);
+        }
+        // Welford M2 of the per-wavelength p(d|lambda) (welford.rs:26-57)
+        const F2 s1 = ff::mul(sc1, unit);  // sum over rows of p
+        const F2 s2 = ff::mul(ff::from_u64(__ldcg(&a.S2[J.acc_off + b])), s2unit);
+        F2 m2 = df::sub(s2, ff::mul(ff::mul(s1, s1), inv_n));
+        if (df::neg_(m2)) m2 = F2{0.f, 0.f};
+        conv &= df::lt(m2, thr) ? 1 : 0;
+        m2max = fmaxf(m2max, m2.hi);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        hdet += (long long)__shfl_xor_sync(0xffffffffu, (unsigned long long)hdet, o);
+        m2max = fmaxf(m2max, __shfl_xor_sync(0xffffffffu, m2max, o));
+    }
+    conv = __all_sync(0xffffffffu, conv);
+    if (nthr > 32u) {
+        if (lane == 0) red[tid >> 5] = FinalizeRed{hdet, m2max, conv};
+        __syncthreads();
+        if (tid >= 32u) return;
+        const uint32_t nw = nthr >> 5;
+        FinalizeRed r = lane < nw ? red[lane] : FinalizeRed{0, 0.f, 1};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            r.hdet += (long long)__shfl_xor_sync(0xffffffffu, (unsigned long long)r.hdet, o);
+            r.m2max = fmaxf(r.m2max, __shfl_xor_sync(0xffffffffu, r.m2max, o));
+        }
+        hdet = r.hdet;
+        m2max = r.m2max;
+        conv = __all_sync(0xffffffffu, r.conv);
+    }
+    const bool cp = lane < (uint32_t)kSpread;
+    const unsigned long long hits = warp_sum_u64(cp ? __ldcg(&a.acc[d].hits[lane]) : 0ull);
+    const unsigned long long retraced = warp_sum_u64(cp ? __ldcg(&a.acc[d].retraced[lane]) : 0ull);
+    const unsigned long long fast = warp_sum_u64(cp ? __ldcg(&a.acc[d].fast[lane]) : 0ull);
+    if (lane == 0) {
+        const F2 H = ff::mul(ff::from_u64(__ldcg(&a.acc[d].H)), F2{(float)kHScaleInv, 0.f});
+        const F2 hc = ff::mul(H, inv_n);
+        const double h_cond = -((double)hc.hi + (double)hc.lo);
+        const double h_det = (double)hdet * (1.0 / 1125899906842624.0);
+        DesignOut o;
+        o.h_cond = h_cond;
+        o.h_det = h_det;
+        o.info = h_cond - h_det;
+        const float fn = (float)rows;
+        o.max_sem = rows > 1ull ? (double)sqrtf(m2max / (fn - 1.f) / fn) : (double)INFINITY;
+        const DevDesign &D = a.designs[d];
+        o.size = D.size;
+        o.deviation = D.deviation;
+        o.hits = hits;
+        o.retraced = retraced;
+        o.rows = rows;
+        o.fast = fast;
+        o.converged = conv;
+        o.status = D.status;
+        a.out[d] = o;
+        a.acc[d].rows = rows;
+    }
 }
 
 // One nonzero cell of the histogram: -p log2 p (2^-40 units) and p^2 (2^-46 units) in
@@ -713,7 +739,7 @@ __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_warp_kernel(const 
         else entropy_tile<1>(a, J, r0, r1, lane, tab, hl);
         hl = warp_sum_u64(hl);
         if (lane == 0 && hl) atomicAdd(&a.acc[d].H, hl);
-        if (a.njobs == 1 && last_tile_of_design(a, J, lane)) finalize_warp(a, d, J, lane, tab);
+        if (a.njobs == 1 && last_tile_of_design(a, J, lane)) finalize_design(a, d, J, lane, 32u, tab, nullptr);
     }
 }
 
@@ -731,6 +757,7 @@ __global__ void __launch_bounds__(kEntropyThreads, 4) entropy_block_kernel(const
     extern __shared__ __align__(16) unsigned long long ent_smem[];  // per-bin s1, s2 (max_B each)
     __shared__ unsigned long long hsum;
     __shared__ unsigned last_tile;
+    __shared__ FinalizeRed fin_red[kEntropyThreads / 32];
     cudaTriggerProgrammaticLaunchCompletion();
     for (uint32_t i = threadIdx.x; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = a.logtab[i];
     __syncthreads();
@@ -755,23 +782,36 @@ __global__ void __launch_bounds__(kEntropyThreads, 4) entropy_block_kernel(const
         const uint32_t db = (uint32_t)kEntropyThreads % B, dr = (uint32_t)kEntropyThreads / B;
         uint32_t b = t % B, row = r0 + t / B;
         unsigned long long hl = 0ull;
-        for (uint32_t i = t; i < cells; i += kEntropyThreads) {
-            const uint64_t idx = (uint64_t)row * B + b;
-            const unsigned long long cv = base[idx];
-            if (cv) {
-                base[idx] = 0ull;
-                unsigned long long hq, pq;
-                entropy_cell(cv, unit, lu, tab, hq, pq);
-                hl += hq;
-                atomicAdd(s1 + b, cv);
-                atomicAdd(s2 + b, pq);
+        // two cells per step, both loaded before either is processed, so that their
+        // memory latencies and their float-float chains overlap
+        for (uint32_t i0 = t; i0 < cells; i0 += 2u * kEntropyThreads) {
+            uint64_t idx[2];
+            uint32_t bc[2];
+            unsigned long long cv[2];
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const bool in = i0 + (uint32_t)k * kEntropyThreads < cells;
+                idx[k] = (uint64_t)row * B + b;
+                bc[k] = b;
+                cv[k] = in ? base[idx[k]] : 0ull;
+                if (in && a.p_out) a.p_out[idx[k]] = (double)cv[k] * (kTScaleInv / (double)J.R);
+                b += db;
+                row += dr;
+                if (b >= B) {
+                    b -= B;
+                    row++;
+                }
             }
-            if (a.p_out) a.p_out[idx] = (double)cv * (kTScaleInv / (double)J.R);
-            b += db;
-            row += dr;
-            if (b >= B) {
-                b -= B;
-                row++;
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                if (cv[k]) {
+                    base[idx[k]] = 0ull;
+                    unsigned long long hq, pq;
+                    entropy_cell(cv[k], unit, lu, tab, hq, pq);
+                    hl += hq;
+                    atomicAdd(s1 + bc[k], cv[k]);
+                    atomicAdd(s2 + bc[k], pq);
+                }
             }
         }
         hl = warp_sum_u64(hl);
@@ -793,9 +833,9 @@ __global__ void __launch_bounds__(kEntropyThreads, 4) entropy_block_kernel(const
             __syncthreads();
             if (t == 0) last_tile = atomicAdd(&a.ctl->tiles_done, 1u) == J.ntiles - 1u ? 1u : 0u;
             __syncthreads();
-            if (last_tile && t < 32u) {
+            if (last_tile) {
                 __threadfence();
-                finalize_warp(a, d, J, lane, tab);
+                finalize_design(a, d, J, t, kEntropyThreads, tab, fin_red);
             }
         }
         __syncthreads();  // the shared sums are reused by the block's next tile
@@ -815,7 +855,7 @@ __global__ void __launch_bounds__(128) finalize_kernel(const LaunchArgs a)
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; d < a.njobs; d += nw) {
         const DesignJob J = a.jobs[d];
-        finalize_warp(a, d, J, lane, tab);
+        finalize_design(a, d, J, lane, 32u, tab, nullptr);
     }
 }
 
