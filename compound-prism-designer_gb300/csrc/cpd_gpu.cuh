@@ -117,8 +117,9 @@ struct LaunchArgs {
     const float *logtab;  // float-float log2 table (cpd_ff.h), 4 x 256 floats
 };
 
-// Most warps that trace one wavelength's rounds at once under adaptive sampling.
-constexpr uint32_t kMaxAdaptWarps = 4;
+// Most warps that trace (and decide) one wavelength's rounds at once under adaptive
+// sampling: one round per warp.
+constexpr uint32_t kMaxAdaptWarps = 8;
 
 // Per-bin state of one wavelength under adaptive sampling: shared memory, one array per
 // field (consecutive bins in consecutive words), carved from B-sized slices.
@@ -128,6 +129,9 @@ struct BinStates {
     unsigned long long *q2;  // sum of t_q^2
     uint32_t *n;             // Welford samples: the sizes of the rounds that hit the bin
     uint32_t *h;             // hits
+    // Within one group of rounds: for round w of the group, byte w & 3 of word 2 b + w / 4
+    // holds 1 + the lane that carries the round's sums for bin b (0: the round missed b).
+    uint32_t *lanes;
     __device__ BinStates(void *base, uint32_t B)
     {
         s1 = static_cast<unsigned long long *>(base);
@@ -135,10 +139,11 @@ struct BinStates {
         q2 = q1 + B;
         n = reinterpret_cast<uint32_t *>(q2 + B);
         h = n + B;
+        lanes = h + B;
     }
 };
 // Bytes of shared memory the bin states of a B-bin detector take.
-constexpr size_t bin_state_bytes(uint32_t B) { return (size_t)B * (3 * 8 + 2 * 4); }
+constexpr size_t bin_state_bytes(uint32_t B) { return (size_t)B * (3 * 8 + 4 * 4); }
 
 // Launches setup -> trace -> retrace -> entropy -> finalize on `stream` (adaptive
 // sampling: setup -> adaptive rounds -> exact rounds of the unsure rows -> entropy ->

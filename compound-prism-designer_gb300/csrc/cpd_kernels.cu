@@ -299,32 +299,54 @@ __device__ __noinline__ uint2 trace_df_exact_call(const DevDesign &D, const LamD
     return trace_df_exact_packed(D, E, zh, zl);
 }
 
-// Per-block scratch of the adaptive kernels: KW warps trace KW rounds of one wavelength
-// at once (warp w takes round g0 + w of the group), and warp 0 then applies them in order.
-struct RoundSlots {
-    uint32_t bin[kMaxAdaptWarps][32];  // ~0u: no hit
-    uint32_t tf[kMaxAdaptWarps][32];   // t_fixed of a hit
-    uint32_t df[kMaxAdaptWarps];       // ballot of the rays traced in float-float
-    uint32_t flag;                     // 0 go on, 1 stopped or out of rays, 2 unsure
-    uint32_t count;                    // rays consumed
+// Per-warp scratch of the adaptive kernels (dynamic shared memory, one slot per warp,
+// before the bin states). A group of KW rounds is traced by KW warps, warp w taking round
+// w of the group; each warp sums its round's hits per bin into its slot, and the group's
+// stop decisions are then taken by all warps at once, each from its round's exact Welford
+// states (the states at the group's start plus the sums of the group's rounds up to its
+// own). The first round that stops, or that the FP32 sums cannot settle, ends the row.
+struct RoundSlot {
+    unsigned long long s1[32];  // leader lane of a bin: the round's sum of t_fixed there
+    unsigned long long q2[32];  // ... of t_q^2
+    uint32_t q1[32];            // ... of t_q
+    uint32_t hc[32];            // ... and its hits
+    uint32_t tf[32];            // each lane's t_fixed (0: no hit)
+    uint32_t df;                // ballot of the rays traced in float-float
+    uint32_t nh;                // hits of the round
+    uint32_t verdict;           // 0 go on, 1 stop, 2 unsure
+    uint32_t pad;
 };
+static_assert(sizeof(RoundSlot) % 16 == 0, "bin states follow the slots 16-byte aligned");
+// Dynamic shared memory of an adaptive block of KW warps over B-bin detectors.
+constexpr size_t adapt_smem_bytes(uint32_t KW, uint32_t B) { return KW * sizeof(RoundSlot) + bin_state_bytes(B); }
+static_assert(adapt_smem_bytes(kMaxAdaptWarps, CPD_MAX_BINS) <= 48u * 1024u, "default shared memory limit");
+
+// Byte v of a bin's group lane table (v = the round within the group).
+__device__ __forceinline__ uint32_t lane_entry(uint32_t w0, uint32_t w1, uint32_t v)
+{
+    return ((v < 4u ? w0 : w1) >> (8u * (v & 3u))) & 0xffu;
+}
 
 // One wavelength row under adaptive sampling (the stop rule of src/spectrometer/
 // kernel.rs:127-178, restated with exact integer Welford sums: cpd_model.h, sem_test)
-// by one block of KW warps; st holds the row's B bin states in shared memory.
+// by one block of KW warps; the bin states live in shared memory after the KW slots.
 // Tracing: lane l of warp w takes ray g0 + 32 w + l in index order; `rank` maps it to its
 // place in the sorted z table, whose band / core ranges (from the setup) say how to trace
 // it: lost outside the band, the FP32 fast path inside the core, the float-float trace
 // (exact transmittance) otherwise or when the fast path flags it.
-// Applying a round (warp 0): its hits add to their bins' sums with shared-memory integer
-// atomics (order-independent), one leader lane per bin hit adds the round's size to the
-// bin's Welford count and runs its SEM test, all bins at once. Rounds of a group after the
-// one that stops the wavelength were traced for nothing and are dropped.
+// Deciding: each bin a round hit is led by the lowest lane that hit it; the leader sums
+// the round's hits there, and the bin's group lane table records which lane of which round
+// holds those sums. A round's leaders then add the sums of the group's rounds up to theirs
+// to the states at the group's start, run the SEM test, and vote: the round stops the row
+// when it hit some bin and every bin it hit passes. Rounds after the first one that stops
+// were traced for nothing and are dropped; the states through that round are written back
+// by the leader of each bin's latest round. Everything is integer, so the result equals
+// the one-round-at-a-time order bit for bit.
 // kExact: every ray by the float-float trace and the exact test. Otherwise a row whose
 // stop decision the FP32 transmittances cannot settle (sem_test: SEM_UNSURE) is queued
 // for the exact path and leaves nothing behind.
 template <bool kExact>
-__device__ void adaptive_row(const LaunchArgs &a, uint64_t row, void *st_base, RoundSlots &rs, uint32_t KW,
+__device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long long *smem, uint32_t KW,
                              uint32_t warp, uint32_t lane)
 {
     const uint32_t d = find_job<F_ROW>(a.jobs, a.njobs, row);
@@ -332,155 +354,211 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, void *st_base, R
     const uint32_t k = (uint32_t)(row - J.row_off);
     const uint32_t B = J.B, R = J.R;
     const DevDesign &D = a.designs[d];
+    const uint32_t tid = warp * 32u + lane, nthr = KW * 32u;
     if (!kExact && a.adaptive == 2u) {
         // verification mode: every row on the exact path
-        if (warp == 0 && lane == 0) {
+        if (tid == 0) {
             const unsigned long long pos = atomicAdd(&a.ctl->queue_count, 1ull);
             if (pos < a.qcap) a.queue[pos] = QEntry{d, k, 0u, 0u};
             else atomicOr(&a.ctl->overflow, 1u);
         }
         return;
     }
+    RoundSlot *slots = reinterpret_cast<RoundSlot *>(smem);
+    RoundSlot &my = slots[warp];
     const FastConst C = D.fc;
     const LamParams P = a.lp[row];
     const LamDF &E = a.lx[row];
-    const BinStates st(st_base, B);
-    for (uint32_t b = warp * 32u + lane; b < B; b += KW * 32u) {
+    const BinStates st(slots + KW, B);
+    for (uint32_t b = tid; b < B; b += nthr) {
         st.s1[b] = st.q1[b] = st.q2[b] = 0ull;
         st.n[b] = st.h[b] = 0u;
-    }
-    if (warp == 0 && lane == 0) {
-        rs.flag = 0u;
-        rs.count = 0u;
+        st.lanes[2u * b] = st.lanes[2u * b + 1u] = 0u;
     }
     __syncthreads();
     const uint32_t *rank = a.rank + J.rank_off;
     const float2 *zt = reinterpret_cast<const float2 *>(a.z32) + J.ray_off;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    uint32_t count = 0, hits = 0, ndf = 0;  // warp 0
+    uint32_t count = 0, hits = 0, ndf = 0, flag = 0;  // the same in every thread
     // no ray clears the flat faces: every round runs without a hit
     const uint32_t g_start = P.band_lo >= P.band_hi ? R : 0u;
-    if (g_start == R && warp == 0) count = R;
+    if (g_start == R) count = R;
+    // the ray a lane traces in the next group, loaded while the current group is decided:
+    // its sorted position (~0u: none, or no finite start height; outside the band either
+    // way) and its start height
+    uint32_t s_nx = 0xffffffffu;
+    float2 z_nx = make_float2(0.f, 0.f);
+    const auto fetch = [&](uint32_t g) {
+        const uint32_t j = g + warp * kRoundRays + lane;
+        s_nx = j < R ? rank[j] : 0xffffffffu;
+        if (s_nx >= P.band_lo && s_nx < P.band_hi) z_nx = zt[s_nx];
+    };
+    if (g_start < R) fetch(g_start);
     for (uint32_t g0 = g_start; g0 < R; g0 += KW * kRoundRays) {
+        // 1. trace round `warp` of the group; each bin's leader sums the round's hits there
+        uint32_t bin = 0xffffffffu, tf = 0u;
+        bool used_df = false;
         {
-            const uint32_t j = g0 + warp * kRoundRays + lane;
-            uint32_t bin = 0xffffffffu, tf = 0u;
-            bool used_df = false;
-            if (j < R) {
-                const uint32_t s = rank[j];  // ~0u (no finite start height) is outside the band
-                if (s >= P.band_lo && s < P.band_hi) {
-                    const float2 z = zt[s];
-                    int res = RAY_FLAG;
-                    if (!kExact && !P.all_exact && s >= P.core_lo && s < P.core_hi) {
-                        uint32_t b = 0;
-                        float t = 0.f;
-                        res = fast_ray(C, P, a.guards, z.x, z.y, b, t);
-                        if (res == RAY_HIT) {
-                            bin = b;
-                            tf = t_fixed(t);
-                        }
-                    }
-                    if (res == RAY_FLAG) {
-                        const uint2 r = kExact ? trace_df_exact_packed(D, E, z.x, z.y)
-                                               : trace_df_exact_call(D, E, z.x, z.y);
-                        bin = r.x;
-                        tf = r.y;
-                        used_df = true;
+            const uint32_t s = s_nx;
+            if (s >= P.band_lo && s < P.band_hi) {
+                const float2 z = z_nx;
+                int res = RAY_FLAG;
+                if (!kExact && !P.all_exact && s >= P.core_lo && s < P.core_hi) {
+                    uint32_t b = 0;
+                    float t = 0.f;
+                    res = fast_ray(C, P, a.guards, z.x, z.y, b, t);
+                    if (res == RAY_HIT) {
+                        bin = b;
+                        tf = t_fixed(t);
                     }
                 }
-            }
-            rs.bin[warp][lane] = bin;
-            rs.tf[warp][lane] = tf;
-            const uint32_t dfb = __ballot_sync(0xffffffffu, used_df);
-            if (lane == 0) rs.df[warp] = dfb;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            uint32_t flag = 0u;
-            for (uint32_t w = 0; w < KW; w++) {
-                const uint32_t r0 = g0 + w * kRoundRays;
-                if (r0 >= R) break;
-                const uint32_t nr = min(kRoundRays, R - r0);
-                const uint32_t bin = rs.bin[w][lane], tf = rs.tf[w][lane];
-                const bool hit = bin != 0xffffffffu;
-                const uint32_t hm = __ballot_sync(0xffffffffu, hit);
-                count += nr;
-                hits += __popc(hm);
-                ndf += __popc(rs.df[w]);
-                if (!hm) continue;  // no hit: a certain "go on"
-                const uint32_t grp = __match_any_sync(0xffffffffu, bin);
-                if (hit) {
-                    const uint32_t q = tf >> kTqShift;  // <= 2^20
-                    atomicAdd(st.s1 + bin, (unsigned long long)tf);
-                    atomicAdd(st.q1 + bin, (unsigned long long)q);
-                    atomicAdd(st.q2 + bin, (unsigned long long)q * q);
+                if (res == RAY_FLAG) {
+                    const uint2 r = kExact ? trace_df_exact_packed(D, E, z.x, z.y)
+                                           : trace_df_exact_call(D, E, z.x, z.y);
+                    bin = r.x;
+                    tf = r.y;
+                    used_df = true;
                 }
-                __syncwarp();
-                int verdict = SEM_PASS;
-                if (hit && (grp & lt_mask) == 0u) {  // the lowest lane of each bin's group
-                    const uint32_t n = st.n[bin] + nr, h = st.h[bin] + (uint32_t)__popc(grp);
-                    st.n[bin] = n;
-                    st.h[bin] = h;
-                    verdict = sem_test(n, h, st.q1[bin], st.q2[bin], kExact ? 0u : kTqDelta);
-                }
-                const bool fail = __any_sync(0xffffffffu, verdict == SEM_FAIL);
-                const bool unsure = __any_sync(0xffffffffu, verdict == SEM_UNSURE);
-                __syncwarp();
-                if (fail) continue;
-                flag = (!kExact && unsure) ? 2u : 1u;
-                break;
-            }
-            if (!flag && g0 + KW * kRoundRays >= R) flag = 1u;  // out of rays
-            if (lane == 0) {
-                rs.flag = flag;
-                rs.count = count;
             }
         }
-        __syncthreads();
-        if (rs.flag) break;
-    }
-    if (warp == 0 && rs.flag == 2u) {
+        if (g0 + KW * kRoundRays < R) fetch(g0 + KW * kRoundRays);
+        const bool hit = bin != 0xffffffffu;
+        const uint32_t hm = __ballot_sync(0xffffffffu, hit);
+        const uint32_t dfb = __ballot_sync(0xffffffffu, used_df);
+        const uint32_t grp = __match_any_sync(0xffffffffu, bin);
+        const bool leader = hit && (grp & lt_mask) == 0u;
         if (lane == 0) {
+            my.df = dfb;
+            my.nh = (uint32_t)__popc(hm);
+        }
+        my.tf[lane] = hit ? tf : 0u;
+        __syncwarp();
+        if (leader) {  // the bin's sums over its lanes
+            unsigned long long s1 = 0, q2 = 0;
+            uint32_t q1 = 0;
+            for (uint32_t m = grp; m; m &= m - 1u) {
+                const uint32_t t = my.tf[__ffs(m) - 1], q = t >> kTqShift;  // q <= 2^20
+                s1 += t;
+                q1 += q;
+                q2 += (unsigned long long)q * q;
+            }
+            my.s1[lane] = s1;
+            my.q1[lane] = q1;
+            my.q2[lane] = q2;
+            my.hc[lane] = (uint32_t)__popc(grp);
+            atomicOr(st.lanes + 2u * bin + (warp >> 2), (lane + 1u) << (8u * (warp & 3u)));
+        }
+        __syncthreads();
+        // 2. every round's decision at once, from the states through that round
+        uint32_t w0 = 0, w1 = 0;
+        unsigned long long cs1 = 0, cq1 = 0, cq2 = 0;
+        uint32_t cn = 0, ch = 0;
+        int verdict = SEM_PASS;
+        if (leader) {
+            w0 = st.lanes[2u * bin];
+            w1 = st.lanes[2u * bin + 1u];
+            cs1 = st.s1[bin];
+            cq1 = st.q1[bin];
+            cq2 = st.q2[bin];
+            cn = st.n[bin];
+            ch = st.h[bin];
+#pragma unroll
+            for (uint32_t v = 0; v < kMaxAdaptWarps; v++) {
+                const uint32_t l = v <= warp ? lane_entry(w0, w1, v) : 0u;
+                if (!l) continue;
+                const RoundSlot &o = slots[v];
+                cs1 += o.s1[l - 1u];
+                cq1 += o.q1[l - 1u];
+                cq2 += o.q2[l - 1u];
+                ch += o.hc[l - 1u];
+                cn += min(kRoundRays, R - (g0 + v * kRoundRays));
+            }
+            verdict = sem_quick(cn, ch, cq1, cq2, kExact ? 0u : kTqDelta);
+        }
+        if (__any_sync(0xffffffffu, verdict < 0) && verdict < 0)
+            verdict = sem_test(cn, ch, cq1, cq2, kExact ? 0u : kTqDelta);
+        const bool fail = __any_sync(0xffffffffu, verdict == SEM_FAIL);
+        const bool unsure = __any_sync(0xffffffffu, verdict == SEM_UNSURE);
+        if (lane == 0) my.verdict = (!hm || fail) ? 0u : (!kExact && unsure) ? 2u : 1u;
+        __syncthreads();
+        // 3. the first round that stops ends the row; the states through it are kept
+        // (lane v reads round v's verdict and counts)
+        const uint32_t vv = lane < KW ? slots[lane].verdict : 0u;
+        const uint32_t vb = __ballot_sync(0xffffffffu, vv != 0u);
+        const uint32_t last = vb ? (uint32_t)__ffs(vb) - 1u : KW - 1u;
+        if (vb) flag = __shfl_sync(0xffffffffu, vv, last);
+        {
+            const uint32_t rv = g0 + lane * kRoundRays;
+            const bool in = lane <= last && rv < R;
+            count += __reduce_add_sync(0xffffffffu, in ? min(kRoundRays, R - rv) : 0u);
+            hits += __reduce_add_sync(0xffffffffu, in ? slots[lane].nh : 0u);
+            ndf += __reduce_add_sync(0xffffffffu, in ? (uint32_t)__popc(slots[lane].df) : 0u);
+        }
+        if (leader) {
+            uint32_t later = 0, earlier = 0;
+            for (uint32_t v = warp + 1u; v <= last; v++) later |= lane_entry(w0, w1, v);
+            for (uint32_t v = 0; v < warp; v++) earlier |= lane_entry(w0, w1, v);
+            if (warp <= last && !later) {  // the bin's latest round through `last`
+                st.s1[bin] = cs1;
+                st.q1[bin] = cq1;
+                st.q2[bin] = cq2;
+                st.n[bin] = cn;
+                st.h[bin] = ch;
+            }
+            if (!earlier) {  // the bin's first round of the group clears its lane table
+                st.lanes[2u * bin] = 0u;
+                st.lanes[2u * bin + 1u] = 0u;
+            }
+        }
+        if (!flag && g0 + KW * kRoundRays >= R) flag = 1u;  // out of rays
+        __syncthreads();
+        if (flag) break;
+    }
+    if (flag == 2u) {
+        if (tid == 0) {
             const unsigned long long pos = atomicAdd(&a.ctl->queue_count, 1ull);
             if (pos < a.qcap) a.queue[pos] = QEntry{d, k, 0u, 0u};
             else atomicOr(&a.ctl->overflow, 1u);
         }
-    } else if (warp == 0) {
+    } else {
         unsigned long long *hrow = a.hist + J.hist_off + (uint64_t)k * B;
-        for (uint32_t b = lane; b < B; b += 32u) {
+        for (uint32_t b = tid; b < B; b += nthr) {
             const unsigned long long s1 = st.s1[b];
             if (s1) hrow[b] = rescale_cell(s1, R, count);
         }
-        if (lane == 0) {
+        if (tid == 0) {
             const uint32_t sp = (uint32_t)(row % (uint64_t)kSpread);
             atomicAdd(&a.acc[d].fast[sp], (unsigned long long)count);
             if (hits) atomicAdd(&a.acc[d].hits[sp], (unsigned long long)hits);
             if (ndf) atomicAdd(&a.acc[d].retraced[sp], (unsigned long long)ndf);
         }
     }
-    __syncthreads();  // every warp: st and rs are reused by the block's next row
+    __syncthreads();  // the slots and bin states are reused by the block's next row
 }
 
+#ifndef CPD_ADAPT_KW_MANY
+#define CPD_ADAPT_KW_MANY 2  // warps per row when at least 8 rows per SM
+#endif
+#ifndef CPD_ADAPT_KW_SOME
+#define CPD_ADAPT_KW_SOME 4  // warps per row at 2 to 7 rows per SM
+#endif
 #ifndef CPD_ADAPT_MIN_BLOCKS
-#define CPD_ADAPT_MIN_BLOCKS 8  // 64 registers: more resident rows, which the one-warp rows need
+#define CPD_ADAPT_MIN_BLOCKS 4  // 64 registers at kMaxAdaptWarps warps per block
 #endif
 // One row per block of KW = blockDim.x / 32 warps: rows differ widely in length (a single
 // round to all R / 32), and one row per block lets the block scheduler balance them.
 __global__ void __launch_bounds__(32 * kMaxAdaptWarps, CPD_ADAPT_MIN_BLOCKS) adaptive_kernel(const LaunchArgs a)
 {
     extern __shared__ __align__(16) unsigned long long adapt_smem[];
-    __shared__ RoundSlots rs;
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();  // the setup's LamParams and LamDF
-    adaptive_row<false>(a, blockIdx.x, adapt_smem, rs, blockDim.x >> 5,
-                        threadIdx.x >> 5, threadIdx.x & 31u);
+    adaptive_row<false>(a, blockIdx.x, adapt_smem, blockDim.x >> 5, threadIdx.x >> 5, threadIdx.x & 31u);
 }
 
 // The queued rows: the float-float path from the first round on, one warp per block.
 __global__ void __launch_bounds__(32) adaptive_exact_kernel(const LaunchArgs a)
 {
     extern __shared__ __align__(16) unsigned long long adapt_smem[];
-    __shared__ RoundSlots rs;
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();  // the adaptive kernel's queue
     publish_status(a);
@@ -488,8 +566,7 @@ __global__ void __launch_bounds__(32) adaptive_exact_kernel(const LaunchArgs a)
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
     for (uint64_t i = blockIdx.x; i < n; i += gridDim.x) {
         const QEntry e = a.queue[i];
-        adaptive_row<true>(a, a.jobs[e.design].row_off + e.k, adapt_smem, rs, 1u, 0u,
-                           threadIdx.x);
+        adaptive_row<true>(a, a.jobs[e.design].row_off + e.k, adapt_smem, 1u, 0u, threadIdx.x);
     }
 }
 
@@ -981,18 +1058,19 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         launches++;
     }
     if (a.adaptive) {
-        const size_t smem = bin_state_bytes(a.max_B ? a.max_B : (uint32_t)CPD_MAX_BINS);
+        const uint32_t maxB = a.max_B ? a.max_B : (uint32_t)CPD_MAX_BINS;
         if (ev) cudaEventRecord(ev[1], stream);
         if (a.total_rows) {
-            // enough rows to fill the GPU: one warp per row; fewer: up to kMaxAdaptWarps
-            // warps per row trace that many rounds at once
+            // enough rows to fill the GPU: few warps per row (rounds traced past a row's
+            // stop are wasted); fewer rows: up to kMaxAdaptWarps warps per row trace and
+            // decide that many rounds at once
             const uint64_t per_sm = a.total_rows / (uint64_t)num_sms;
-            const uint32_t kw = per_sm >= 8 ? 1u : per_sm >= 2 ? 2u : kMaxAdaptWarps;
-            launch_k(adaptive_kernel, (unsigned)a.total_rows, 32 * kw, smem, stream, pdl, a);
+            const uint32_t kw = per_sm >= 8 ? CPD_ADAPT_KW_MANY : per_sm >= 2 ? CPD_ADAPT_KW_SOME : kMaxAdaptWarps;
+            launch_k(adaptive_kernel, (unsigned)a.total_rows, 32 * kw, adapt_smem_bytes(kw, maxB), stream, pdl, a);
             launches++;
         }
         if (ev) cudaEventRecord(ev[2], stream);
-        launch_k(adaptive_exact_kernel, (unsigned)(num_sms * 8), 32, smem, stream, pdl, a);
+        launch_k(adaptive_exact_kernel, (unsigned)(num_sms * 8), 32, adapt_smem_bytes(1u, maxB), stream, pdl, a);
         launches++;
     } else {
     if (ev) cudaEventRecord(ev[1], stream);

@@ -463,6 +463,28 @@ CPD_HD int sem_test(uint64_t N, uint64_t h, uint64_t q1, uint64_t q2, uint32_t d
     return SEM_UNSURE;
 }
 
+// An FP32 screen of sem_test (same arguments, N <= 2^22): SEM_PASS or SEM_FAIL when
+// float arithmetic with error bounds settles the test, else -1 (run sem_test). With
+// A = N q2 and Q = q1^2 in float, every conversion, product and sum rounds by at most
+// 2^-24 relative, so the computed 40000 (A - Q) is within 6 2^-24 40000 (A + Q) of lhs and
+// the computed N^2 (N - 1) 2^40 within 3 2^-24 of rhs; the margins (2^-18 of the terms,
+// and of the err bound) exceed those errors and the rounding of the comparisons' own sums.
+CPD_HD int sem_quick(uint32_t N, uint32_t h, uint64_t q1, uint64_t q2, uint32_t delta)
+{
+    const float n = (float)N, f1 = (float)q1, f2 = (float)q2;
+    const float A = n * f2, Q = f1 * f1;
+    const float L = 40000.f * (A - Q), eL = 40000.f * 0x1p-18f * (A + Q);
+    const float Y = n * n * (n - 1.f) * 0x1p40f, eY = Y * 0x1p-18f;
+    float E = 0.f;
+    if (delta) {
+        const float d = (float)delta, hd = (float)h * d;
+        E = 40000.f * (n * (float)h * (d * (0x1p21f + d)) + hd * (2.f * f1 + hd)) * (1.f + 0x1p-18f);
+    }
+    if (L + eL + E < Y - eY) return SEM_PASS;
+    if (L - eL >= Y + eY + E) return SEM_FAIL;
+    return -1;
+}
+
 // A cell's sum of t over `count` rays rescaled to the pass's common divisor R:
 // round(s1 R / count), so that p = cell 2^-31 / R everywhere downstream.
 CPD_HD uint64_t rescale_cell(uint64_t s1, uint32_t R, uint32_t count)
