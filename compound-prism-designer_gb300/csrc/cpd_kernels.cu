@@ -306,14 +306,13 @@ __device__ __noinline__ uint2 trace_df_exact_call(const DevDesign &D, const LamD
 // states (the states at the group's start plus the sums of the group's rounds up to its
 // own). The first round that stops, or that the FP32 sums cannot settle, ends the row.
 struct RoundSlot {
-    unsigned long long s1[32];  // leader lane of a bin: the round's sum of t_fixed there
-    unsigned long long q2[32];  // ... of t_q^2
-    uint32_t q1[32];            // ... of t_q
-    uint32_t hc[32];            // ... and its hits
-    uint32_t tf[32];            // each lane's t_fixed (0: no hit)
-    uint32_t df;                // ballot of the rays traced in float-float
-    uint32_t nh;                // hits of the round
-    uint32_t verdict;           // 0 go on, 1 stop, 2 unsure
+    // indexed by the leader lane of a bin the round hit: the round's sums there, in 32-bit
+    // pieces (t_fixed = q 2^11 + low, q = qh 2^10 + ql, q <= 2^20): sum q, sum low,
+    // sum qh^2, sum qh ql, sum ql^2, and the hits
+    uint32_t p[6][32];
+    uint32_t df;       // ballot of the rays traced in float-float
+    uint32_t nh;       // hits of the round
+    uint32_t verdict;  // 0 go on, 1 stop, 2 unsure
     uint32_t pad;
 };
 static_assert(sizeof(RoundSlot) % 16 == 0, "bin states follow the slots 16-byte aligned");
@@ -431,21 +430,22 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
             my.df = dfb;
             my.nh = (uint32_t)__popc(hm);
         }
-        my.tf[lane] = hit ? tf : 0u;
-        __syncwarp();
-        if (leader) {  // the bin's sums over its lanes
-            unsigned long long s1 = 0, q2 = 0;
-            uint32_t q1 = 0;
-            for (uint32_t m = grp; m; m &= m - 1u) {
-                const uint32_t t = my.tf[__ffs(m) - 1], q = t >> kTqShift;  // q <= 2^20
-                s1 += t;
-                q1 += q;
-                q2 += (unsigned long long)q * q;
+        {
+            // the bin's sums over its lanes: shared-memory adds into the leader's slot
+            my.p[0][lane] = my.p[1][lane] = my.p[2][lane] = my.p[3][lane] = my.p[4][lane] = 0u;
+            __syncwarp();
+            if (hit) {
+                const uint32_t ld = (uint32_t)__ffs(grp) - 1u, q = tf >> kTqShift;
+                const uint32_t qh = q >> 10, ql = q & 0x3ffu;
+                atomicAdd(&my.p[0][ld], q);
+                atomicAdd(&my.p[1][ld], tf & 0x7ffu);
+                atomicAdd(&my.p[2][ld], qh * qh);
+                atomicAdd(&my.p[3][ld], qh * ql);
+                atomicAdd(&my.p[4][ld], ql * ql);
             }
-            my.s1[lane] = s1;
-            my.q1[lane] = q1;
-            my.q2[lane] = q2;
-            my.hc[lane] = (uint32_t)__popc(grp);
+        }
+        if (leader) {
+            my.p[5][lane] = (uint32_t)__popc(grp);
             atomicOr(st.lanes + 2u * bin + (warp >> 2), (lane + 1u) << (8u * (warp & 3u)));
         }
         __syncthreads();
@@ -464,13 +464,16 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
             ch = st.h[bin];
 #pragma unroll
             for (uint32_t v = 0; v < kMaxAdaptWarps; v++) {
-                const uint32_t l = v <= warp ? lane_entry(w0, w1, v) : 0u;
+                if (v > warp) break;
+                const uint32_t l = lane_entry(w0, w1, v);
                 if (!l) continue;
                 const RoundSlot &o = slots[v];
-                cs1 += o.s1[l - 1u];
-                cq1 += o.q1[l - 1u];
-                cq2 += o.q2[l - 1u];
-                ch += o.hc[l - 1u];
+                const uint32_t sq = o.p[0][l - 1u];
+                cs1 += ((unsigned long long)sq << kTqShift) + o.p[1][l - 1u];
+                cq1 += sq;
+                cq2 += ((unsigned long long)o.p[2][l - 1u] << 20) + ((unsigned long long)o.p[3][l - 1u] << 11) +
+                       o.p[4][l - 1u];
+                ch += o.p[5][l - 1u];
                 cn += min(kRoundRays, R - (g0 + v * kRoundRays));
             }
             verdict = sem_quick(cn, ch, cq1, cq2, kExact ? 0u : kTqDelta);

@@ -463,22 +463,43 @@ CPD_HD int sem_test(uint64_t N, uint64_t h, uint64_t q1, uint64_t q2, uint32_t d
     return SEM_UNSURE;
 }
 
-// An FP32 screen of sem_test (same arguments, N <= 2^22): SEM_PASS or SEM_FAIL when
-// float arithmetic with error bounds settles the test, else -1 (run sem_test). With
-// A = N q2 and Q = q1^2 in float, every conversion, product and sum rounds by at most
-// 2^-24 relative, so the computed 40000 (A - Q) is within 6 2^-24 40000 (A + Q) of lhs and
-// the computed N^2 (N - 1) 2^40 within 3 2^-24 of rhs; the margins (2^-18 of the terms,
-// and of the err bound) exceed those errors and the rounding of the comparisons' own sums.
+// Integers to float with integer-unit and FP32 instructions only: below 2^23 exactly (the
+// float of exponent 23 whose mantissa is v, minus 2^23); below 2^63 in 21-bit pieces,
+// within 2^-23 relative (two roundings).
+CPD_HD float f32_small(uint32_t v)
+{
+    const uint32_t b = 0x4B000000u | v;
+    float f;
+#if defined(__CUDA_ARCH__)
+    f = __uint_as_float(b);
+#else
+    std::memcpy(&f, &b, 4);
+#endif
+    return f - 8388608.f;
+}
+CPD_HD float f32_wide(uint64_t v)
+{
+    const float a = f32_small((uint32_t)(v >> 42)), b = f32_small((uint32_t)(v >> 21) & 0x1fffffu);
+    return (a * 0x1p42f + b * 0x1p21f) + f32_small((uint32_t)v & 0x1fffffu);
+}
+
+// An FP32 screen of sem_test (same arguments, N <= 2^22, q2 < 2^63): SEM_PASS or SEM_FAIL
+// when float arithmetic with error bounds settles the test, else -1 (run sem_test). With
+// A = N q2 and Q = q1^2 in float, every product and sum rounds by at most 2^-24 relative
+// and each conversion by 2^-23, so the computed 40000 (A - Q) is within 8 2^-24 40000 (A + Q)
+// of lhs and the computed N^2 (N - 1) 2^40 within 3 2^-24 of rhs; the margins (2^-18 of the
+// terms, and of the err bound) exceed those errors and the rounding of the comparisons'
+// own sums.
 CPD_HD int sem_quick(uint32_t N, uint32_t h, uint64_t q1, uint64_t q2, uint32_t delta)
 {
-    const float n = (float)N, f1 = (float)q1, f2 = (float)q2;
+    const float n = f32_small(N), f1 = f32_wide(q1), f2 = f32_wide(q2);
     const float A = n * f2, Q = f1 * f1;
     const float L = 40000.f * (A - Q), eL = 40000.f * 0x1p-18f * (A + Q);
     const float Y = n * n * (n - 1.f) * 0x1p40f, eY = Y * 0x1p-18f;
     float E = 0.f;
     if (delta) {
-        const float d = (float)delta, hd = (float)h * d;
-        E = 40000.f * (n * (float)h * (d * (0x1p21f + d)) + hd * (2.f * f1 + hd)) * (1.f + 0x1p-18f);
+        const float d = (float)delta, hd = f32_small(h) * d;
+        E = 40000.f * (n * f32_small(h) * (d * (0x1p21f + d)) + hd * (2.f * f1 + hd)) * (1.f + 0x1p-18f);
     }
     if (L + eL + E < Y - eY) return SEM_PASS;
     if (L - eL >= Y + eY + E) return SEM_FAIL;
