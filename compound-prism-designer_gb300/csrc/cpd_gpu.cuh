@@ -119,31 +119,38 @@ struct LaunchArgs {
 
 // Most warps that trace (and decide) one wavelength's rounds at once under adaptive
 // sampling: one round per warp.
-constexpr uint32_t kMaxAdaptWarps = 8;
+constexpr uint32_t kMaxAdaptWarps = 16;
 
 // Per-bin state of one wavelength under adaptive sampling: shared memory, one array per
 // field (consecutive bins in consecutive words), carved from B-sized slices.
 struct BinStates {
+    // Within one group of rounds: byte v of lanes[b] holds 1 + the lane of round v that
+    // carries the round's sums for bin b (0: round v missed b); bit v of rounds[b] is set
+    // when round v hit b.
+    uint4 *lanes;
     unsigned long long *s1;  // sum of t_fixed over the bin's hits
     unsigned long long *q1;  // sum of t_q
     unsigned long long *q2;  // sum of t_q^2
     uint32_t *n;             // Welford samples: the sizes of the rounds that hit the bin
     uint32_t *h;             // hits
-    // Within one group of rounds: for round w of the group, byte w & 3 of word 2 b + w / 4
-    // holds 1 + the lane that carries the round's sums for bin b (0: the round missed b).
-    uint32_t *lanes;
+    uint32_t *rounds;
     __device__ BinStates(void *base, uint32_t B)
     {
-        s1 = static_cast<unsigned long long *>(base);
+        lanes = static_cast<uint4 *>(base);
+        s1 = reinterpret_cast<unsigned long long *>(lanes + B);
         q1 = s1 + B;
         q2 = q1 + B;
         n = reinterpret_cast<uint32_t *>(q2 + B);
         h = n + B;
-        lanes = h + B;
+        rounds = h + B;
     }
 };
 // Bytes of shared memory the bin states of a B-bin detector take.
-constexpr size_t bin_state_bytes(uint32_t B) { return (size_t)B * (3 * 8 + 4 * 4); }
+constexpr size_t bin_state_bytes(uint32_t B) { return (size_t)B * (16 + 3 * 8 + 3 * 4); }
+
+// Once per device, before the first pass: the adaptive kernels' shared-memory limit
+// (above the default 48 KB).
+cudaError_t configure_kernels();
 
 // Launches setup -> trace -> retrace -> entropy -> finalize on `stream` (adaptive
 // sampling: setup -> adaptive rounds -> exact rounds of the unsure rows -> entropy ->

@@ -318,12 +318,13 @@ struct RoundSlot {
 static_assert(sizeof(RoundSlot) % 16 == 0, "bin states follow the slots 16-byte aligned");
 // Dynamic shared memory of an adaptive block of KW warps over B-bin detectors.
 constexpr size_t adapt_smem_bytes(uint32_t KW, uint32_t B) { return KW * sizeof(RoundSlot) + bin_state_bytes(B); }
-static_assert(adapt_smem_bytes(kMaxAdaptWarps, CPD_MAX_BINS) <= 48u * 1024u, "default shared memory limit");
+static_assert(adapt_smem_bytes(kMaxAdaptWarps, CPD_MAX_BINS) <= 227u * 1024u, "shared memory per block");
 
 // Byte v of a bin's group lane table (v = the round within the group).
-__device__ __forceinline__ uint32_t lane_entry(uint32_t w0, uint32_t w1, uint32_t v)
+__device__ __forceinline__ uint32_t lane_entry(const uint4 &w, uint32_t v)
 {
-    return ((v < 4u ? w0 : w1) >> (8u * (v & 3u))) & 0xffu;
+    const uint32_t word = v < 8u ? (v < 4u ? w.x : w.y) : (v < 12u ? w.z : w.w);
+    return (word >> (8u * (v & 3u))) & 0xffu;
 }
 
 // One wavelength row under adaptive sampling (the stop rule of src/spectrometer/
@@ -372,13 +373,15 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
     for (uint32_t b = tid; b < B; b += nthr) {
         st.s1[b] = st.q1[b] = st.q2[b] = 0ull;
         st.n[b] = st.h[b] = 0u;
-        st.lanes[2u * b] = st.lanes[2u * b + 1u] = 0u;
+        st.lanes[b] = make_uint4(0u, 0u, 0u, 0u);
+        st.rounds[b] = 0u;
     }
     __syncthreads();
     const uint32_t *rank = a.rank + J.rank_off;
     const float2 *zt = reinterpret_cast<const float2 *>(a.z32) + J.ray_off;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    uint32_t count = 0, hits = 0, ndf = 0, flag = 0;  // the same in every thread
+    uint32_t count = 0, flag = 0;  // the same in every thread
+    uint32_t hits = 0, ndf = 0;    // thread 0
     // no ray clears the flat faces: every round runs without a hit
     const uint32_t g_start = P.band_lo >= P.band_hi ? R : 0u;
     if (g_start == R) count = R;
@@ -446,27 +449,26 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
         }
         if (leader) {
             my.p[5][lane] = (uint32_t)__popc(grp);
-            atomicOr(st.lanes + 2u * bin + (warp >> 2), (lane + 1u) << (8u * (warp & 3u)));
+            atomicOr(reinterpret_cast<uint32_t *>(st.lanes + bin) + (warp >> 2), (lane + 1u) << (8u * (warp & 3u)));
+            atomicOr(st.rounds + bin, 1u << warp);
         }
         __syncthreads();
         // 2. every round's decision at once, from the states through that round
-        uint32_t w0 = 0, w1 = 0;
+        uint4 lw = make_uint4(0u, 0u, 0u, 0u);
+        uint32_t rmask = 0u;  // leader: the group's rounds that hit its bin
         unsigned long long cs1 = 0, cq1 = 0, cq2 = 0;
         uint32_t cn = 0, ch = 0;
         int verdict = SEM_PASS;
         if (leader) {
-            w0 = st.lanes[2u * bin];
-            w1 = st.lanes[2u * bin + 1u];
+            lw = st.lanes[bin];
+            rmask = st.rounds[bin];
             cs1 = st.s1[bin];
             cq1 = st.q1[bin];
             cq2 = st.q2[bin];
             cn = st.n[bin];
             ch = st.h[bin];
-#pragma unroll
-            for (uint32_t v = 0; v < kMaxAdaptWarps; v++) {
-                if (v > warp) break;
-                const uint32_t l = lane_entry(w0, w1, v);
-                if (!l) continue;
+            for (uint32_t m = rmask & ((2u << warp) - 1u); m; m &= m - 1u) {  // rounds <= warp
+                const uint32_t v = (uint32_t)__ffs(m) - 1u, l = lane_entry(lw, v);
                 const RoundSlot &o = slots[v];
                 const uint32_t sq = o.p[0][l - 1u];
                 cs1 += ((unsigned long long)sq << kTqShift) + o.p[1][l - 1u];
@@ -485,22 +487,21 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
         if (lane == 0) my.verdict = (!hm || fail) ? 0u : (!kExact && unsure) ? 2u : 1u;
         __syncthreads();
         // 3. the first round that stops ends the row; the states through it are kept
-        // (lane v reads round v's verdict and counts)
+        // (lane v reads round v's verdict)
         const uint32_t vv = lane < KW ? slots[lane].verdict : 0u;
         const uint32_t vb = __ballot_sync(0xffffffffu, vv != 0u);
         const uint32_t last = vb ? (uint32_t)__ffs(vb) - 1u : KW - 1u;
         if (vb) flag = __shfl_sync(0xffffffffu, vv, last);
-        {
-            const uint32_t rv = g0 + lane * kRoundRays;
-            const bool in = lane <= last && rv < R;
-            count += __reduce_add_sync(0xffffffffu, in ? min(kRoundRays, R - rv) : 0u);
-            hits += __reduce_add_sync(0xffffffffu, in ? slots[lane].nh : 0u);
-            ndf += __reduce_add_sync(0xffffffffu, in ? (uint32_t)__popc(slots[lane].df) : 0u);
+        for (uint32_t v = 0; v <= last && g0 + v * kRoundRays < R; v++) {
+            count += min(kRoundRays, R - (g0 + v * kRoundRays));
+            if (tid == 0) {  // the row's totals, published by thread 0
+                hits += slots[v].nh;
+                ndf += (uint32_t)__popc(slots[v].df);
+            }
         }
         if (leader) {
-            uint32_t later = 0, earlier = 0;
-            for (uint32_t v = warp + 1u; v <= last; v++) later |= lane_entry(w0, w1, v);
-            for (uint32_t v = 0; v < warp; v++) earlier |= lane_entry(w0, w1, v);
+            const uint32_t later = rmask & ((2u << last) - 1u) & ~((2u << warp) - 1u);
+            const uint32_t earlier = rmask & ((1u << warp) - 1u);
             if (warp <= last && !later) {  // the bin's latest round through `last`
                 st.s1[bin] = cs1;
                 st.q1[bin] = cq1;
@@ -509,8 +510,8 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
                 st.h[bin] = ch;
             }
             if (!earlier) {  // the bin's first round of the group clears its lane table
-                st.lanes[2u * bin] = 0u;
-                st.lanes[2u * bin + 1u] = 0u;
+                st.lanes[bin] = make_uint4(0u, 0u, 0u, 0u);
+                st.rounds[bin] = 0u;
             }
         }
         if (!flag && g0 + KW * kRoundRays >= R) flag = 1u;  // out of rays
@@ -546,7 +547,7 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
 #define CPD_ADAPT_KW_SOME 4  // warps per row at 2 to 7 rows per SM
 #endif
 #ifndef CPD_ADAPT_MIN_BLOCKS
-#define CPD_ADAPT_MIN_BLOCKS 4  // 64 registers at kMaxAdaptWarps warps per block
+#define CPD_ADAPT_MIN_BLOCKS 2  // 64 registers at kMaxAdaptWarps warps per block
 #endif
 // One row per block of KW = blockDim.x / 32 warps: rows differ widely in length (a single
 // round to all R / 32), and one row per block lets the block scheduler balance them.
@@ -1122,6 +1123,16 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     }
     if (ev) cudaEventRecord(ev[4], stream);
     return launches;
+}
+
+cudaError_t configure_kernels()
+{
+    const int bytes = (int)adapt_smem_bytes(kMaxAdaptWarps, CPD_MAX_BINS);
+    cudaError_t e = cudaFuncSetAttribute(adaptive_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(adaptive_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)adapt_smem_bytes(1u, CPD_MAX_BINS));
+    return e;
 }
 
 uint64_t trace_resident_warps(int num_sms, uint32_t warps_per_cta)

@@ -891,7 +891,7 @@ int cpd_context_create(int device, cpd_context **out)
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     std::vector<float> tab(4 * ff::kLogTable);
     ff::make_log_table(tab.data());
-    if (ctx->main.create() != cudaSuccess || ctx->logtab.ensure(sizeof(float) * tab.size()) != cudaSuccess ||
+    if (configure_kernels() != cudaSuccess || ctx->main.create() != cudaSuccess || ctx->logtab.ensure(sizeof(float) * tab.size()) != cudaSuccess ||
         cudaMemcpy(ctx->logtab.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
         ctx->main.destroy();
         ctx->logtab.release();
