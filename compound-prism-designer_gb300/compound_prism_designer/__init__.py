@@ -63,6 +63,18 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def _seed_array(seeds):
+    """A few seeds as a ctypes double array (the per-call path: a numpy pointer costs
+    several microseconds, a small ctypes array well under one)."""
+    if isinstance(seeds, np.ndarray):
+        vals = seeds.ravel().tolist()
+    elif isinstance(seeds, (float, int)):
+        vals = [seeds]
+    else:
+        vals = np.asarray(seeds, dtype=np.float64).ravel().tolist()
+    return (C.c_double * len(vals))(*vals), len(vals)
+
+
 class Glass:
     """Glass(name, coefficents): the 6-coefficient Horner dispersion polynomial
     (src/pylib.rs:37-95, src/spectrometer/glasscat.rs:7-22)."""
@@ -468,15 +480,15 @@ class Spectrometer:
 
     def gpu_fitness_full(self, seeds, *, max_n: int = 256, nwarp: int = 2, max_eval: int = 16_384,
                          adaptive: bool = False, context: Optional[Context] = None) -> N.Fitness:
-        seeds = np.ascontiguousarray(np.atleast_1d(seeds), dtype=np.float64)
+        sarr, ns = _seed_array(seeds)
         ctx = context or default_context()
         f = N.Fitness()
         if adaptive:
-            _check(N.lib.cpd_fitness_gpu_ex(ctx.handle, C.byref(self.design), _dp(seeds), seeds.size, int(max_n),
+            _check(N.lib.cpd_fitness_gpu_ex(ctx.handle, C.byref(self.design), sarr, ns, int(max_n),
                                             int(nwarp), int(max_eval), N.SAMPLING_ADAPTIVE, C.byref(f)),
                    "gpu_fitness")
         else:
-            _check(N.lib.cpd_fitness_gpu(ctx.handle, C.byref(self.design), _dp(seeds), seeds.size, int(max_n),
+            _check(N.lib.cpd_fitness_gpu(ctx.handle, C.byref(self.design), sarr, ns, int(max_n),
                                          int(nwarp), int(max_eval), C.byref(f)), "gpu_fitness")
         return f
 
