@@ -336,6 +336,35 @@ def run_batch_only(args):
                       "ms": ms, "shape": [rt, wp]}), flush=True)
 
 
+def run_adaptive_only(args):
+    """--adaptive-only N: the adaptive form's batched pass (adaptive sampling, 128
+    wavelengths x up to 8192 rays) on N generation-0 designs, for profiler captures;
+    prints one JSON line of device times."""
+    import numpy as np
+    import compound_prism_designer as cpd
+    from compound_prism_designer import generations as gen
+
+    rng = np.random.default_rng(11)
+    cat = gen.glass_catalog(rng, 64)
+    pop = gen.initial_population(rng, args.adaptive_only, cat)
+    designs, ok = gen.build(pop, cat)
+    specs = []
+    for i in range(len(designs)):
+        sp = cpd.Spectrometer.__new__(cpd.Spectrometer)
+        sp._design = cpd._native.Design.from_buffer_copy(designs[i].tobytes())
+        specs.append(sp)
+    ctx = cpd.Context(0)
+    mode = cpd.TRACE_HYBRID | cpd.SAMPLING_ADAPTIVE
+    for _ in range(args.warmup):
+        cpd.fitness_batch(specs, seeds=0.5, max_n=128, max_eval=8192, mode=mode, context=ctx)
+    ms, rays = [], 0
+    for _ in range(args.steps):
+        outs = cpd.fitness_batch(specs, seeds=0.5, max_n=128, max_eval=8192, mode=mode, context=ctx)
+        ms.append(ctx.last_timing()[0])
+        rays = sum(o.rays for o in outs)
+    print(json.dumps({"form": "adaptive batch", "designs": len(specs), "rays": int(rays), "ms": ms}), flush=True)
+
+
 def run_reference(args, dist):
     """--impl reference: the reference CPU algorithm (oracle port) on the same workload."""
     if dist.rank != 0:
@@ -400,6 +429,8 @@ def main():
                     help="fixed launch shape RAY_TILE,WARPS instead of the autotuner (for profiler runs)")
     ap.add_argument("--batch-only", type=int, default=0, metavar="N",
                     help="profiler run: only the batched form, on the first N designs of its population")
+    ap.add_argument("--adaptive-only", type=int, default=0, metavar="N",
+                    help="profiler run: only the adaptive form's batched pass, on N designs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = Dist()
@@ -412,6 +443,9 @@ def main():
 
     if args.batch_only:
         run_batch_only(args)
+        return
+    if args.adaptive_only:
+        run_adaptive_only(args)
         return
     ctx = cpd.Context(dist.local)
     if args.shape:
