@@ -107,8 +107,8 @@ struct PassSlot {
     cudaEvent_t kev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     // inputs (tables, designs, jobs) in one arena, uploaded with one copy; results
     // (DesignOut[n] then HostStatus) written by the kernels into mapped host memory;
-    // `outs` holds the device-side Control words
-    DevBuf in, lp, lx, hist, S1, S2, acc, outs, queue, pout;
+    // `in` ends with the device-side Control words
+    DevBuf in, lp, lx, hist, S1, S2, acc, queue, pout;
     HostBuf h_in, h_outs;
     size_t ctl_off = 0;
     bool hist_dirty = true;
@@ -147,7 +147,7 @@ struct PassSlot {
         if (stream) cudaStreamSynchronize(stream);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
-        for (DevBuf *b : {&in, &lp, &lx, &hist, &S1, &S2, &acc, &outs, &queue, &pout}) b->release();
+        for (DevBuf *b : {&in, &lp, &lx, &hist, &S1, &S2, &acc, &queue, &pout}) b->release();
         for (HostBuf *b : {&h_in, &h_outs}) b->release();
         for (cudaEvent_t *ev : {&ev0, &ev1, &done, &kev[0], &kev[1], &kev[2], &kev[3], &kev[4]})
             if (*ev) cudaEventDestroy(*ev), *ev = nullptr;
@@ -342,7 +342,10 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     const size_t o_des = o_rank + al(sizeof(uint32_t) * rnk);
     const size_t o_job = o_des + al(sizeof(DevDesign) * n);
     const size_t o_par = o_job + al(sizeof(DesignJob) * n);  // parameter records (device builds)
-    const size_t in_bytes = o_par + (on_device ? al(sizeof(cpd_spectrometer_params) * n) : 0);
+    // the pass's Control words close the arena: uploaded as zeros with the inputs (one copy
+    // node instead of a copy and a memset ahead of the first kernel)
+    const size_t o_ctl = o_par + (on_device ? al(sizeof(cpd_spectrometer_params) * n) : 0);
+    const size_t in_bytes = o_ctl + sizeof(Control);
     const size_t ctl_off = al(sizeof(DesignOut) * n);
     const size_t out_bytes = ctl_off + sizeof(HostStatus);
     CPD_TRY(S.h_in.ensure(in_bytes));
@@ -356,6 +359,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     // a device build writes the design records itself: they are not uploaded
     const size_t up_off = resident ? (on_device ? o_job : o_des) : 0, up_bytes = in_bytes - up_off;
     char *hin = S.h_in.as<char>();
+    std::memset(hin + o_ctl, 0, sizeof(Control));
     for (uint32_t i = 0; i < n; i++) {
         if (on_device) reinterpret_cast<cpd_spectrometer_params *>(hin + o_par)[i] = *ds[i].params;
         else reinterpret_cast<DevDesign *>(hin + o_des)[i] = *ds[i].dev;
@@ -394,7 +398,6 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     CPD_TRY(S.S1.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
     CPD_TRY(S.S2.ensure(sizeof(unsigned long long) * std::max<uint64_t>(accc, 1)));
     CPD_TRY(S.acc.ensure(sizeof(DesignAcc) * n));
-    CPD_TRY(S.outs.ensure(sizeof(Control)));
     CPD_TRY(S.queue.ensure(sizeof(QEntry) * S.qcap));
     if (p_out_host) CPD_TRY(S.pout.ensure(hist_bytes));
     S.ctl_off = ctl_off;
@@ -430,7 +433,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     a.acc = S.acc.as<DesignAcc>();
     a.out = reinterpret_cast<DesignOut *>(S.h_outs.dev);
     a.status = reinterpret_cast<HostStatus *>(reinterpret_cast<char *>(S.h_outs.dev) + ctl_off);
-    a.ctl = S.outs.as<Control>();
+    a.ctl = reinterpret_cast<Control *>(din + o_ctl);
     a.clear_acc = fresh ? 1u : 0u;
     a.acc_cells = accc;
     a.queue = S.queue.as<QEntry>();
@@ -461,10 +464,10 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     std::memcpy(key.data() + sizeof(a), extra, sizeof(extra));
     auto record = [&](cudaStream_t st, bool capturing) -> int {
         const unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-        cudaMemcpyAsync(S.in.as<char>() + up_off, S.h_in.as<char>() + up_off, up_bytes, cudaMemcpyHostToDevice, st);
         // the per-design accumulators are cleared by the setup kernel (clear_acc), the
-        // results arrive in mapped host memory: one copy and one memset around the kernels
-        cudaMemsetAsync(a.ctl, 0, sizeof(Control), st);
+        // Control words arrive zeroed with the inputs, and the results are written into
+        // mapped host memory: one copy ahead of the kernels
+        cudaMemcpyAsync(S.in.as<char>() + up_off, S.h_in.as<char>() + up_off, up_bytes, cudaMemcpyHostToDevice, st);
         // External: under stream capture these become event-record nodes of the graph
         cudaEventRecordWithFlags(S.ev0, st, evf);
         const int l = launch_pass(a, ctx->num_sms, ctx->warps_per_cta, st, profile ? S.kev : nullptr, true);
