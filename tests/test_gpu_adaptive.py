@@ -126,3 +126,14 @@ def test_adaptive_rejects_other_trace_modes(designs):
                  cpd.TRACE_HYBRID | cpd.SAMPLING_EXACT):
         with pytest.raises(ValueError):
             s.gpu_fitness_points(lam_u, ray_u, mode=mode)
+
+
+@pytest.mark.parametrize("W", [1, 33, 500, 2000])
+def test_adaptive_ragged_sizes(designs, W):
+    """Rounds past the last ray, a single partial round, and every width of the round groups
+    (16 warps per row for a few rows, 4 at 2-7 rows per SM, 2 when rows fill the GPU)."""
+    for R in (1, 31, 33, 1000):
+        lam_u = O.qrng_points(0.5, W)
+        ray_u = O.qrng_points(0.25, R)
+        for name, s, d in designs[:3]:
+            _check(s, d, lam_u, ray_u)
