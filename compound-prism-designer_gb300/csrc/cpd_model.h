@@ -526,7 +526,16 @@ CPD_HD void split_f32(double v, float &hi, float &lo)
 
 // ----------------------------------------------------------------- FP32 fast path
 
-CPD_HD float fabs_f(float a) { return a < 0.f ? -a : a; }
+// |a|: an operand modifier of the consuming instruction on the device. It differs from
+// (a < 0 ? -a : a) only in the sign of -0 and of NaN, which no comparison or sum below sees.
+CPD_HD float fabs_f(float a)
+{
+#if defined(__CUDA_ARCH__)
+    return fabsf(a);
+#else
+    return std::fabs(a);
+#endif
+}
 
 CPD_HD float sqrt_fast(float a)
 {
