@@ -180,24 +180,30 @@ def batched_population(n=1024, seed=20261205):
     return [s for s, _ in pop], W, rej
 
 
-def cpu_oracle_rate(d, W, R, target_s=10.0, nthreads=None):
+def cpu_oracle_rate(d, W, R, target_s=10.0, nthreads=None, gpu_info=None):
     """Oracle (reference CPU algorithm) on all host threads: designs/s extrapolated from
-    a bounded sample of the design's wavelengths (all R rays each)."""
+    a bounded sample of whole designs, on the points of the plain GPU call (seed 0.5, the
+    GPU policy). The oracle's MI on those points is the check of the GPU's (gpu_info)."""
     import oracle as O
+    from compound_prism_designer import precision as P
 
     nthreads = nthreads or os.cpu_count() or 1
-    ray_u = O.qrng_points(0.5, R)
-    lam_all = O.qrng_points(0.5, W)
+    lam_all = P.synth_points(0.5, W)
+    ray_u = P.synth_points(0.5, R, first=1)
     # whole designs until target_s of CPU time has elapsed (at least one)
     done, t0 = 0, time.perf_counter()
     while done == 0 or time.perf_counter() - t0 < target_s:
-        O.fitness_points(d, lam_all, ray_u, nthreads=nthreads, want_p=False)
+        _, st = O.fitness_points(d, lam_all, ray_u, nthreads=nthreads, want_p=False)
         done += W
     dt = time.perf_counter() - t0
     rate = done / (W * dt)
-    return {"value": rate, "unit": "designs/s", "cores": nthreads, "kind": "port",
-            "sample": f"{done} wavelength rows ({done / W:.2f} designs) x {R} rays of the benchmark design "
-                      f"({done * R} rays, {dt:.1f} s, {nthreads} threads)"}
+    out = {"value": rate, "unit": "designs/s", "cores": nthreads, "kind": "port",
+           "sample": f"{done} wavelength rows ({done / W:.2f} designs) x {R} rays of the benchmark design "
+                     f"({done * R} rays, {dt:.1f} s, {nthreads} threads)"}
+    if gpu_info is not None:
+        out["mi_check"] = {"gpu_mi": gpu_info, "oracle_mi": st["info"],
+                           "rel_err": abs(gpu_info - st["info"]) / abs(st["info"]), "tolerance": 1e-4}
+    return out
 
 
 def adaptive_form(ctx, n=256):
@@ -546,7 +552,7 @@ def main():
         except Exception as e:  # noqa: BLE001
             extras.setdefault("forms", {})["adaptive"] = {"error": repr(e)}
         try:
-            extras["cpu_baseline"] = cpu_oracle_rate(d, W_PLAIN, R_PLAIN)
+            extras["cpu_baseline"] = cpu_oracle_rate(d, W_PLAIN, R_PLAIN, gpu_info=f.info)
         except Exception as e:  # noqa: BLE001
             extras["cpu_baseline"] = {"error": repr(e)}
 
