@@ -400,7 +400,7 @@ CPD_HD int trace(const DevDesign &D, double lambda, double y, uint32_t &bin, dou
 // Guard widths of the fast path. A decision whose FP32 margin is inside its guard
 // is not trusted: the ray is re-traced with the exact model. The widths are
 // upper bounds on the FP32 error of each margin measured over random designs,
-// times a safety factor ("guard bands").
+// times a safety factor.
 struct Guards {
     float pos;      // mm, detector coordinate vs 0, L and every bin edge
     float cosine;   // exit-face cr^2, AR threshold 0.5, detector min_ci

@@ -3,7 +3,7 @@
  *
  * A plain-C, double-precision restatement of the compound-prism spectrometer
  * fitness path of jdtatz/compound-prism-designer (Rust crate `src/`). It is the
- * parity checker for the CUDA implementation and the timed CPU baseline. Only
+ * parity reference of the CUDA implementation's tests and the timed CPU baseline. Only
  * tests, the smoke check and the benchmark's CPU-baseline / reference legs may
  * load it; the product library never links or calls it.
  *

@@ -19,7 +19,7 @@ from compound_prism_designer import synth
 
 
 @pytest.fixture(scope="module")
-def checker(tmp_path_factory):
+def fastpath_bin(tmp_path_factory):
     out = tmp_path_factory.mktemp("fastpath") / "fastpath_check"
     csrc = os.path.join(PKG_DIR, "csrc")
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-I", csrc, "-I",
@@ -28,34 +28,34 @@ def checker(tmp_path_factory):
     return out
 
 
-def _run(checker, tmp_path, spec, lam_u, ray_u):
+def _run(fastpath_bin, tmp_path, spec, lam_u, ray_u):
     dp, lp, rp = tmp_path / "d.bin", tmp_path / "l.bin", tmp_path / "r.bin"
     dp.write_bytes(bytes(spec.design))
     np.asarray(lam_u, dtype=np.float64).tofile(lp)
     np.asarray(ray_u, dtype=np.float64).tofile(rp)
-    out = subprocess.run([str(checker), str(dp), str(len(lam_u)), str(len(ray_u)), str(lp), str(rp)],
+    out = subprocess.run([str(fastpath_bin), str(dp), str(len(lam_u)), str(len(ray_u)), str(lp), str(rp)],
                          capture_output=True, text=True, check=True).stdout.split()
     return dict(zip(out[0::2], map(int, out[1::2])))
 
 
-def test_far_reference_ray_design(checker, tmp_path):
+def test_far_reference_ray_design(fastpath_bin, tmp_path):
     case = json.load(open(os.path.join(GOLDEN, "regression_designs.json")))["far_reference_detector"]
     spec = synth.spectrometer_from_dict(case["design"])
     pts = case["points"]
     lam_u = P.synth_points(pts["lam_seed"], pts["wavelengths"])[case["bad_rows"]]
     ray_u = P.synth_points(pts["ray_seed"], pts["rays"], first=pts["ray_first"])
-    r = _run(checker, tmp_path, spec, lam_u, ray_u)
+    r = _run(fastpath_bin, tmp_path, spec, lam_u, ray_u)
     assert r["rays"] == len(lam_u) * len(ray_u)
     assert r["mismatches"] == 0 and r["outside_band_hits"] == 0 and r["df_mismatches"] == 0, r
 
 
-def test_random_designs(checker, tmp_path):
+def test_random_designs(fastpath_bin, tmp_path):
     rng = np.random.default_rng(8)
     lam_u = P.synth_points(0.3, 256)
     ray_u = P.synth_points(0.3, 1024, first=1)
     for G, B in [(2, 16), (3, 32), (4, 64), (5, 128), (6, 64), (6, 128)]:
         spec, _, _ = synth.random_design(rng, G, B)
-        r = _run(checker, tmp_path, spec, lam_u, ray_u)
+        r = _run(fastpath_bin, tmp_path, spec, lam_u, ray_u)
         assert r["mismatches"] == 0 and r["outside_band_hits"] == 0 and r["df_mismatches"] == 0, (G, B, r)
         assert r["flagged"] < 0.01 * r["rays"], (G, B, r)
         # adaptive sampling's decision guard (kTqDelta = 2 quanta of 2^-20) assumes the

@@ -1,6 +1,6 @@
 """GPU parity: the CUDA fitness path against the C oracle on identical points.
 
-Tolerances (the benchmark spec):
+Tolerances (the parity bar of this path):
 * hit-bin index: exactly equal for every ray (the hybrid trace re-traces every ray
   inside a guard band of any decision in float-float, ~2^-46 relative, which decides
   like the f64 oracle except within ~1e-11 mm of a threshold);

@@ -2,7 +2,7 @@
 all-FP64 trace, and the FP64 trace against the CPU oracle, on near-critical designs
 (exit-face incidence within 2 degrees of total internal reflection) and ordinary ones.
 
-Bounds (the benchmark spec): the hybrid trace must agree with FP64 exactly on hit
+Bounds (the parity bar of this path): the hybrid trace must agree with FP64 exactly on hit
 bins, within 1e-6 absolute on p(d|lambda) and within 1e-4 relative on MI. The
 FP64 trace must agree with the oracle within the 2^-32 fixed-point quantum on p and
 1e-8 relative on MI. FP32-only has no bound; its errors are the study's output and
