@@ -626,7 +626,19 @@ __device__ void finalize_design(const LaunchArgs &a, uint32_t d, const DesignJob
 {
     using ff::F2;
     const uint32_t lane = tid & 31u;
+    // every load first, so that their L2 round trips overlap one another and the
+    // float-float prologue: the design's sums, its ray counters and this thread's first bin
     const unsigned long long rows = __ldcg(&a.acc[d].rows) + J.W;
+    const unsigned long long Hsum = __ldcg(&a.acc[d].H);
+    const bool cp = lane < (uint32_t)kSpread;
+    const unsigned long long hits_l = cp ? __ldcg(&a.acc[d].hits[lane]) : 0ull;
+    const unsigned long long retraced_l = cp ? __ldcg(&a.acc[d].retraced[lane]) : 0ull;
+    const unsigned long long fast_l = cp ? __ldcg(&a.acc[d].fast[lane]) : 0ull;
+    unsigned long long c1n = 0ull, c2n = 0ull;
+    if (tid < J.B) {
+        c1n = __ldcg(&a.S1[J.acc_off + tid]);
+        c2n = __ldcg(&a.S2[J.acc_off + tid]);
+    }
     const F2 n = ff::from_u64(rows);
     const F2 inv_n = df::rcp(n);
     const F2 unit{J.unit_hi, J.unit_lo};  // p per count unit, 2^-31 / R
@@ -639,7 +651,11 @@ __device__ void finalize_design(const LaunchArgs &a, uint32_t d, const DesignJob
     float m2max = 0.f;
     int conv = 1;
     for (uint32_t b = tid; b < J.B; b += nthr) {
-        const unsigned long long c1 = __ldcg(&a.S1[J.acc_off + b]);
+        const unsigned long long c1 = c1n, c2 = c2n;
+        if (b + nthr < J.B) {  // the next bin's sums
+            c1n = __ldcg(&a.S1[J.acc_off + b + nthr]);
+            c2n = __ldcg(&a.S2[J.acc_off + b + nthr]);
+        }
         const F2 sc1 = ff::from_u64(c1);
         if (c1) {
             const F2 pbar = ff::mul(sc1, inv_nr);
@@ -649,7 +665,7 @@ __device__ void finalize_design(const LaunchArgs &a, uint32_t d, const DesignJob
         }
         // Welford M2 of the per-wavelength p(d|lambda) (welford.rs:26-57)
         const F2 s1 = ff::mul(sc1, unit);  // sum over rows of p
-        const F2 s2 = ff::mul(ff::from_u64(__ldcg(&a.S2[J.acc_off + b])), s2unit);
+        const F2 s2 = ff::mul(ff::from_u64(c2), s2unit);
         F2 m2 = df::sub(s2, ff::mul(ff::mul(s1, s1), inv_n));
         if (df::neg_(m2)) m2 = F2{0.f, 0.f};
         conv &= df::lt(m2, thr) ? 1 : 0;
@@ -676,12 +692,11 @@ __device__ void finalize_design(const LaunchArgs &a, uint32_t d, const DesignJob
         m2max = r.m2max;
         conv = __all_sync(0xffffffffu, r.conv);
     }
-    const bool cp = lane < (uint32_t)kSpread;
-    const unsigned long long hits = warp_sum_u64(cp ? __ldcg(&a.acc[d].hits[lane]) : 0ull);
-    const unsigned long long retraced = warp_sum_u64(cp ? __ldcg(&a.acc[d].retraced[lane]) : 0ull);
-    const unsigned long long fast = warp_sum_u64(cp ? __ldcg(&a.acc[d].fast[lane]) : 0ull);
+    const unsigned long long hits = warp_sum_u64(hits_l);
+    const unsigned long long retraced = warp_sum_u64(retraced_l);
+    const unsigned long long fast = warp_sum_u64(fast_l);
     if (lane == 0) {
-        const F2 H = ff::mul(ff::from_u64(__ldcg(&a.acc[d].H)), F2{(float)kHScaleInv, 0.f});
+        const F2 H = ff::mul(ff::from_u64(Hsum), F2{(float)kHScaleInv, 0.f});
         const F2 hc = ff::mul(H, inv_n);
         const double h_cond = -((double)hc.hi + (double)hc.lo);
         const double h_det = (double)hdet * (1.0 / 1125899906842624.0);
