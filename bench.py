@@ -538,6 +538,7 @@ def main():
                 "workload": f"{nb} designs, G in 2..6, B in 16..128, W in 512..4096, R={R_PLAIN}",
                 "designs_per_s_device": nb / (min(bdev) / 1e3), "designs_per_s_e2e": nb / min(bt),
                 "ms_device": min(bdev), "ms_e2e": 1e3 * min(bt), "rays": int(sum(int(w) for w in Ws) * R_PLAIN),
+                "rays_per_s_device": sum(int(w) for w in Ws) * R_PLAIN / (min(bdev) / 1e3),
                 "speedup_vs_plain_e2e": (nb / min(bt)) / e2e,
                 "autotuned_shape": {"ray_tile": tuned[0], "warps_per_cta": tuned[1], "best_ms": tuned[2],
                                     "tuning_s": t_tune}}}
@@ -569,6 +570,7 @@ def main():
                     "ms_per_step": 1e3 * wall_s / args.steps},
             "gpu_launches": launches_total, "clocks": clk, "wall_s": t_total,
             "mi": f.info, "retraced_per_step": f.retraced,
+            "rays_per_s": value * W_PLAIN * R_PLAIN, "rays_per_s_e2e": e2e * W_PLAIN * R_PLAIN,
         }
         line.update(extras)
         print(json.dumps(line), flush=True)
