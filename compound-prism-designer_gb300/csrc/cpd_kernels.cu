@@ -559,8 +559,10 @@ __global__ void __launch_bounds__(32 * kMaxAdaptWarps, CPD_ADAPT_MIN_BLOCKS) ada
     adaptive_row<false>(a, blockIdx.x, adapt_smem, blockDim.x >> 5, threadIdx.x >> 5, threadIdx.x & 31u);
 }
 
-// The queued rows: the float-float path from the first round on, one warp per block.
-__global__ void __launch_bounds__(32) adaptive_exact_kernel(const LaunchArgs a)
+// The queued rows: the float-float path from the first round on, one row per block of
+// blockDim.x / 32 warps (as many as the rounds kernel used: a queued row of a plain call
+// is on the pass's critical path).
+__global__ void __launch_bounds__(32 * kMaxAdaptWarps, 1) adaptive_exact_kernel(const LaunchArgs a)
 {
     extern __shared__ __align__(16) unsigned long long adapt_smem[];
     cudaTriggerProgrammaticLaunchCompletion();
@@ -570,7 +572,8 @@ __global__ void __launch_bounds__(32) adaptive_exact_kernel(const LaunchArgs a)
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
     for (uint64_t i = blockIdx.x; i < n; i += gridDim.x) {
         const QEntry e = a.queue[i];
-        adaptive_row<true>(a, a.jobs[e.design].row_off + e.k, adapt_smem, 1u, 0u, threadIdx.x);
+        adaptive_row<true>(a, a.jobs[e.design].row_off + e.k, adapt_smem, blockDim.x >> 5, threadIdx.x >> 5,
+                           threadIdx.x & 31u);
     }
 }
 
@@ -1089,7 +1092,9 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
             launches++;
         }
         if (ev) cudaEventRecord(ev[2], stream);
-        launch_k(adaptive_exact_kernel, (unsigned)(num_sms * 8), 32, adapt_smem_bytes(1u, maxB), stream, pdl, a);
+        const uint32_t kwe = a.total_rows / (uint64_t)num_sms >= 8 ? 1u : kMaxAdaptWarps;
+        launch_k(adaptive_exact_kernel, (unsigned)(num_sms * (kwe == 1u ? 8 : 1)), 32 * kwe, adapt_smem_bytes(kwe, maxB),
+                 stream, pdl, a);
         launches++;
     } else {
     if (ev) cudaEventRecord(ev[1], stream);
@@ -1145,8 +1150,7 @@ cudaError_t configure_kernels()
     const int bytes = (int)adapt_smem_bytes(kMaxAdaptWarps, CPD_MAX_BINS);
     cudaError_t e = cudaFuncSetAttribute(adaptive_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(adaptive_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)adapt_smem_bytes(1u, CPD_MAX_BINS));
+        e = cudaFuncSetAttribute(adaptive_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
 }
 
