@@ -346,7 +346,7 @@ __device__ __forceinline__ uint32_t lane_entry(const uint4 &w, uint32_t v)
 // stop decision the FP32 transmittances cannot settle (sem_test: SEM_UNSURE) is queued
 // for the exact path and leaves nothing behind.
 template <bool kExact>
-__device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long long *smem, uint32_t KW,
+__device__ bool adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long long *smem, uint32_t KW,
                              uint32_t warp, uint32_t lane)
 {
     const uint32_t d = find_job<F_ROW>(a.jobs, a.njobs, row);
@@ -362,7 +362,7 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
             if (pos < a.qcap) a.queue[pos] = QEntry{d, k, 0u, 0u};
             else atomicOr(&a.ctl->overflow, 1u);
         }
-        return;
+        return false;
     }
     RoundSlot *slots = reinterpret_cast<RoundSlot *>(smem);
     RoundSlot &my = slots[warp];
@@ -415,8 +415,7 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
                     }
                 }
                 if (res == RAY_FLAG) {
-                    const uint2 r = kExact ? trace_df_exact_packed(D, E, z.x, z.y)
-                                           : trace_df_exact_call(D, E, z.x, z.y);
+                    const uint2 r = trace_df_exact_call(D, E, z.x, z.y);
                     bin = r.x;
                     tf = r.y;
                     used_df = true;
@@ -519,11 +518,9 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
         if (flag) break;
     }
     if (flag == 2u) {
-        if (tid == 0) {
-            const unsigned long long pos = atomicAdd(&a.ctl->queue_count, 1ull);
-            if (pos < a.qcap) a.queue[pos] = QEntry{d, k, 0u, 0u};
-            else atomicOr(&a.ctl->overflow, 1u);
-        }
+        // the caller redoes the row on the exact path at once
+        __syncthreads();
+        return true;
     } else {
         unsigned long long *hrow = a.hist + J.hist_off + (uint64_t)k * B;
         for (uint32_t b = tid; b < B; b += nthr) {
@@ -538,6 +535,7 @@ __device__ void adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
         }
     }
     __syncthreads();  // the slots and bin states are reused by the block's next row
+    return false;
 }
 
 #ifndef CPD_ADAPT_KW_MANY
@@ -556,7 +554,11 @@ __global__ void __launch_bounds__(32 * kMaxAdaptWarps, CPD_ADAPT_MIN_BLOCKS) ada
     extern __shared__ __align__(16) unsigned long long adapt_smem[];
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();  // the setup's LamParams and LamDF
-    adaptive_row<false>(a, blockIdx.x, adapt_smem, blockDim.x >> 5, threadIdx.x >> 5, threadIdx.x & 31u);
+    const uint32_t kw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    // a row whose stop decision the FP32 transmittances cannot settle is redone here, on
+    // the float-float path from its first round, while other blocks go on with theirs
+    if (adaptive_row<false>(a, blockIdx.x, adapt_smem, kw, warp, lane))
+        adaptive_row<true>(a, blockIdx.x, adapt_smem, kw, warp, lane);
 }
 
 // The queued rows: the float-float path from the first round on, one row per block of
