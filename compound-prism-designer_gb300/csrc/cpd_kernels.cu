@@ -343,8 +343,9 @@ __device__ __forceinline__ uint32_t lane_entry(const uint4 &w, uint32_t v)
 // by the leader of each bin's latest round. Everything is integer, so the result equals
 // the one-round-at-a-time order bit for bit.
 // kExact: every ray by the float-float trace and the exact test. Otherwise a row whose
-// stop decision the FP32 transmittances cannot settle (sem_test: SEM_UNSURE) is queued
-// for the exact path and leaves nothing behind.
+// stop decision the FP32 transmittances cannot settle (sem_test: SEM_UNSURE) leaves
+// nothing behind and returns true: the caller redoes it on the exact path. (In the
+// verification mode every row is queued for adaptive_exact_kernel instead.)
 template <bool kExact>
 __device__ bool adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long long *smem, uint32_t KW,
                              uint32_t warp, uint32_t lane)
