@@ -520,15 +520,22 @@ class Spectrometer:
                                     fl.ctypes.data_as(C.POINTER(C.c_uint8))), "trace_rays")
         return bins, ts, fl.astype(bool)
 
-    def transmission_probability(self, wavelengths, *, max_m: int = 16_384,
-                                 context: Optional[Context] = None) -> np.ndarray:
-        """p(d|lambda) for each given wavelength (src/pylib.rs:1028-1058), max_m rays each."""
+    def transmission_probability(self, wavelengths, *, max_m: int = 16_384, fixed_n: bool = False,
+                                 return_rays: bool = False, context: Optional[Context] = None):
+        """p(d|lambda) for each given wavelength, shape (len(wavelengths), bin_count)
+        (src/pylib.rs:1028-1058): the reference's estimator, p_dets_l_wavelength
+        (src/fitness.rs:5-69), which stops a wavelength at the first hit whose bin's SEM is
+        <= 5e-3 (at most max_m rays). fixed_n=True traces all max_m rays instead.
+        return_rays=True also returns the rays each wavelength consumed."""
         w = np.ascontiguousarray(wavelengths, dtype=np.float64).reshape(-1)
         ctx = context or default_context()
         out = np.zeros((w.size, self.detector_array.bin_count))
-        _check(N.lib.cpd_transmission_probability(ctx.handle, C.byref(self.design), _dp(w), w.size, int(max_m),
-                                                  _dp(out)), "transmission_probability")
-        return out
+        rays = np.zeros(w.size, dtype=np.uint32)
+        _check(N.lib.cpd_transmission_probability_ex(ctx.handle, C.byref(self.design), _dp(w), w.size, int(max_m),
+                                                     N.TP_FIXED_N if fixed_n else 0, _dp(out),
+                                                     rays.ctypes.data_as(C.POINTER(C.c_uint32))),
+               "transmission_probability")
+        return (out, rays) if return_rays else out
 
     def ray_trace(self, wavelength: float, inital_y: float) -> np.ndarray:
         """Propagation path rows (x, y, ux, uy) (src/pylib.rs:1060-1083)."""

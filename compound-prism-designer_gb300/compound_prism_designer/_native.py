@@ -37,6 +37,7 @@ TRACE_FP32 = 1
 TRACE_FP64 = 2
 SAMPLING_ADAPTIVE = 0x10  # OR-ed into a trace mode: the per-wavelength SEM stop
 SAMPLING_EXACT = 0x20     # with SAMPLING_ADAPTIVE: every wavelength on the exact path
+TP_FIXED_N = 0x1          # cpd_transmission_probability_ex: all max_m rays per wavelength
 
 
 class SpectrometerParams(C.Structure):
@@ -146,6 +147,8 @@ SIGNATURES = [
     ("cpd_fitness_gpu_points_static", C.c_int, [C.POINTER(Design), _dp, C.c_uint32, _dp, C.c_uint32, C.c_uint32,
                                                 C.POINTER(Fitness), _dp]),
     ("cpd_transmission_probability", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, C.c_uint32, _dp]),
+    ("cpd_transmission_probability_ex", C.c_int, [_ctxp, C.POINTER(Design), _dp, C.c_uint32, C.c_uint32,
+                                                  C.c_uint32, _dp, _up]),
     ("cpd_trace_rays", C.c_int, [_ctxp, C.POINTER(Design), _dp, _dp, C.c_uint32, C.c_uint32, _up, _dp,
                                  C.POINTER(C.c_uint8)]),
     ("cpd_fitness_gpu_batch", C.c_int, [_ctxp, C.POINTER(Design), C.POINTER(BatchItem), C.c_uint32, C.c_uint32,

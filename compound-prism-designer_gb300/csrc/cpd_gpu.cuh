@@ -173,6 +173,12 @@ void launch_build_records(const cpd_spectrometer_params *p, uint32_t n, double a
 void launch_trace_pairs(const DevDesign *d, const double *lam_u, const double *z64, uint32_t n, uint32_t mode,
                         uint32_t *bins, double *ts, uint8_t *flags, cudaStream_t stream);
 
+// The reference CPU estimator of p(d|lambda) (p_dets_l_wavelength, src/fitness.rs:5-69) for
+// n explicit wavelengths, one block each: out[n x B] and the rays each consumed. z64 holds
+// norminv of the reference's ray points in ray order (max_m of them).
+void launch_tp_adaptive(const DevDesign *d, uint32_t B, const double *lambdas, uint32_t n, const double *z64,
+                        uint32_t max_m, double *out, uint32_t *rays_out, cudaStream_t stream);
+
 // FP32 FMA throughput probe.
 void launch_fma_peak(float *out, uint32_t iters, int blocks, int threads, cudaStream_t stream);
 

@@ -1022,6 +1022,147 @@ __global__ void __launch_bounds__(128) trace_pairs_kernel(const DevDesign *__res
     if (flags) flags[i] = fl;
 }
 
+// ------------------------------------------------------------------ p_dets_l_wavelength
+//
+// The reference CPU estimator of p(d|lambda) for one wavelength
+// (vector_quasi_monte_carlo_integration + p_dets_l_wavelength, src/fitness.rs:5-34,48-69),
+// the one Spectrometer.transmission_probability returns (src/pylib.rs:1028-1058): rays in
+// order; a ray that hits bin b pads b's Welford state with zeros up to the ray count
+// (Welford::skip), adds its t (next_sample), and the integration stops at the first hit
+// after which its bin's SEM^2 <= (5e-3)^2 (sem_le_error_threshold, welford.rs:5-57); every
+// bin is then padded to the final count and p = its mean. The bin that fired the stop keeps
+// a count one ahead of the rays (skip then next_sample), as the reference does.
+//
+// One block per wavelength, kTpRays threads. A round traces kTpRays rays in exact f64
+// (x::trace, bit-identical to the reference's f64 trace), sorts the round's hits by (bin,
+// ray), and the first thread of each bin's run replays the run's Welford updates in the
+// reference's f64 operation order, keeping the state after each update and stopping at the
+// run's first passing hit. The round's stop is the earliest passing hit over all bins;
+// each bin then keeps its state after its last hit before or at that ray. The result is
+// the one-ray-at-a-time order of the reference bit for bit: the bins' states are
+// independent, and every hit up to the stop is applied in ray order within its bin.
+constexpr uint32_t kTpRays = 256;
+
+struct TpWelford {
+    double c, m, m2;
+};
+
+// Welford::skip (welford.rs:34-42).
+__device__ __forceinline__ void tp_skip(TpWelford &w, double n)
+{
+    if (w.c < n) {
+        const double z = x::sub(n, w.c);
+        w.m = x::div(x::mul(w.c, w.m), n);
+        w.m2 = x::add(w.m2, x::div(x::mul(x::mul(x::sqr(w.m), w.c), z), n));
+        w.c = n;
+    }
+}
+
+// Welford::next_sample (welford.rs:26-32).
+__device__ __forceinline__ void tp_next(TpWelford &w, double v)
+{
+    w.c = x::add(w.c, 1.0);
+    const double d = x::sub(v, w.m);
+    w.m = x::add(w.m, x::div(d, w.c));
+    w.m2 = x::add(w.m2, x::mul(d, x::sub(v, w.m)));
+}
+
+__global__ void __launch_bounds__(kTpRays) tp_adaptive_kernel(const DevDesign *__restrict__ dd,
+                                                              const double *__restrict__ lambdas,
+                                                              const double *__restrict__ z64, uint32_t max_m,
+                                                              double *out, uint32_t *rays_out)
+{
+    __shared__ __align__(16) DevDesign sD;
+    __shared__ uint32_t key[kTpRays];   // (bin << 8) | ray within the round; ~0u: no hit
+    __shared__ double tv[kTpRays];      // t of the round's ray i
+    __shared__ double sc[kTpRays], sm[kTpRays], sm2[kTpRays];  // state after sorted hit k
+    __shared__ uint32_t stop_i;
+    extern __shared__ __align__(16) double wst[];  // c[B] | m[B] | m2[B]
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t i = tid; i < sizeof(DevDesign) / 4; i += blockDim.x)
+        reinterpret_cast<uint32_t *>(&sD)[i] = reinterpret_cast<const uint32_t *>(dd)[i];
+    const uint32_t B = dd->B;
+    double *wc = wst, *wm = wst + B, *wm2 = wst + 2 * B;
+    for (uint32_t b = tid; b < B; b += blockDim.x) wc[b] = wm[b] = wm2[b] = 0.0;
+    __syncthreads();
+    const double lambda = lambdas[blockIdx.x];
+    const double e2 = x::mul(5e-3, 5e-3);
+    uint32_t count = max_m;
+    for (uint32_t j0 = 0; j0 < max_m; j0 += kTpRays) {
+        const uint32_t j = j0 + tid;
+        uint32_t k = ~0u;
+        if (j < max_m) {
+            uint32_t bin = 0;
+            double t = 0.0;
+            if (x::trace(sD, lambda, x::beam_y(sD, z64[j]), bin, t) == 0) {
+                k = (bin << 8) | tid;
+                tv[tid] = t;
+            }
+        }
+        key[tid] = k;
+        if (tid == 0) stop_i = ~0u;
+        if (!__syncthreads_or(k != ~0u)) continue;  // no hit this round
+        // bitonic sort of the keys: hits grouped by bin, in ray order within a bin
+        for (uint32_t w = 2; w <= kTpRays; w <<= 1)
+            for (uint32_t h = w >> 1; h > 0; h >>= 1) {
+                const uint32_t o = tid ^ h;
+                if (o > tid) {
+                    const uint32_t a = key[tid], b = key[o];
+                    if ((a > b) == ((tid & w) == 0)) {
+                        key[tid] = b;
+                        key[o] = a;
+                    }
+                }
+                __syncthreads();
+            }
+        const uint32_t kk = key[tid];
+        const bool head = kk != ~0u && (tid == 0 || (key[tid - 1] >> 8) != (kk >> 8));
+        uint32_t last = tid;  // sorted position of the run's last hit
+        if (head) {
+            const uint32_t b = kk >> 8;
+            TpWelford st{wc[b], wm[b], wm2[b]};
+            while (last + 1 < kTpRays && key[last + 1] != ~0u && (key[last + 1] >> 8) == b) last++;
+            for (uint32_t q = tid; q <= last; q++) {
+                const uint32_t i = key[q] & 0xffu;
+                tp_skip(st, (double)(j0 + i + 1u));
+                tp_next(st, tv[i]);
+                sc[q] = st.c;
+                sm[q] = st.m;
+                sm2[q] = st.m2;
+                if (st.m2 < x::mul(e2, x::mul(st.c, x::sub(st.c, 1.0)))) {
+                    atomicMin(&stop_i, i);
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t si = stop_i;
+        if (head) {
+            // the bin's state after its last hit at or before the stop
+            int q_keep = -1;
+            for (uint32_t q = tid; q <= last && (key[q] & 0xffu) <= si; q++) q_keep = (int)q;
+            if (q_keep >= 0) {
+                const uint32_t b = kk >> 8;
+                wc[b] = sc[q_keep];
+                wm[b] = sm[q_keep];
+                wm2[b] = sm2[q_keep];
+            }
+        }
+        __syncthreads();
+        if (si != ~0u) {
+            count = j0 + si + 1u;
+            break;
+        }
+    }
+    // every bin padded to the final ray count (the reference's closing skip)
+    for (uint32_t b = tid; b < B; b += blockDim.x) {
+        TpWelford st{wc[b], wm[b], wm2[b]};
+        tp_skip(st, (double)count);
+        out[(uint64_t)blockIdx.x * B + b] = st.m;
+    }
+    if (tid == 0 && rays_out) rays_out[blockIdx.x] = count;
+}
+
 __global__ void fma_peak_kernel(float *out, uint32_t iters)
 {
     float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
@@ -1177,6 +1318,13 @@ void launch_trace_pairs(const DevDesign *d, const double *lam_u, const double *z
 {
     if (!n) return;
     trace_pairs_kernel<<<(n + 127) / 128, 128, 0, stream>>>(d, lam_u, z64, n, mode, bins, ts, flags);
+}
+
+void launch_tp_adaptive(const DevDesign *d, uint32_t B, const double *lambdas, uint32_t n, const double *z64,
+                        uint32_t max_m, double *out, uint32_t *rays_out, cudaStream_t stream)
+{
+    if (!n) return;
+    tp_adaptive_kernel<<<n, kTpRays, 3 * sizeof(double) * B, stream>>>(d, lambdas, z64, max_m, out, rays_out);
 }
 
 void launch_fma_peak(float *out, uint32_t iters, int blocks, int threads, cudaStream_t stream)

@@ -169,6 +169,10 @@ struct cpd_context {
     PassSlot main;
     DevBuf pair_design, pair_lam, pair_z, pair_bins, pair_ts, pair_flags, peak, logtab;
     DevBuf bld_params, bld_out, bld_status;  // cpd_design_build_device
+    // cpd_transmission_probability: the design, the wavelengths, the ray table of the
+    // reference's ray points (kept while max_m stays the same), the results
+    DevBuf tp_design, tp_lam, tp_z, tp_out, tp_rays;
+    uint32_t tp_m = 0;
     uint32_t ray_tile = 32;
     uint32_t warps_per_cta = 8;
     bool profiling = false;
@@ -910,6 +914,8 @@ void cpd_context_destroy(cpd_context *ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     ctx->main.destroy();
+    for (DevBuf *b : {&ctx->tp_design, &ctx->tp_lam, &ctx->tp_z, &ctx->tp_out, &ctx->tp_rays})
+        b->release();
     for (DevBuf *b : {&ctx->bld_params, &ctx->bld_out, &ctx->bld_status, &ctx->pair_design, &ctx->pair_lam,
                       &ctx->pair_z, &ctx->pair_bins, &ctx->pair_ts,
                       &ctx->pair_flags, &ctx->peak, &ctx->logtab})
@@ -1160,22 +1166,74 @@ int cpd_set_autotune(cpd_context *ctx, int on)
 int cpd_transmission_probability(cpd_context *ctx, const cpd_design *d, const double *wavelengths, uint32_t n,
                                  uint32_t max_m, double *out)
 {
+    return cpd_transmission_probability_ex(ctx, d, wavelengths, n, max_m, 0u, out, nullptr);
+}
+
+int cpd_transmission_probability_ex(cpd_context *ctx, const cpd_design *d, const double *wavelengths, uint32_t n,
+                                    uint32_t max_m, uint32_t flags, double *out, uint32_t *rays_out)
+{
     if (!ctx || !valid_design(d) || !wavelengths || !out || n == 0 || n > CPD_MAX_WAVELENGTHS || max_m == 0 ||
-        max_m > CPD_MAX_RAYS)
+        max_m > CPD_MAX_RAYS || (flags & ~(uint32_t)CPD_TP_FIXED_N))
         return CPD_INVALID_ARGUMENT;
-    // explicit wavelengths: bounds (0, 1) make wmin + (wmax - wmin)*u == u exactly
-    cpd_design dd = *d;
-    dd.wavelength_bounds[0] = 0.0;
-    dd.wavelength_bounds[1] = 1.0;
-    std::vector<double> ray_u(max_m);
-    double st = 0.5;  // the reference CPU ray points (fitness.rs:19)
-    for (uint32_t j = 0; j < max_m; j++) {
-        st = st + kAlpha;
-        st = st - std::trunc(st);
-        ray_u[j] = st;
+    // the reference CPU ray points (fitness.rs:19): the incremental R1 sequence from 0.5
+    auto ref_points = [](uint32_t m, double *u) {
+        double st = 0.5;
+        for (uint32_t j = 0; j < m; j++) {
+            st = st + kAlpha;
+            st = st - std::trunc(st);
+            u[j] = st;
+        }
+    };
+    if (flags & CPD_TP_FIXED_N) {
+        // explicit wavelengths: bounds (0, 1) make wmin + (wmax - wmin)*u == u exactly
+        cpd_design dd = *d;
+        dd.wavelength_bounds[0] = 0.0;
+        dd.wavelength_bounds[1] = 1.0;
+        std::vector<double> ray_u(max_m);
+        ref_points(max_m, ray_u.data());
+        cpd_fitness f;
+        const int e = cpd_fitness_gpu_points(ctx, &dd, wavelengths, n, ray_u.data(), max_m, CPD_TRACE_HYBRID, &f, out);
+        if (!e && rays_out)
+            for (uint32_t i = 0; i < n; i++) rays_out[i] = max_m;
+        return e;
     }
-    cpd_fitness f;
-    return cpd_fitness_gpu_points(ctx, &dd, wavelengths, n, ray_u.data(), max_m, CPD_TRACE_HYBRID, &f, out);
+    CPD_SYNC_ENTRY(ctx);
+    PassSlot &S = ctx->main;
+    cudaStream_t s = S.stream;
+    DevDesign D;
+    design_to_dev(*d, D);
+    if (ctx->tp_m != max_m) {
+        std::vector<double> z(max_m);
+        ref_points(max_m, z.data());
+        for (uint32_t j = 0; j < max_m; j++) z[j] = norminv(z[j]);
+        CPD_TRY(ctx->tp_z.ensure(sizeof(double) * max_m));
+        CPD_TRY(cudaMemcpyAsync(ctx->tp_z.p, z.data(), sizeof(double) * max_m, cudaMemcpyHostToDevice, s));
+        ctx->tp_m = max_m;
+        S.h2d += sizeof(double) * max_m;
+    }
+    const size_t out_bytes = sizeof(double) * (size_t)n * D.B;
+    CPD_TRY(ctx->tp_design.ensure(sizeof(DevDesign)));
+    CPD_TRY(ctx->tp_lam.ensure(sizeof(double) * n));
+    CPD_TRY(ctx->tp_out.ensure(out_bytes));
+    CPD_TRY(ctx->tp_rays.ensure(sizeof(uint32_t) * n));
+    CPD_TRY(cudaMemcpyAsync(ctx->tp_design.p, &D, sizeof(DevDesign), cudaMemcpyHostToDevice, s));
+    CPD_TRY(cudaMemcpyAsync(ctx->tp_lam.p, wavelengths, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    CPD_TRY(cudaEventRecord(S.ev0, s));
+    launch_tp_adaptive(ctx->tp_design.as<DevDesign>(), D.B, ctx->tp_lam.as<double>(), n, ctx->tp_z.as<double>(),
+                       max_m, ctx->tp_out.as<double>(), ctx->tp_rays.as<uint32_t>(), s);
+    CPD_TRY(cudaGetLastError());
+    CPD_TRY(cudaEventRecord(S.ev1, s));
+    CPD_TRY(cudaMemcpyAsync(out, ctx->tp_out.p, out_bytes, cudaMemcpyDeviceToHost, s));
+    if (rays_out)
+        CPD_TRY(cudaMemcpyAsync(rays_out, ctx->tp_rays.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
+    CPD_TRY(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, S.ev0, S.ev1);
+    S.last_ms = ms;
+    S.launches = 1;
+    S.h2d += sizeof(DevDesign) + sizeof(double) * n;
+    S.d2h += out_bytes + (rays_out ? sizeof(uint32_t) * n : 0);
+    return CPD_OK;
 }
 
 int cpd_trace_rays(cpd_context *ctx, const cpd_design *d, const double *lam_u, const double *ray_u, uint32_t n,

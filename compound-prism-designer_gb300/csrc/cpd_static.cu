@@ -8,11 +8,13 @@
 // cpd_fitness_gpu_points_static serves them. It runs the same kernels as
 // cpd_fitness_gpu_points, with every intermediate buffer carved out of one file-scope
 // device array of fixed size (limits below). The caller passes host inputs and outputs
-// only, and no context is needed. The first call on a device resolves the array's
-// device address (cudaGetSymbolAddress) and loads the log2 table into it, so that first
-// call should come before any stream capture. Calls share the array, which keeps the
-// last call's contents; each call clears what must start at zero. Calls that overlap on
-// the GPU race on it; calls from threads of one process are serialised per device.
+// only, and no context is needed. Every call resolves the array's address in the
+// current context (cudaGetSymbolAddress) and uploads the log2 table with its inputs, so a
+// call made after a cudaDeviceReset, or from another driver context on the same GPU, finds
+// a valid array with the table in it. Calls share the array, which keeps the last call's
+// contents; each call clears what must start at zero. Calls that overlapped on the GPU
+// would race on it, so calls from threads of one process are serialised per device; the
+// work runs on the legacy default stream, and the call returns when it is done.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -56,34 +58,34 @@ constexpr size_t kScratchBytes = kOffQueue + al256(sizeof(QEntry) * kStaticQueue
 // address: the kernels receive the address that call returns.
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
+// One upload per call: design | job | log2 table | wavelength points | z64 | z32, at the
+// offsets they have in the array (kOffDesign .. kOffLog, then kOffLam .. kOffZ32 as one
+// contiguous span).
+constexpr size_t kUpHead = kOffLog + sizeof(float) * 4 * ff::kLogTable;  // design, job, table
+constexpr size_t kUpTail = kOffLp - kOffLam;                             // lam, z64, z32
+
+// Host-side state of one device: the call lock and fixed staging storage (file-scope, no
+// allocation; used only under `call`).
 struct DeviceState {
-    unsigned char *base = nullptr;  // device address of g_scratch on this device
+    std::mutex call;  // one call at a time per device within this process
     int sms = 0;
-    bool ready = false;
-    std::mutex call;                // one call at a time per device within this process
+    double z64[kStaticMaxR];
+    alignas(256) unsigned char head[kUpHead];
+    alignas(256) unsigned char tail[kUpTail];
 };
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
+constexpr int kMaxDevices = 16;
 DeviceState g_dev[kMaxDevices];
 
-// Once per device, with that device current: resolve the array's device address and
-// load the float-float log2 table into it.
-int static_setup(int dev, DeviceState *&st)
+// The scratch array's device address in the current context. Resolved on every call (a
+// host-side lookup): after a cudaDeviceReset the module is loaded again, and another
+// driver context on the same GPU has its own copy of the array.
+int static_base(int dev, DeviceState &st, unsigned char *&base)
 {
-    if (dev < 0 || dev >= kMaxDevices) return CPD_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    st = &g_dev[dev];
-    if (st->ready) return CPD_OK;
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return CPD_CUDA_ERROR;
-    if (cudaDeviceGetAttribute(&st->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return CPD_CUDA_ERROR;
-    float tab[4 * ff::kLogTable];
-    ff::make_log_table(tab);
-    if (cudaMemcpy(static_cast<unsigned char *>(p) + kOffLog, tab, sizeof(tab), cudaMemcpyHostToDevice) !=
-        cudaSuccess)
+    if (st.sms == 0 && cudaDeviceGetAttribute(&st.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return CPD_CUDA_ERROR;
-    st->base = static_cast<unsigned char *>(p);
-    st->ready = true;
+    base = static_cast<unsigned char *>(p);
     return CPD_OK;
 }
 
@@ -101,27 +103,31 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     if (W > kStaticMaxW || R > kStaticMaxR || d->bin_count > kStaticMaxB) return CPD_NO_CAPACITY;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return CPD_CUDA_ERROR;
-    DeviceState *st = nullptr;
-    int e = static_setup(dev, st);
+    if (dev < 0 || dev >= kMaxDevices) return CPD_INVALID_ARGUMENT;
+    DeviceState &st = g_dev[dev];
+    std::lock_guard<std::mutex> lk(st.call);
+    unsigned char *b = nullptr;
+    int e = static_base(dev, st, b);
     if (e) return e;
-    std::lock_guard<std::mutex> lk(st->call);
 
-    // host-side tables in fixed storage (no allocation)
-    static thread_local double z64[kStaticMaxR];
-    static thread_local float z32[2 * kStaticMaxR];
+    // host-side tables in the device's fixed staging storage (no allocation)
+    double *z64 = reinterpret_cast<double *>(st.tail + (kOffZ64 - kOffLam));
+    float *z32 = reinterpret_cast<float *>(st.tail + (kOffZ32 - kOffLam));
     uint32_t Rz = 0;
     for (uint32_t j = 0; j < R; j++) {
         const double z = norminv(ray_u[j]);
-        if (std::isfinite(z)) z64[Rz++] = z;
+        if (std::isfinite(z)) st.z64[Rz++] = z;
     }
-    std::sort(z64, z64 + Rz);
+    std::sort(st.z64, st.z64 + Rz);
     for (uint32_t j = 0; j < Rz; j++) {
+        z64[j] = st.z64[j];
         z32[2 * j] = (float)z64[j];
         z32[2 * j + 1] = (float)(z64[j] - (double)z32[2 * j]);
     }
-    DevDesign D;
+    std::memcpy(st.tail, lam_u, 8 * (size_t)W);
+    DevDesign &D = *reinterpret_cast<DevDesign *>(st.head + kOffDesign);
     design_to_dev(*d, D);
-    DesignJob J;
+    DesignJob &J = *reinterpret_cast<DesignJob *>(st.head + kOffJob);
     std::memset(&J, 0, sizeof(J));
     const uint32_t ray_tile = 32;
     J.W = W;
@@ -133,20 +139,16 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     J.ntiles = (W + J.tile_rows - 1) / J.tile_rows;
     ff::split(kTScaleInv / (double)R, J.unit_hi, J.unit_lo);
     ff::split(-31.0 - std::log2((double)R), J.lu_hi, J.lu_lo);
+    ff::make_log_table(reinterpret_cast<float *>(st.head + kOffLog));
 
-    unsigned char *b = st->base;
+    // The array keeps the previous call's contents: everything that must start at zero is
+    // cleared. The control words, accumulators and results lie between the job and the log2
+    // table, so the head upload carries their zeros; the histogram is cleared on the device.
+    std::memset(st.head + kOffCtl, 0, kOffLog - kOffCtl);
     const size_t cells = (size_t)W * D.B;
-    if (cudaMemcpy(b + kOffDesign, &D, sizeof(D), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(b + kOffJob, &J, sizeof(J), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(b + kOffLam, lam_u, 8 * (size_t)W, cudaMemcpyHostToDevice) != cudaSuccess ||
-        (Rz && cudaMemcpy(b + kOffZ64, z64, 8 * (size_t)Rz, cudaMemcpyHostToDevice) != cudaSuccess) ||
-        (Rz && cudaMemcpy(b + kOffZ32, z32, 8 * (size_t)Rz, cudaMemcpyHostToDevice) != cudaSuccess))
-        return CPD_CUDA_ERROR;
-    // the array keeps the previous call's contents: clear everything that must start at zero
-    if (cudaMemset(b + kOffCtl, 0, sizeof(Control)) != cudaSuccess ||
-        cudaMemset(b + kOffAcc, 0, sizeof(DesignAcc)) != cudaSuccess ||
-        cudaMemset(b + kOffS1, 0, 8 * (size_t)D.B) != cudaSuccess ||
-        cudaMemset(b + kOffS2, 0, 8 * (size_t)D.B) != cudaSuccess ||
+    const size_t tail_bytes = (kOffZ32 - kOffLam) + 8 * (size_t)Rz;
+    if (cudaMemcpy(b, st.head, kUpHead, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b + kOffLam, st.tail, tail_bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(b + kOffHist, 0, 8 * cells) != cudaSuccess)
         return CPD_CUDA_ERROR;
 
@@ -183,7 +185,7 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     }
     a.p_out = p_out ? reinterpret_cast<double *>(b + kOffPout) : nullptr;
     a.logtab = reinterpret_cast<const float *>(b + kOffLog);
-    launch_pass(a, st->sms, 8, 0);
+    launch_pass(a, st.sms, 8, 0);
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(0) != cudaSuccess) return CPD_CUDA_ERROR;
 
     Control ctl;

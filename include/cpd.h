@@ -6,7 +6,7 @@
  * sizes and returns a cpd_status; nothing throws across the ABI. Each
  * declaration names the reference interface it replaces (paths inside the
  * reference project). A Rust -sys crate, a ctypes stub or a pyo3 shim binds
- * this header unchanged (INTEGRATION.md shows the bindings).
+ * this header unchanged.
  *
  * Units: lengths in millimetres, wavelengths in micrometres, angles in radians.
  */
@@ -218,21 +218,44 @@ int cpd_fitness_gpu_points(cpd_context *ctx, const cpd_design *d, const double *
  * intermediate buffer lives in one file-scope device array of about 3 MiB, which every
  * GPU that loads the library holds until the process exits. Inputs and outputs are host
  * pointers; no context is used; the work runs on the legacy default stream of the
- * current device and the call returns when it is done. Limits per call: W <= 1024
- * wavelengths, R <= 4096 rays, bin_count <= 128, at most 32768 guard-band rays re-traced;
- * larger requests return CPD_NO_CAPACITY. The first call on a device resolves the
- * array's device address and loads a table into it, so make that first call before any
- * stream capture. Every call shares the array, which keeps the previous call's contents;
- * each call clears what must start at zero. Calls that overlap on the GPU race on the
- * array; calls from threads of one process are serialised per device. */
+ * current device and the call returns when it is done. Each call resolves the array's
+ * address in the current context and uploads every table it needs with its inputs, so
+ * it stays valid after a cudaDeviceReset and from another driver context on the same
+ * GPU. Limits per call: W <= 1024 wavelengths, R <= 4096 rays, bin_count <= 128;
+ * larger requests return CPD_NO_CAPACITY. CPD_NO_CAPACITY also depends on the data: at
+ * most 32768 guard-band rays are re-traced per call (about 0.8% of the rays at the
+ * largest W and R), so a design with many rays near a decision threshold (near-critical
+ * exit faces) can exceed it at sizes within the limits; the allocating entry points grow
+ * their queue instead. Every call on a device shares the array, which keeps the previous
+ * call's contents; each call clears what must start at zero. Calls that overlapped on the
+ * GPU would race on the array: calls from threads of one process are therefore serialised
+ * per device, and each returns only when its work is done. */
 int cpd_fitness_gpu_points_static(const cpd_design *d, const double *lam_u, uint32_t W, const double *ray_u,
                                   uint32_t R, uint32_t trace_mode, cpd_fitness *out, double *p_out);
 
-/* Spectrometer.transmission_probability (src/pylib.rs:1029-1058): p(d|lambda) for
- * explicit wavelengths, max_m rays each (fixed N: no early SEM stop).
- * out is n*B row-major. */
+/* Spectrometer.transmission_probability (src/pylib.rs:1028-1058): p(d|lambda) for
+ * explicit wavelengths by the reference's estimator, p_dets_l_wavelength
+ * (src/fitness.rs:5-34,48-69): the reference's ray points (the R1 sequence from 0.5,
+ * fitness.rs:19) in order, at most max_m per wavelength; each hit pads its bin's Welford
+ * state with zeros up to the ray count and adds its t, and the wavelength stops at the
+ * first hit after which its bin's SEM <= 5e-3; p is each bin's mean after padding every bin
+ * to the final count. Each ray is traced in exact f64 and the Welford updates follow the
+ * reference's f64 operation order, so the results are the reference's own. out is n*B
+ * row-major. */
 int cpd_transmission_probability(cpd_context *ctx, const cpd_design *d, const double *wavelengths,
                                  uint32_t n, uint32_t max_m, double *out);
+
+/* Flag of cpd_transmission_probability_ex: every wavelength uses all max_m rays (fixed N,
+ * p = sum of t / max_m, the estimator of cpd_fitness_gpu_points) instead of the reference's
+ * SEM stop. */
+#define CPD_TP_FIXED_N 0x1u
+
+/* cpd_transmission_probability with flags (0 or CPD_TP_FIXED_N) and, optionally, the rays
+ * each wavelength consumed (rays_out, n entries: the ray at which the stop fired, or
+ * max_m). */
+int cpd_transmission_probability_ex(cpd_context *ctx, const cpd_design *d, const double *wavelengths,
+                                    uint32_t n, uint32_t max_m, uint32_t flags, double *out,
+                                    uint32_t *rays_out);
 
 /* launch_propagation_test / propagation_test_kernel (src/cuda_fitness.rs:247-317,
  * src/spectrometer/kernel.rs:195-224): one ray per (lam_u[i], ray_u[i]) pair.

@@ -564,8 +564,9 @@ int orc_propagation_path(const orc_spec *s, double wavelength, double initial_y,
     return n;
 }
 
-/* vector_quasi_monte_carlo_integration + p_dets_l_wavelength (fitness.rs:5-34, 48-69). */
-static void p_dets_adaptive(const spectrometer *sp, double w, size_t max_m, welford *stats)
+/* vector_quasi_monte_carlo_integration + p_dets_l_wavelength (fitness.rs:5-34, 48-69).
+ * Returns the rays consumed (the integration's final `count`). */
+static size_t p_dets_adaptive(const spectrometer *sp, double w, size_t max_m, welford *stats)
 {
     uint32_t nbin = sp->det.bin_count;
     const double max_err = 5e-3;
@@ -585,19 +586,27 @@ static void p_dets_adaptive(const spectrometer *sp, double w, size_t max_m, welf
         }
     }
     for (uint32_t i = 0; i < nbin; i++) wf_skip(&stats[i], count);
+    return (size_t)count;
 }
 
-int orc_p_dets_l_wavelength(const orc_spec *s, double wavelength, size_t max_m, double *out)
+int orc_p_dets_l_wavelength_count(const orc_spec *s, double wavelength, size_t max_m, double *out,
+                                  uint64_t *rays_out)
 {
     spectrometer sp;
     int e = build_spectrometer(s, &sp);
     if (e) return e;
     welford *stats = calloc(sp.det.bin_count, sizeof(welford));
     if (!stats) return ORC_INVALID;
-    p_dets_adaptive(&sp, wavelength, max_m, stats);
+    size_t c = p_dets_adaptive(&sp, wavelength, max_m, stats);
     for (uint32_t i = 0; i < sp.det.bin_count; i++) out[i] = stats[i].mean;
+    if (rays_out) *rays_out = c;
     free(stats);
     return ORC_OK;
+}
+
+int orc_p_dets_l_wavelength(const orc_spec *s, double wavelength, size_t max_m, double *out)
+{
+    return orc_p_dets_l_wavelength_count(s, wavelength, max_m, out, NULL);
 }
 
 /* mutual_information + fitness (fitness.rs:79-147). */

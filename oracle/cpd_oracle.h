@@ -94,6 +94,10 @@ int orc_fitness_adaptive(const orc_spec *s, size_t max_n, size_t max_m, double o
 
 /* p_dets_l_wavelength (src/fitness.rs:48-69) for one wavelength: writes bin_count means. */
 int orc_p_dets_l_wavelength(const orc_spec *s, double wavelength, size_t max_m, double *out);
+/* The same, also writing the rays consumed (the integration's final count: the ray at
+ * which the SEM stop fired, or max_m). */
+int orc_p_dets_l_wavelength_count(const orc_spec *s, double wavelength, size_t max_m, double *out,
+                                  uint64_t *rays_out);
 
 /* Fixed-N estimator on explicit point sets: wavelength u-points lam_u[W]
  * (lambda = wmin + (wmax-wmin)*u) and ray u-points ray_u[R]. p(d|lambda) = sum(t)/R over

@@ -48,8 +48,15 @@ class OrcSpec(C.Structure):
     ]
 
 
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    return any(os.path.getmtime(os.path.join(HERE, f)) > t for f in ("cpd_oracle.c", "cpd_oracle.h", "build.sh"))
+
+
 def build(force: bool = False) -> str:
-    if force or not os.path.exists(LIB_PATH):
+    if force or _stale():
         subprocess.check_call(["bash", os.path.join(HERE, "build.sh")])
     return LIB_PATH
 
@@ -76,6 +83,7 @@ def lib():
         L.orc_propagation_path.argtypes = [sp, C.c_double, C.c_double, dp]
         L.orc_fitness_adaptive.argtypes = [sp, C.c_size_t, C.c_size_t, dp]
         L.orc_p_dets_l_wavelength.argtypes = [sp, C.c_double, C.c_size_t, dp]
+        L.orc_p_dets_l_wavelength_count.argtypes = [sp, C.c_double, C.c_size_t, dp, C.POINTER(C.c_uint64)]
         L.orc_fitness_points.argtypes = [sp, dp, C.c_size_t, dp, C.c_size_t, C.c_int, dp, dp,
                                          C.POINTER(C.c_uint64)]
         L.orc_fitness_adaptive_points.argtypes = [sp, dp, C.c_size_t, dp, C.c_size_t, C.c_int, dp, dp,
@@ -179,6 +187,16 @@ def p_dets_l_wavelength(d: dict, wavelength: float, max_m: int = 16384) -> np.nd
     e = lib().orc_p_dets_l_wavelength(C.byref(s), float(wavelength), max_m, _dp(out))
     assert e == OK, e
     return out
+
+
+def p_dets_l_wavelength_count(d: dict, wavelength: float, max_m: int = 16384):
+    """(p(d|lambda)[B], rays consumed) of the reference's adaptive per-bin estimator."""
+    s = make_spec(d)
+    out = np.zeros(int(d["bin_count"]))
+    n = C.c_uint64(0)
+    e = lib().orc_p_dets_l_wavelength_count(C.byref(s), float(wavelength), max_m, _dp(out), C.byref(n))
+    assert e == OK, e
+    return out, int(n.value)
 
 
 def fitness_points(d: dict, lam_u, ray_u, nthreads: int = 1, want_p: bool = True):

@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures in this folder from the reference sources.
 
-Run in a container where the reference project is checked out (its path is the
-first argument, default /root/reference). Nothing here runs during the tests:
+Run in a container where the reference project is checked out; its path is the
+required first argument. Nothing here runs during the tests:
 the tests read the JSON files this script writes.
 
 * f1_known_design.json -- the known 3-glass design of the reference's
@@ -127,7 +127,9 @@ def glass_fits(ref: str, n: int = 8, seed: int = 20261203):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference project>")
+    ref = sys.argv[1]
     for name, obj in (("f1_known_design.json", f1(ref)),
                       ("norminv_points.json", norminv_points(ref)),
                       ("glass_fits.json", glass_fits(ref))):

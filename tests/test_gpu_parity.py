@@ -184,16 +184,6 @@ def test_launch_shapes_give_identical_bits(designs):
         ctx.set_launch_shape(*old)
 
 
-def test_transmission_probability_vs_oracle(designs):
-    name, s, d = designs[0]
-    w = np.linspace(0.5, 0.82, 17)
-    p = s.transmission_probability(w, max_m=1024)
-    dd = dict(d)
-    dd["wavelength_bounds"] = (0.0, 1.0)
-    po, _ = O.fitness_points(dd, w, O.qrng_points(0.5, 1024))
-    assert np.abs(p - po).max() <= 1e-6
-
-
 def test_edge_cases(designs):
     name, s, d = designs[1]
     # one wavelength, one ray; ragged sizes
