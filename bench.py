@@ -4,22 +4,27 @@ Default workload (N=1): the plain one-design GPU call -- 6 prisms, 64 detector
 bins, 4096 QMC wavelengths x 1024 rays (4,194,304 rays per design), FP32 trace
 with FP64/int64 accumulation and entropy. A step is one gpu_fitness call of one
 design. Also measured on the same run, under "forms": the batched population form
-(1024 designs of mixed G, B, W in one captured launch sequence) and the serving form
+(1024 designs of mixed G, B, W in one captured launch sequence), the serving form
 (a continuous-batching server fed by a synthetic generational optimizer: designs/s,
-p50/p99 request latency), and adaptive sampling (the reference kernel's per-wavelength SEM
-stop) beside fixed N at the reference optimizer's sampling.
+p50/p99 request latency) and adaptive sampling (the reference kernel's per-wavelength
+SEM stop) beside fixed N at the reference optimizer's sampling; each form's results
+are checked against the oracle on sampled designs (mi_check).
 
   value   designs/s with inputs resident on the device: 1 / (device time of the pass)
   e2e     designs/s through the C ABI with host buffers (design + point tables H2D,
           result D2H, inside the timed call)
-  roofline  FP32 ALU roofline of the dominant kernel (the trace kernel): algorithmic
-          FLOP of the fast path per evaluated ray x rays evaluated / kernel time,
-          against a live FP32 FMA throughput probe
+  roofline  FP32 roofline of the dominant kernel (the trace kernel): the algorithmic
+          FLOP of the reference's per-ray formulation (the frozen table
+          roofline/ops_per_ray.json, counted by the op-counting build of the oracle) x
+          the design's rays / kernel time, against a live FP32 FMA throughput probe;
+          beside it the executed fast-path count and the SFU bound (live probe)
   cpu_baseline  the C oracle (the reference CPU algorithm restated) on all host cores,
-          on a bounded sample of the same design
+          whole designs, fixed N on the GPU call's own points and the reference's
+          adaptive estimator
 
   --impl reference  times the reference's CPU path (the oracle port: the reference
-          itself is Rust and cannot be built here) on the same workload.
+          itself is Rust and cannot be built here) on the same design and points, built
+          and positioned by the oracle alone (the library is not imported).
 
 Multi-GPU: designs are independent; each rank evaluates its own designs on its own
 GPU with no collective (weak scaling); rank 0 prints the aggregate.
@@ -29,7 +34,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -42,11 +46,22 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 METRIC = "MI fitness designs/sec, batched-serving vs plain at <=1e-4 rel MI err; p50/p99 ms"
 G_PLAIN, B_PLAIN, W_PLAIN, R_PLAIN = 6, 64, 4096, 1024
+PLAIN_SEED = 20261203 + 1
+# The frozen per-ray operation table of the reference's formulation, keyed by prism count.
+OPS_TABLE = os.path.join(ROOT, "roofline", "ops_per_ray.json")
 # FP32 arithmetic of fast_ray on its full path for an anti-reflection-coated design (exit
 # face, refraction, detector, binning and the guard-band thresholds): adds/muls count 1,
 # FMAs 2; the 5 hardware estimates (2 sqrt, 3 reciprocals) and the floor are not counted.
 # Rays lost early execute fewer, so this is an upper bound per evaluated ray.
 FLOP_PER_FAST_RAY = 102
+# Special-function-unit results of fast_ray's full path: 2 square-root and 3 reciprocal
+# estimates.
+SFU_PER_FAST_RAY = 5
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one trace_kernel launch of
+# this workload, from the ncu capture summarised in
+# profiles/fitness_pass_plain_g6_b64_w4096_r1024.md (the figure is copied here when the
+# kernel is re-profiled; bench.py reads no profile file).
+TRACE_TRAFFIC_BYTES = 2725888
 
 
 def dist_info():
@@ -161,49 +176,110 @@ def l2_flusher():
         return (lambda: None), f"not flushed ({type(e).__name__})"
 
 
-def plain_design(seed_offset=1):
+def plain_design():
     import numpy as np
     from compound_prism_designer import synth
 
-    rng = np.random.default_rng(20261203 + seed_offset)
-    spec, d, rej = synth.random_design(rng, G_PLAIN, B_PLAIN)
+    spec, d, rej = synth.random_design(np.random.default_rng(PLAIN_SEED), G_PLAIN, B_PLAIN)
     return spec, d
 
 
-def batched_population(n=1024, seed=20261205):
+def batched_population(n=1024, seed=20261205, with_params=False):
     import numpy as np
     from compound_prism_designer import synth
 
     pop, rej = synth.population(seed, n)
     rng = np.random.default_rng(seed + 1)
     W = rng.integers(512, 4097, n)
+    if with_params:
+        return [s for s, _ in pop], [d for _, d in pop], W, rej
     return [s for s, _ in pop], W, rej
 
 
-def cpu_oracle_rate(d, W, R, target_s=10.0, nthreads=None, gpu_info=None):
-    """Oracle (reference CPU algorithm) on all host threads: designs/s extrapolated from
-    a bounded sample of whole designs, on the points of the plain GPU call (seed 0.5, the
-    GPU policy). The oracle's MI on those points is the check of the GPU's (gpu_info)."""
+def record_to_dict(rec) -> dict:
+    """A cpd_spectrometer_params record (numpy) as the flat parameter dict of the oracle."""
+    G = int(rec["nglass"])
+    f = float
+    return dict(glasses=[[f(c) for c in rec["glass"][g]] for g in range(G)],
+                angles=[f(a) for a in rec["angles"][:G + 1]], lengths=[f(v) for v in rec["lengths"][:G]],
+                curvature=f(rec["curvature"]), height=f(rec["height"]), width=f(rec["width"]),
+                ar_coated=bool(rec["ar_coated"]), bin_count=int(rec["bin_count"]), bin_size=f(rec["bin_size"]),
+                linear_slope=f(rec["linear_slope"]), linear_intercept=f(rec["linear_intercept"]),
+                det_length=f(rec["det_length"]), max_incident_angle=f(rec["max_incident_angle"]),
+                det_angle=f(rec["det_angle"]), det_position=(f(rec["det_position"][0]), f(rec["det_position"][1])),
+                det_flipped=bool(rec["det_flipped"]),
+                wavelength_bounds=(f(rec["wavelength_bounds"][0]), f(rec["wavelength_bounds"][1])),
+                beam_width=f(rec["beam_width"]), beam_y_mean=f(rec["beam_y_mean"]))
+
+
+def oracle_check(cases, adaptive=False, nthreads=None):
+    """The oracle on the GPU results of sampled designs, on their own points (GPU seed
+    policy): cases = [(params dict, seed, W, R, gpu info, gpu hits, gpu rays)]. Returns the
+    largest relative MI error, and whether hits (and, adaptive, rays consumed) are equal."""
     import oracle as O
-    from compound_prism_designer import precision as P
 
     nthreads = nthreads or os.cpu_count() or 1
-    lam_all = P.synth_points(0.5, W)
-    ray_u = P.synth_points(0.5, R, first=1)
-    # whole designs until target_s of CPU time has elapsed (at least one)
+    worst, equal, rows = 0.0, True, []
+    for d, seed, W, R, info, hits, rays in cases:
+        lam, ray_u = O.gpu_points(seed, W), O.gpu_points(seed, R, first=1)
+        if adaptive:
+            _, st, counts = O.fitness_adaptive_points(d, lam, ray_u, nthreads=nthreads)
+            same = hits == st["hits"] and rays == int(counts.sum())
+        else:
+            _, st = O.fitness_points(d, lam, ray_u, nthreads=nthreads, want_p=False)
+            same = hits == st["hits"]
+        rel = abs(info - st["info"]) / max(abs(st["info"]), 1e-300)
+        worst = max(worst, rel)
+        equal = equal and same
+        rows.append({"W": W, "R": R, "G": len(d["glasses"]), "B": d["bin_count"], "rel_err": rel})
+    return {"designs": len(cases), "max_rel_err": worst, "tolerance": 1e-4,
+            "hits_equal" if not adaptive else "hits_and_rays_equal": equal, "per_design": rows}
+
+
+def cpu_oracle_rate(d, W, R, target_s=10.0, nthreads=None, gpu_info=None):
+    """Oracle (reference CPU algorithm) on all host threads, whole designs for at least
+    target_s, on the points of the plain GPU call (seed 0.5, the GPU policy): fixed N, the
+    GPU's own estimator. The oracle's MI on those points is the check of the GPU's
+    (gpu_info). Beside it the reference's adaptive estimator (reference_adaptive)."""
+    import oracle as O
+
+    nthreads = nthreads or os.cpu_count() or 1
+    lam_all = O.gpu_points(0.5, W)
+    ray_u = O.gpu_points(0.5, R, first=1)
     done, t0 = 0, time.perf_counter()
     while done == 0 or time.perf_counter() - t0 < target_s:
         _, st = O.fitness_points(d, lam_all, ray_u, nthreads=nthreads, want_p=False)
-        done += W
+        done += 1
     dt = time.perf_counter() - t0
-    rate = done / (W * dt)
-    out = {"value": rate, "unit": "designs/s", "cores": nthreads, "kind": "port",
-           "sample": f"{done} wavelength rows ({done / W:.2f} designs) x {R} rays of the benchmark design "
-                     f"({done * R} rays, {dt:.1f} s, {nthreads} threads)"}
+    out = {"value": done / dt, "unit": "designs/s", "cores": nthreads, "kind": "port",
+           "sample": f"{done} whole designs of the benchmark workload ({W} wavelengths x {R} rays each, "
+                     f"{done * W * R} rays, {dt:.1f} s, {nthreads} threads, fixed N on the GPU call's points)",
+           "reference_adaptive": reference_adaptive_rate(d, W, R, nthreads)}
     if gpu_info is not None:
         out["mi_check"] = {"gpu_mi": gpu_info, "oracle_mi": st["info"],
                            "rel_err": abs(gpu_info - st["info"]) / abs(st["info"]), "tolerance": 1e-4}
     return out
+
+
+def reference_adaptive_rate(d, max_n, max_m, nthreads, target_s=3.0):
+    """The reference CPU fitness as it runs (src/fitness.rs:79-147: SEM stops per
+    wavelength and across wavelengths, its own point set), one design per thread as the
+    reference is single-threaded per design, whole designs for at least target_s."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import oracle as O
+
+    res = [O.fitness_adaptive(d, max_n, max_m)]
+    done, t0 = 0, time.perf_counter()
+    with ThreadPoolExecutor(nthreads) as ex:  # ctypes releases the GIL during each call
+        while done == 0 or time.perf_counter() - t0 < target_s:
+            res = list(ex.map(lambda _: O.fitness_adaptive(d, max_n, max_m), range(nthreads * 4)))
+            done += len(res)
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "designs/s", "cores": nthreads, "max_n": max_n, "max_m": max_m,
+            "info": res[0][1], "sample": f"{done} whole designs, one per thread, {dt:.2f} s",
+            "note": "a different estimator: stops each wavelength at the first hit whose bin's SEM <= 5e-3 "
+                    "and stops the wavelengths once every bin's SEM across them is <= 5e-3"}
 
 
 def adaptive_form(ctx, n=256):
@@ -245,6 +321,17 @@ def adaptive_form(ctx, n=256):
             ms.append(ctx.last_timing()[0])
         out[f"batch_{name}_ms_device"] = min(ms[1:])
         out[f"batch_{name}_designs_per_s_device"] = nb / (min(ms[1:]) / 1e3)
+        if sampling:
+            # the oracle on 8 designs of the batch (their rays consumed must be equal too)
+            recs = gen.to_params(pop, cat)[ok]
+            idx = np.linspace(0, nb - 1, 8).astype(int)
+            import oracle as O
+
+            cases = []
+            for i in idx:
+                dct = O.accept_params(record_to_dict(recs[i]))
+                cases.append((dct, 0.5, W, R, outs[i].info, outs[i].hits, outs[i].rays))
+            out["mi_check"] = oracle_check(cases, adaptive=True)
     return out
 
 
@@ -309,6 +396,16 @@ def serving_form(ctx, generations=200):
         # records submitted; no host build step)
         dev = gen.serve(sv, generations=generations, seed=2, device_build=True)
         st = sv.stats()
+        # the oracle on a request of 8 designs served by the same server
+        import oracle as O
+
+        recs = gen.to_params(pre, cat)[pok]
+        idx = np.linspace(0, len(pd) - 1, 8).astype(int)
+        rid = sv.submit(pd[idx], seeds=0.375, max_n=W, max_eval=R)
+        souts, _ = sv.wait(rid)
+        cases = [(O.accept_params(record_to_dict(recs[i])), 0.375, W, R, float(souts["info"][k]),
+                  int(souts["hits"][k]), W * R) for k, i in enumerate(idx)]
+        out["mi_check"] = oracle_check(cases)
     for r in (sat, poi, dev):
         r.pop("latency_ms")
     out["back_to_back"] = sat
@@ -371,35 +468,57 @@ def run_adaptive_only(args):
     print(json.dumps({"form": "adaptive batch", "designs": len(specs), "rays": int(rays), "ms": ms}), flush=True)
 
 
+def _workload_module():
+    """compound_prism_designer/workload.py loaded by file path: the numpy-only parameter
+    draws, without importing the library's package (which would load libcpd.so)."""
+    import importlib.util
+
+    path = os.path.join(ROOT, "compound-prism-designer_gb300", "compound_prism_designer", "workload.py")
+    spec = importlib.util.spec_from_file_location("cpd_workload", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def run_reference(args, dist):
-    """--impl reference: the reference CPU algorithm (oracle port) on the same workload."""
+    """--impl reference: the reference's CPU fitness path (the oracle port, f64, all host
+    threads) on the plain workload's own design and points. The design is drawn by the same
+    seeded numpy generator as the GPU arm's and built and positioned by the oracle alone;
+    the library's package is never imported. A step is one whole design, fixed N on the GPU
+    call's points (the same work as a GPU step); the reference's adaptive estimator (its
+    cpu_fitness, with its early stops) is timed beside it."""
     if dist.rank != 0:
         return
-    spec, d = plain_design()
+    import numpy as np
     import oracle as O
 
+    wl = _workload_module()
+    d, rej = wl.random_params(np.random.default_rng(PLAIN_SEED), G_PLAIN, B_PLAIN, O.accept_params)
     nthreads = os.cpu_count() or 1
-    ray_u = O.qrng_points(0.5, R_PLAIN)
-    lam = O.qrng_points(0.5, W_PLAIN)
-    S = max(nthreads * 4, 64)
+    lam = O.gpu_points(0.5, W_PLAIN)
+    ray_u = O.gpu_points(0.5, R_PLAIN, first=1)
     for _ in range(args.warmup):
-        O.fitness_points(d, lam[:S], ray_u, nthreads=nthreads, want_p=False)
+        O.fitness_points(d, lam, ray_u, nthreads=nthreads, want_p=False)
     t0 = time.perf_counter()
-    for k in range(args.steps):
-        off = (k * S) % (W_PLAIN - S)
-        O.fitness_points(d, lam[off:off + S], ray_u, nthreads=nthreads, want_p=False)
+    for _ in range(args.steps):
+        _, st = O.fitness_points(d, lam, ray_u, nthreads=nthreads, want_p=False)
     dt = time.perf_counter() - t0
-    rate = args.steps * S / (W_PLAIN * dt)
+    rate = args.steps / dt
+    adaptive = reference_adaptive_rate(d, W_PLAIN, R_PLAIN, nthreads)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "designs/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": plain_config("none (CPU)"),
+        "config": plain_config("none (CPU)"), "same_config": True,
         "cpu_baseline": {"value": rate, "unit": "designs/s", "cores": nthreads, "kind": "port",
-                         "sample": f"each step {S} of {W_PLAIN} wavelengths x {R_PLAIN} rays"},
+                         "sample": f"each step one whole design: {W_PLAIN} wavelengths x {R_PLAIN} rays, fixed N "
+                                   f"on the GPU call's points; {args.steps} steps, {dt:.1f} s"},
         "e2e": {"value": rate, "unit": "designs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "mi": st["info"], "hits": st["hits"], "design_rejections": rej,
+        "reference_adaptive": adaptive,
+        "library_imported": "compound_prism_designer" in sys.modules,
         "note": "reference is Rust (nightly, un-vendored git deps): not buildable here; the oracle restates "
-                "its CPU fitness path (src/fitness.rs) in C, f64, on all host threads",
+                "its CPU fitness path (src/fitness.rs, src/spectrometer/*.rs) in C, f64, on all host threads",
     }
     print(json.dumps(line), flush=True)
 
@@ -413,15 +532,9 @@ def plain_config(l2):
             "l2": l2}
 
 
-def traffic_from_profiles():
-    """dram bytes per trace-kernel launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "fitness_pass_plain_g6_b64_w4096_r1024.md")
-    try:
-        txt = open(p).read()
-    except OSError:
-        return None
-    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", txt)
-    return float(m.group(1)) if m else None
+def load_ops_table() -> dict:
+    with open(OPS_TABLE) as fh:
+        return json.load(fh)["by_glasses"]
 
 
 def main():
@@ -497,6 +610,7 @@ def main():
     e2e = designs / wall_s
 
     extras = {}
+    peak = None
     if not args.no_extras and dist.rank == 0:
         try:
             # per-kernel CUDA events on the pass's stream (they stand between the kernels,
@@ -511,17 +625,43 @@ def main():
             kt = {k: statistics.median(x[k] for x in kts) for k in kts[0]}
             ctx.set_profiling(False)
             peak = max(ctx.fp32_peak_tflops(2048) for _ in range(3))
-            achieved = fp.fast_rays * FLOP_PER_FAST_RAY / (kt["trace"] * 1e-3) / 1e12
-            extras["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                                  "frac": achieved / peak, "traffic": traffic_from_profiles(),
-                                  "kernel": "trace_kernel", "kernel_ms": kt,
-                                  "fast_rays": fp.fast_rays, "flop_per_fast_ray": FLOP_PER_FAST_RAY,
-                                  "peak_source": "measured live: FP32 FMA probe on all SMs (cpd_measure_fp32_peak)",
-                                  "retraced": fp.retraced, "hits": fp.hits}
+            sfu_peak = max(ctx.sfu_peak_gops(2048) for _ in range(3))
+            ops = load_ops_table()[str(G_PLAIN)]["per_ray"]
+            rays = W_PLAIN * R_PLAIN
+            t_trace = kt["trace"] * 1e-3
+            t_pass = statistics.median(dev_ms) * 1e-3
+            alg = rays * ops["flop"] / t_trace / 1e12
+            alg_pass = rays * ops["flop"] / t_pass / 1e12
+            executed = fp.fast_rays * FLOP_PER_FAST_RAY / t_trace / 1e12
+            sfu_alg = rays * (ops["div"] + ops["sqrt"] + ops["log"]) / t_trace / 1e9
+            sfu_exec = fp.fast_rays * SFU_PER_FAST_RAY / t_trace / 1e9
+            extras["roofline"] = {
+                "bound": "fp32", "achieved": alg, "peak": peak, "unit": "TFLOP/s", "frac": alg / peak,
+                "traffic": TRACE_TRAFFIC_BYTES,
+                "traffic_source": "ncu capture of trace_kernel on this workload (dram__bytes_read.sum + "
+                                  "dram__bytes_write.sum), profiles/fitness_pass_plain_g6_b64_w4096_r1024.md",
+                "kernel": "trace_kernel", "kernel_ms": kt,
+                "frac_algorithmic": alg / peak,
+                "frac_algorithmic_pass": alg_pass / peak,
+                "frac_executed": executed / peak,
+                "flop_per_ray_algorithmic": ops["flop"],
+                "flop_basis": "the design's W x R rays x the frozen per-ray FLOP of the reference's formulation "
+                              f"(roofline/ops_per_ray.json, G={G_PLAIN}), over the trace kernel's time "
+                              "(frac_algorithmic) and over the whole pass (frac_algorithmic_pass); frac_executed: "
+                              f"{FLOP_PER_FAST_RAY} FP32 FLOP per ray the fast path evaluated",
+                "sfu": {"peak_gops": sfu_peak, "algorithmic_gops": sfu_alg, "frac_algorithmic": sfu_alg / sfu_peak,
+                        "executed_gops": sfu_exec, "frac_executed": sfu_exec / sfu_peak,
+                        "per_ray_algorithmic": ops["div"] + ops["sqrt"] + ops["log"],
+                        "per_fast_ray_executed": SFU_PER_FAST_RAY,
+                        "peak_source": "measured live: reciprocal-square-root chains on all SMs "
+                                       "(cpd_measure_sfu_peak)"},
+                "fast_rays": fp.fast_rays, "flop_per_fast_ray": FLOP_PER_FAST_RAY,
+                "peak_source": "measured live: FP32 FMA probe on all SMs (cpd_measure_fp32_peak)",
+                "retraced": fp.retraced, "hits": fp.hits}
         except Exception as e:  # noqa: BLE001
             extras["roofline"] = {"error": repr(e)}
         try:
-            pop, Ws, rej = batched_population()
+            pop, pdicts, Ws, rej = batched_population(with_params=True)
             t_tune = time.perf_counter()
             tuned = cpd.autotune_batch(pop, seeds=0.5, max_n=Ws, max_eval=R_PLAIN, context=ctx)
             t_tune = time.perf_counter() - t_tune
@@ -540,7 +680,19 @@ def main():
             cpd.fitness_batch(pop, seeds=0.5, max_n=Ws, max_eval=R_PLAIN, context=ctx)
             bk = ctx.last_kernel_times()
             ctx.set_profiling(False)
+            if peak is None:
+                peak = max(ctx.fp32_peak_tflops(2048) for _ in range(3))
+            table = load_ops_table()
+            bflop = sum(int(w) * R_PLAIN * table[str(len(dd["glasses"]))]["per_ray"]["flop"]
+                        for dd, w in zip(pdicts, Ws))
+            idx = np.linspace(0, nb - 1, 8).astype(int)
+            bcheck = oracle_check([(pdicts[i], 0.5, int(Ws[i]), R_PLAIN, outs[i].info, outs[i].hits, 0) for i in idx])
             extras["forms"] = {"batched": {
+                "mi_check": bcheck,
+                "roofline": {"achieved": bflop / (bk["trace"] * 1e-3) / 1e12, "unit": "TFLOP/s",
+                             "frac_algorithmic": bflop / (bk["trace"] * 1e-3) / 1e12 / peak,
+                             "frac_algorithmic_pass": bflop / (min(bdev) * 1e-3) / 1e12 / peak,
+                             "basis": "sum over designs of W x R x the frozen per-ray FLOP of its prism count"},
                 "kernel_ms": bk,
                 "workload": f"{nb} designs, G in 2..6, B in 16..128, W in 512..4096, R={R_PLAIN}",
                 "designs_per_s_device": nb / (min(bdev) / 1e3), "designs_per_s_e2e": nb / min(bt),

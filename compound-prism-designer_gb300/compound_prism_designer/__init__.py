@@ -396,6 +396,12 @@ class Context:
         _check(N.lib.cpd_measure_fp32_peak(self._h, int(iters), C.byref(t)))
         return t.value
 
+    def sfu_peak_gops(self, iters: int = 2048) -> float:
+        """Measured special-function-unit throughput (reciprocal-square-root estimates), G/s."""
+        t = C.c_double(0.0)
+        _check(N.lib.cpd_measure_sfu_peak(self._h, int(iters), C.byref(t)))
+        return t.value
+
 
 _contexts: dict[int, Context] = {}
 _ctx_lock = threading.Lock()

@@ -164,6 +164,7 @@ SIGNATURES = [
     ("cpd_get_launch_shape", C.c_int, [_ctxp, _up, _up]),
     ("cpd_last_timing", C.c_int, [_ctxp, _dp, _up]),
     ("cpd_measure_fp32_peak", C.c_int, [_ctxp, C.c_uint32, _dp]),
+    ("cpd_measure_sfu_peak", C.c_int, [_ctxp, C.c_uint32, _dp]),
     ("cpd_set_profiling", C.c_int, [_ctxp, C.c_int]),
     ("cpd_last_kernel_times", C.c_int, [_ctxp, _dp]),
     ("cpd_last_transfer_bytes", C.c_int, [_ctxp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),

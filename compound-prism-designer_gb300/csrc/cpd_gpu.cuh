@@ -181,5 +181,7 @@ void launch_tp_adaptive(const DevDesign *d, uint32_t B, const double *lambdas, u
 
 // FP32 FMA throughput probe.
 void launch_fma_peak(float *out, uint32_t iters, int blocks, int threads, cudaStream_t stream);
+// SFU (MUFU) throughput probe: 8 x 16 reciprocal-square-root estimates per thread and iteration.
+void launch_mufu_peak(float *out, uint32_t iters, int blocks, int threads, cudaStream_t stream);
 
 }  // namespace cpd

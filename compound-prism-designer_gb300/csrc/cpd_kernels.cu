@@ -1185,6 +1185,25 @@ __global__ void fma_peak_kernel(float *out, uint32_t iters)
     if (s == 12345.0f) out[blockIdx.x] = s;  // keeps the chains live
 }
 
+// SFU throughput probe: eight independent chains of the reciprocal-square-root estimate
+// (MUFU.RSQ) per thread; the values stay near 1.
+__global__ void mufu_peak_kernel(float *out, uint32_t iters)
+{
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = 1.0f + 1e-3f * (float)k + 1e-7f * (float)threadIdx.x;
+    for (uint32_t i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 16; u++)
+#pragma unroll
+            for (int k = 0; k < 8; k++) asm volatile("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(a[k]));
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += a[k];
+    if (s == 12345.0f) out[blockIdx.x] = s;  // keeps the chains live
+}
+
 }  // namespace
 
 // A launch that, with `pdl`, may start before the previous kernel on the stream has
@@ -1325,6 +1344,11 @@ void launch_tp_adaptive(const DevDesign *d, uint32_t B, const double *lambdas, u
 {
     if (!n) return;
     tp_adaptive_kernel<<<n, kTpRays, 3 * sizeof(double) * B, stream>>>(d, lambdas, z64, max_m, out, rays_out);
+}
+
+void launch_mufu_peak(float *out, uint32_t iters, int blocks, int threads, cudaStream_t stream)
+{
+    mufu_peak_kernel<<<blocks, threads, 0, stream>>>(out, iters);
 }
 
 void launch_fma_peak(float *out, uint32_t iters, int blocks, int threads, cudaStream_t stream)

@@ -1298,6 +1298,29 @@ int cpd_measure_fp32_peak(cpd_context *ctx, uint32_t iters, double *tflops)
     return CPD_OK;
 }
 
+int cpd_measure_sfu_peak(cpd_context *ctx, uint32_t iters, double *gops)
+{
+    if (!ctx || !gops || iters == 0) return CPD_INVALID_ARGUMENT;
+    CPD_SYNC_ENTRY(ctx);
+    PassSlot &S = ctx->main;
+    const int threads = 256;
+    const int blocks = ctx->num_sms * 8;
+    CPD_TRY(ctx->peak.ensure(sizeof(float) * blocks));
+    cudaStream_t s = S.stream;
+    launch_mufu_peak(ctx->peak.as<float>(), 16, blocks, threads, s);  // warm-up
+    CPD_TRY(cudaEventRecord(S.ev0, s));
+    launch_mufu_peak(ctx->peak.as<float>(), iters, blocks, threads, s);
+    CPD_TRY(cudaEventRecord(S.ev1, s));
+    CPD_TRY(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, S.ev0, S.ev1);
+    const double ops = 8.0 * 16.0 * (double)iters * threads * (double)blocks;
+    *gops = ops / (ms * 1e-3) / 1e9;
+    S.last_ms = ms;
+    S.launches = 2;
+    return CPD_OK;
+}
+
 // ------------------------------------------------------------------ server ABI
 
 int cpd_server_create(cpd_context *ctx, uint64_t mem_budget_bytes, uint32_t slots, uint32_t max_designs_per_pass,

@@ -225,8 +225,9 @@ int cpd_fitness_gpu_points(cpd_context *ctx, const cpd_design *d, const double *
  * larger requests return CPD_NO_CAPACITY. CPD_NO_CAPACITY also depends on the data: at
  * most 32768 guard-band rays are re-traced per call (about 0.8% of the rays at the
  * largest W and R), so a design with many rays near a decision threshold (near-critical
- * exit faces) can exceed it at sizes within the limits; the allocating entry points grow
- * their queue instead. Every call on a device shares the array, which keeps the previous
+ * exit faces) can exceed it at sizes within the limits, and CPD_TRACE_FP64, which
+ * re-traces every ray that clears the flat faces, needs W*R <= 32768; the allocating
+ * entry points grow their queue instead. Every call on a device shares the array, which keeps the previous
  * call's contents; each call clears what must start at zero. Calls that overlapped on the
  * GPU would race on the array: calls from threads of one process are therefore serialised
  * per device, and each returns only when its work is done. */
@@ -335,6 +336,12 @@ int cpd_last_transfer_bytes(cpd_context *ctx, uint64_t *h2d, uint64_t *d2h);
 /* FP32 FMA throughput probe: runs a dependent-chain-free FMA kernel for `iters`
  * iterations on every SM and returns the achieved TFLOP/s (roofline peak). */
 int cpd_measure_fp32_peak(cpd_context *ctx, uint32_t iters, double *tflops);
+
+/* SFU throughput probe: independent chains of the reciprocal-square-root estimate
+ * (the special-function unit that the trace's square roots and reciprocals use) on
+ * every SM for `iters` iterations; returns the achieved results per second, in G/s (the
+ * SFU roofline's peak). */
+int cpd_measure_sfu_peak(cpd_context *ctx, uint32_t iters, double *gops);
 
 /* ---------------------------------------------------------------- serving */
 

@@ -68,6 +68,9 @@ double orc_calc_n(const double coeffs[6], double w);
  * incremental R1 sequence state = fract(state + 1/phi) (src/spectrometer/qrng.rs:526-563). */
 void orc_qrng_points(double seed, size_t n, double *out);
 
+/* The GPU seed policy's points: u_i = fract(fma(first + i, 1/phi, seed)). */
+void orc_gpu_points(double seed, uint64_t first, size_t n, double *out);
+
 /* detector_array_positioning (src/spectrometer/spectrometer.rs:322-364). Uses
  * only the prism fields, the source fields and det_length/det_angle of `s`. */
 int orc_position_detector(const orc_spec *s, double acceptance, double pos_out[2],

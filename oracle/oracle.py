@@ -15,6 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
+OPS_LIB_PATH = os.path.join(HERE, "_build", "liborc_ops.so")
 
 MAX_GLASS = 6
 (OK, NO_SURFACE_INTERSECTION, OUT_OF_BOUNDS, TOTAL_INTERNAL_REFLECTION,
@@ -52,7 +53,8 @@ def _stale() -> bool:
     if not os.path.exists(LIB_PATH):
         return True
     t = os.path.getmtime(LIB_PATH)
-    return any(os.path.getmtime(os.path.join(HERE, f)) > t for f in ("cpd_oracle.c", "cpd_oracle.h", "build.sh"))
+    srcs = ("cpd_oracle.c", "cpd_oracle.h", "cpd_oracle_model.h", "ops_count.cpp", "build.sh")
+    return any(os.path.getmtime(os.path.join(HERE, f)) > t for f in srcs)
 
 
 def build(force: bool = False) -> str:
@@ -77,6 +79,7 @@ def lib():
         L.orc_calc_n.restype = C.c_double
         L.orc_calc_n.argtypes = [dp, C.c_double]
         L.orc_qrng_points.argtypes = [C.c_double, C.c_size_t, dp]
+        L.orc_gpu_points.argtypes = [C.c_double, C.c_uint64, C.c_size_t, dp]
         L.orc_position_detector.argtypes = [sp, C.c_double, dp, C.POINTER(C.c_int32)]
         L.orc_propagate.argtypes = [sp, C.c_double, C.c_double, up, dp]
         L.orc_design_dump.argtypes = [sp, dp]
@@ -138,6 +141,28 @@ def qrng_points(seed: float, n: int) -> np.ndarray:
     out = np.empty(n, dtype=np.float64)
     lib().orc_qrng_points(float(seed), n, _dp(out))
     return out
+
+
+def gpu_points(seed: float, n: int, first: int = 0) -> np.ndarray:
+    """The GPU seed policy's points u_i = fract(fma(first + i, 1/phi, seed))."""
+    out = np.empty(n, dtype=np.float64)
+    lib().orc_gpu_points(float(seed), int(first), n, _dp(out))
+    return out
+
+
+def accept_params(d: dict):
+    """A drawn design positioned by the oracle (acceptance 1.0), or None when it raises
+    RayTraceError or its tables are not finite: the same decision the library's builder
+    takes, so a seeded draw sequence gives the same designs on both sides."""
+    e, pos, fl = position_detector(d, 1.0)
+    if e != OK:
+        return None
+    dd = dict(d, det_position=pos, det_flipped=fl)
+    s = make_spec(dd)
+    out = np.zeros(4 * len(dd["glasses"]) + 6 + 5 + 2)
+    if lib().orc_design_dump(C.byref(s), _dp(out)) != OK or not np.isfinite(out).all():
+        return None
+    return dd
 
 
 def position_detector(d: dict, acceptance: float = 1.0):
@@ -244,3 +269,28 @@ def trace_pairs(d: dict, lam_u, ray_u):
                               bins.ctypes.data_as(C.POINTER(C.c_uint32)), _dp(ts))
     assert e == OK, e
     return bins, ts
+
+
+OP_KINDS = ("add", "mul", "fma", "div", "sqrt", "cmp", "log", "trig", "other")
+
+
+def ops_trace(d: dict, lam_u, ray_u):
+    """The op-counting build of the model (ops_count.cpp) over W x R rays: totals per
+    operation kind for the per-ray work, the per-wavelength work the reference repeats per
+    ray (calc_n), the rays that reached a bin, and the R start heights; plus the hits."""
+    build()
+    L = C.CDLL(OPS_LIB_PATH)
+    u64 = C.POINTER(C.c_uint64)
+    L.orc_ops_trace.argtypes = [C.POINTER(OrcSpec), C.POINTER(C.c_double), C.c_size_t, C.POINTER(C.c_double),
+                                C.c_size_t, u64, u64, u64, u64, u64]
+    assert L.orc_ops_kinds() == len(OP_KINDS)
+    s = make_spec(d)
+    lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
+    ray_u = np.ascontiguousarray(ray_u, dtype=np.float64)
+    bufs = [np.zeros(len(OP_KINDS), dtype=np.uint64) for _ in range(4)]
+    hits = C.c_uint64(0)
+    e = L.orc_ops_trace(C.byref(s), _dp(lam_u), lam_u.size, _dp(ray_u), ray_u.size,
+                        *[b.ctypes.data_as(u64) for b in bufs], C.byref(hits))
+    assert e == OK, e
+    names = ("ray", "lambda", "hit_ray", "beam")
+    return {n: dict(zip(OP_KINDS, (int(v) for v in b))) for n, b in zip(names, bufs)}, int(hits.value)

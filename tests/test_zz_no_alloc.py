@@ -54,7 +54,8 @@ def _cases(f1):
 @pytest.mark.parametrize("mode", [cpd.TRACE_HYBRID, cpd.TRACE_FP32, cpd.TRACE_FP64],
                          ids=["hybrid", "fp32", "fp64"])
 def test_static_entry_matches_allocating_entry_on_two_calls(f1, mode):
-    lam_u = O.qrng_points(0.5, 512)
+    # CPD_TRACE_FP64 re-traces every ray through the fixed 32768-entry queue: W R <= 32768
+    lam_u = O.qrng_points(0.5, 512 if mode != cpd.TRACE_FP64 else 24)
     ray_u = O.qrng_points(0.5, 1024)
     for spec in _cases(f1):
         ref, p_ref = spec.gpu_fitness_points(lam_u, ray_u, mode=mode, want_p=True)
@@ -114,3 +115,9 @@ def test_static_entry_rejects_sizes_beyond_its_array(f1):
     assert rc == N.NO_CAPACITY
     rc, _, _ = _static_call(spec, O.qrng_points(0.5, 16), O.qrng_points(0.5, 8192))
     assert rc == N.NO_CAPACITY
+    # every ray of the FP64 mode goes through the re-trace queue
+    rc, _, _ = _static_call(spec, O.qrng_points(0.5, 512), O.qrng_points(0.5, 1024), cpd.TRACE_FP64)
+    assert rc == N.NO_CAPACITY
+    # the array is still usable after a refused call
+    rc, _, _ = _static_call(spec, O.qrng_points(0.5, 16), O.qrng_points(0.5, 256))
+    assert rc == N.OK
