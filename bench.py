@@ -228,7 +228,8 @@ def oracle_check(cases, adaptive=False, nthreads=None):
         else:
             _, st = O.fitness_points(d, lam, ray_u, nthreads=nthreads, want_p=False)
             same = hits == st["hits"]
-        rel = abs(info - st["info"]) / max(abs(st["info"]), 1e-300)
+        # a design whose rays all miss the detector has MI 0 on both sides
+        rel = abs(info - st["info"]) / abs(st["info"]) if st["info"] != 0.0 else (0.0 if info == 0.0 else 1.0)
         worst = max(worst, rel)
         equal = equal and same
         rows.append({"W": W, "R": R, "G": len(d["glasses"]), "B": d["bin_count"], "rel_err": rel})

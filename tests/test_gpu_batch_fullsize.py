@@ -2,7 +2,8 @@
 16 designs of 6 prisms and 128 bins, 4096 wavelengths x 1024 rays each (the largest
 designs of the 1024-design population), in one batched pass, each on its own seed.
 Every design's MI must be within 1e-4 relative of the oracle's on the same points and its
-hit count equal; a sampled design's p(d|lambda) is compared through the single-design
+hit count equal (one of them reaches its detector with no ray: MI 0 on both sides); a
+sampled design's p(d|lambda) is compared through the single-design
 call (the batch gives each design the same bits as its single call)."""
 import os
 
@@ -28,9 +29,10 @@ def test_full_size_batch_equals_oracle():
     for (s, d), seed, f in zip(pairs, seeds, outs):
         lam, ray = O.gpu_points(seed, W), O.gpu_points(seed, R, first=1)
         _, st = O.fitness_points(d, lam, ray, nthreads=NTHREADS, want_p=False)
-        rel = abs(f.info - st["info"]) / abs(st["info"])
-        worst = max(worst, rel)
-        assert rel <= 1e-4, (seed, f.info, st["info"])
+        # a design may reach its detector with no ray at all (MI 0): the bound has a floor
+        assert abs(f.info - st["info"]) <= 1e-4 * abs(st["info"]) + 1e-12, (seed, f.info, st["info"])
+        if st["info"] != 0.0:
+            worst = max(worst, abs(f.info - st["info"]) / abs(st["info"]))
         assert f.hits == st["hits"], seed
         assert f.rays == W * R and f.wavelengths == W
     # p(d|lambda) of one design at full size through the single-design call
