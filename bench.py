@@ -277,8 +277,10 @@ def reference_adaptive_rate(d, max_n, max_m, nthreads, target_s=3.0):
             res = list(ex.map(lambda _: O.fitness_adaptive(d, max_n, max_m), range(nthreads * 4)))
             done += len(res)
     dt = time.perf_counter() - t0
+    _, _, _, n_w, n_r = O.fitness_adaptive_work(d, max_n, max_m)
     return {"value": done / dt, "unit": "designs/s", "cores": nthreads, "max_n": max_n, "max_m": max_m,
-            "info": res[0][1], "sample": f"{done} whole designs, one per thread, {dt:.2f} s",
+            "info": res[0][1], "wavelengths_used": n_w, "rays_traced": n_r,
+            "sample": f"{done} whole designs, one per thread, {dt:.2f} s",
             "note": "a different estimator: stops each wavelength at the first hit whose bin's SEM <= 5e-3 "
                     "and stops the wavelengths once every bin's SEM across them is <= 5e-3"}
 

@@ -152,6 +152,81 @@ constexpr size_t bin_state_bytes(uint32_t B) { return (size_t)B * (16 + 3 * 8 + 
 // (above the default 48 KB).
 cudaError_t configure_kernels();
 
+// ------------------------------------------------------------ device-resident serving loop
+//
+// A persistent kernel whose CTAs take designs from a ring in mapped host memory and
+// evaluate each one whole (setup, FP32 trace, re-trace of the guard bands and the flagged
+// rays, entropy, finalize) with no host step between designs. The host publishes records
+// and reads completions; nothing on the device waits for anything but new work, and that
+// wait gives up after an idle limit.
+
+// One design of the ring (mapped host memory), written by the host before it publishes
+// the index: the design, its job (W, R, Rz, B, tables' offsets in the table arena,
+// fixed-point units) and the trace mode.
+struct alignas(16) LoopWork {
+    DevDesign d;
+    DesignJob j;
+    uint32_t mode;
+    uint32_t ray_tile;
+    uint32_t pad[2];
+};
+
+// The result slot of a ring entry (mapped host memory): written by the CTA that evaluated
+// the entry, then `seq` = index + 1 after a system-scope fence.
+struct alignas(16) LoopDone {
+    DesignOut o;
+    unsigned long long seq;
+    uint32_t status;   // 0, or the design exceeded the CTA's queue (never: it re-traces inline)
+    uint32_t pad;
+};
+
+// Control words (mapped host memory).
+struct alignas(16) LoopCtl {
+    unsigned long long published;  // host: ring entries published (monotone)
+    unsigned int stop;             // host: exit once the ring is drained
+    unsigned int idle_exits;       // device: CTAs that left after the idle limit
+    unsigned int stop_exits;       // device: CTAs that left on `stop`
+    unsigned int pad;
+    unsigned long long designs;    // device: designs evaluated
+};
+
+struct LoopArgs {
+    const LoopWork *ring;         // capacity entries (mapped)
+    LoopDone *done;               // capacity entries (mapped)
+    LoopCtl *ctl;                 // mapped
+    unsigned long long *claimed;  // device: ring entries claimed by CTAs
+    uint32_t capacity;
+    uint32_t max_cells;           // histogram cells of a slab (W B)
+    uint32_t max_rows;            // wavelength rows of a slab
+    uint32_t qcap;                // flagged rays a slab's queue holds (more are re-traced inline)
+    unsigned char *slabs;         // per-CTA scratch, slab_bytes each
+    size_t slab_bytes;
+    const double *lam;            // table arena: wavelength u-points
+    const double *z64;            // table arena: sorted z, f64
+    const float *z32;             // table arena: sorted z, (hi, lo) float pairs
+    const float *logtab;
+    unsigned long long idle_ns;   // a CTA leaves after this long without work
+    struct LoopCounters *cnt;     // device
+    uint32_t max_B;               // widest detector a slab holds
+    uint32_t pad;
+};
+
+// Device-side counters of the loop kernel.
+struct LoopCounters {
+    unsigned long long claimed;     // ring entries claimed by CTAs
+    unsigned long long designs;     // designs evaluated
+    unsigned long long inline_retraced;  // flagged rays re-traced inline (the queue was full)
+    unsigned int idle_exits;        // CTAs that left after the idle limit
+    unsigned int stop_exits;        // CTAs that left on the host's stop word
+};
+
+// Bytes of one CTA's slab for designs of up to max_rows rows and max_cells cells.
+size_t loop_slab_bytes(uint32_t max_rows, uint32_t max_cells, uint32_t max_B, uint32_t qcap);
+// Launches the loop kernel with `grid` CTAs on `stream`.
+void launch_loop(const LoopArgs &a, uint32_t grid, cudaStream_t stream);
+// CTAs of the loop kernel resident per SM.
+int loop_ctas_per_sm();
+
 // Launches setup -> trace -> retrace -> entropy -> finalize on `stream` (adaptive
 // sampling: setup -> adaptive rounds -> exact rounds of the unsure rows -> entropy ->
 // finalize). Returns the

@@ -1204,6 +1204,321 @@ __global__ void mufu_peak_kernel(float *out, uint32_t iters)
     if (s == 12345.0f) out[blockIdx.x] = s;  // keeps the chains live
 }
 
+// ------------------------------------------------------------------ device-resident loop
+//
+// One CTA evaluates one design at a time, start to finish, with the pass's device code:
+// lambda_setup_df per wavelength row, fast_ray over the core rays (lane = wavelength, items
+// of 32 rows x a ray chunk claimed from a shared counter), trace_df for the guard-band rays
+// of every row and the rays fast_ray flagged, entropy_cell over the W x B cells, then
+// finalize_design. Every sum is the same integer as in the pass, so a design's result is
+// bitwise its batched result. The CTA then claims the next published ring entry.
+
+constexpr uint32_t kLoopThreads = 256;
+#ifndef CPD_LOOP_MIN_BLOCKS
+#define CPD_LOOP_MIN_BLOCKS 3
+#endif
+
+struct SlabLayout {
+    size_t hist, lp, lx, queue, s1, s2, acc, bytes;
+};
+
+__host__ __device__ inline SlabLayout slab_layout(uint32_t rows, uint32_t cells, uint32_t maxB, uint32_t qcap)
+{
+    SlabLayout L;
+    size_t o = 0;
+    L.hist = o;
+    o += (8 * (size_t)cells + 255) & ~size_t(255);
+    L.lp = o;
+    o += (sizeof(LamParams) * (size_t)rows + 255) & ~size_t(255);
+    L.lx = o;
+    o += (sizeof(LamDF) * (size_t)rows + 255) & ~size_t(255);
+    L.queue = o;
+    o += (sizeof(QEntry) * (size_t)qcap + 255) & ~size_t(255);
+    L.s1 = o;
+    o += (8 * (size_t)maxB + 255) & ~size_t(255);
+    L.s2 = o;
+    o += (8 * (size_t)maxB + 255) & ~size_t(255);
+    L.acc = o;
+    o += (sizeof(DesignAcc) + 255) & ~size_t(255);
+    L.bytes = o;
+    return L;
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned long long load_acquire_sys(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void store_release_sys(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// The float-float re-trace of one ray into the CTA's histogram; returns 1 on a hit.
+__device__ __noinline__ uint32_t loop_retrace(const DevDesign &D, const LamDF &E, const float *z32, uint32_t j,
+                                              unsigned long long *hrow)
+{
+    uint32_t bin = 0;
+    float t = 0.f;
+    if (trace_df(D, E, z32[2 * j], z32[2 * j + 1], bin, t)) {
+        atomicAdd(hrow + bin, (unsigned long long)t_fixed(t));
+        return 1u;
+    }
+    return 0u;
+}
+
+__global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel(const LoopArgs L)
+{
+    __shared__ __align__(16) DevDesign sD;
+    __shared__ __align__(16) DesignJob sJ;
+    __shared__ float tab[4 * ff::kLogTable];
+    __shared__ FinalizeRed fin_red[kLoopThreads / 32];
+    __shared__ unsigned long long s_idx, s_hits, s_retraced, s_fast, s_H, s_inline;
+    __shared__ uint32_t s_item, s_qn;
+    extern __shared__ __align__(16) unsigned long long loop_smem[];  // per-bin s1, s2 (max_B each)
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5, nwarps = blockDim.x >> 5;
+    for (uint32_t i = t; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = L.logtab[i];
+    const SlabLayout SL = slab_layout(L.max_rows, L.max_cells, L.max_B, L.qcap);
+    unsigned char *slab = L.slabs + (size_t)blockIdx.x * L.slab_bytes;
+    unsigned long long *hist = reinterpret_cast<unsigned long long *>(slab + SL.hist);
+    LamParams *lp = reinterpret_cast<LamParams *>(slab + SL.lp);
+    LamDF *lx = reinterpret_cast<LamDF *>(slab + SL.lx);
+    QEntry *queue = reinterpret_cast<QEntry *>(slab + SL.queue);
+    unsigned long long *S1 = reinterpret_cast<unsigned long long *>(slab + SL.s1);
+    unsigned long long *S2 = reinterpret_cast<unsigned long long *>(slab + SL.s2);
+    DesignAcc *acc = reinterpret_cast<DesignAcc *>(slab + SL.acc);
+    unsigned long long *s1 = loop_smem, *s2 = loop_smem + L.max_B;
+    const Guards guards = default_guards();
+    // the idle wait: bounded in time and in polls (a poll sleeps about a microsecond)
+    const unsigned long long max_polls = L.idle_ns / 500ull + 1000ull;
+    unsigned long long idle_start = global_ns();
+    for (;;) {
+        // ---- claim the next published ring entry, or leave after the idle limit
+        if (t == 0) {
+            unsigned long long got = ~0ull;
+            for (unsigned long long polls = 0;; polls++) {
+                const unsigned long long pub = load_acquire_sys(&L.ctl->published);
+                const unsigned long long n = *reinterpret_cast<volatile unsigned long long *>(&L.cnt->claimed);
+                if (n < pub) {
+                    if (atomicCAS(&L.cnt->claimed, n, n + 1ull) == n) {
+                        got = n;
+                        break;
+                    }
+                    continue;
+                }
+                if (*reinterpret_cast<volatile unsigned int *>(&L.ctl->stop)) {
+                    atomicAdd(&L.cnt->stop_exits, 1u);
+                    break;
+                }
+                if (polls >= max_polls || global_ns() - idle_start > L.idle_ns) {
+                    atomicAdd(&L.cnt->idle_exits, 1u);
+                    break;
+                }
+                __nanosleep(1000);
+            }
+            s_idx = got;
+            s_item = 0u;
+            s_qn = 0u;
+            s_hits = s_retraced = s_fast = s_H = s_inline = 0ull;
+        }
+        __syncthreads();
+        const unsigned long long idx = s_idx;
+        if (idx == ~0ull) break;
+        const uint32_t slot = (uint32_t)(idx % L.capacity);
+        {
+            // the record (after thread 0's acquire of `published` and the barrier)
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(&L.ring[slot].d);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&sD);
+            for (uint32_t i = t; i < sizeof(DevDesign) / 4; i += blockDim.x) dst[i] = src[i];
+            const uint32_t *srcj = reinterpret_cast<const uint32_t *>(&L.ring[slot].j);
+            uint32_t *dstj = reinterpret_cast<uint32_t *>(&sJ);
+            for (uint32_t i = t; i < sizeof(DesignJob) / 4; i += blockDim.x) dstj[i] = srcj[i];
+        }
+        const uint32_t ray_tile = L.ring[slot].ray_tile;
+        unsigned long long *accw = reinterpret_cast<unsigned long long *>(acc);
+        for (uint32_t i = t; i < sizeof(DesignAcc) / 8; i += blockDim.x) accw[i] = 0ull;
+        __syncthreads();
+        const uint32_t W = sJ.W, B = sJ.B, Rz = sJ.Rz;
+        const float *z32 = L.z32 + 2 * sJ.ray_off;
+        for (uint32_t b = t; b < B; b += blockDim.x) s1[b] = s2[b] = 0ull;
+
+        // ---- per-wavelength setup
+        for (uint32_t k = t; k < W; k += blockDim.x) {
+            LamParams P;
+            lambda_setup_df(sD, L.lam[sJ.lam_off + k], z32, Rz, P, kYGuardRel, lx + k, false);
+            if (P.all_exact) {
+                // no reference ray: every ray of the band is re-traced
+                P.core_lo = P.core_hi = 0;
+            }
+            lp[k] = P;
+        }
+        __syncthreads();
+
+        // ---- FP32 trace of the core rays
+        {
+            const uint32_t nblk = (W + 31u) / 32u;
+            const uint32_t nchunk = Rz ? (Rz + ray_tile - 1u) / ray_tile : 1u;
+            const uint32_t total = nblk * nchunk;
+            const FastConst &C = sD.fc;
+            for (;;) {
+                uint32_t item = 0;
+                if (lane == 0) item = atomicAdd(&s_item, 1u);
+                item = __shfl_sync(0xffffffffu, item, 0);
+                if (item >= total) break;
+                const uint32_t blk = item / nchunk, chunk = item - blk * nchunk;
+                const uint32_t k = blk * 32u + lane;
+                LamParams P;
+                uint32_t lo = 0, hi = 0;
+                if (k < W) {
+                    P = lp[k];
+                    const uint32_t j0 = chunk * ray_tile;
+                    const uint32_t j1 = min(j0 + ray_tile, Rz);
+                    lo = max(j0, P.core_lo);
+                    hi = min(j1, P.core_hi);
+                }
+                const float2 *__restrict__ zt = reinterpret_cast<const float2 *>(z32);
+                unsigned long long *hrow = hist + (uint64_t)k * B;
+                uint32_t cur = 0xffffffffu;
+                unsigned long long sum = 0ull;
+                uint32_t nhit = 0, ninl = 0;
+                for (uint32_t j = lo; j < hi; ++j) {
+                    const float2 z = __ldg(zt + j);
+                    uint32_t bin = 0;
+                    float tt = 0.f;
+                    const int r = fast_ray(C, P, guards, z.x, z.y, bin, tt);
+                    if (r == RAY_HIT) {
+                        if (bin != cur) {
+                            if (sum) atomicAdd(hrow + cur, sum);
+                            cur = bin;
+                            sum = 0ull;
+                        }
+                        sum += t_fixed(tt);
+                        nhit++;
+                    } else if (r == RAY_FLAG) {
+                        const uint32_t pos = atomicAdd(&s_qn, 1u);
+                        if (pos < L.qcap) {
+                            queue[pos] = QEntry{0u, k, j, 0u};
+                        } else {
+                            // the queue is full: re-trace here (counted as re-traced, as queued)
+                            nhit += loop_retrace(sD, lx[k], z32, j, hrow);
+                            ninl++;
+                        }
+                    }
+                }
+                if (sum) atomicAdd(hrow + cur, sum);
+                nhit = __reduce_add_sync(0xffffffffu, nhit);
+                ninl = __reduce_add_sync(0xffffffffu, ninl);
+                const uint32_t nfast = __reduce_add_sync(0xffffffffu, hi > lo ? hi - lo : 0u);
+                if (lane == 0) {
+                    if (nhit) atomicAdd(&s_hits, (unsigned long long)nhit);
+                    if (nfast) atomicAdd(&s_fast, (unsigned long long)nfast);
+                    if (ninl) {
+                        atomicAdd(&s_retraced, (unsigned long long)ninl);
+                        atomicAdd(&s_inline, (unsigned long long)ninl);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---- float-float re-trace: each row's guard bands (a warp per row), then the queue
+        {
+            unsigned long long hits = 0ull, ret = 0ull;
+            for (uint32_t k = warp; k < W; k += nwarps) {
+                const LamParams &P = lp[k];
+                const uint32_t a0 = P.band_lo, a1 = P.all_exact ? P.band_hi : P.core_lo;
+                const uint32_t b0 = P.all_exact ? P.band_hi : P.core_hi, b1 = P.band_hi;
+                unsigned long long *hrow = hist + (uint64_t)k * B;
+                const uint32_t na = a1 > a0 ? a1 - a0 : 0u, nb = b1 > b0 ? b1 - b0 : 0u;
+                for (uint32_t i = lane; i < na + nb; i += 32u) {
+                    const uint32_t j = i < na ? a0 + i : b0 + (i - na);
+                    hits += loop_retrace(sD, lx[k], z32, j, hrow);
+                    ret++;
+                }
+            }
+            const uint32_t qn = min(s_qn, L.qcap);
+            for (uint32_t i = t; i < qn; i += blockDim.x) {
+                const QEntry e = queue[i];
+                hits += loop_retrace(sD, lx[e.k], z32, e.j, hist + (uint64_t)e.k * B);
+                ret++;
+            }
+            hits = warp_sum_u64(hits);
+            ret = warp_sum_u64(ret);
+            if (lane == 0) {
+                if (hits) atomicAdd(&s_hits, hits);
+                if (ret) atomicAdd(&s_retraced, ret);
+            }
+        }
+        __syncthreads();
+
+        // ---- entropy over the W x B cells; each nonzero cell is cleared for the next design
+        {
+            const ff::F2 unit{sJ.unit_hi, sJ.unit_lo}, lu{sJ.lu_hi, sJ.lu_lo};
+            const uint32_t cells = W * B;
+            unsigned long long hl = 0ull;
+            for (uint32_t i = t; i < cells; i += blockDim.x) {
+                const unsigned long long cv = hist[i];
+                if (cv) {
+                    hist[i] = 0ull;
+                    unsigned long long hq, pq;
+                    entropy_cell(cv, unit, lu, tab, hq, pq);
+                    hl += hq;
+                    const uint32_t b = i % B;
+                    atomicAdd(s1 + b, cv);
+                    atomicAdd(s2 + b, pq);
+                }
+            }
+            hl = warp_sum_u64(hl);
+            if (lane == 0 && hl) atomicAdd(&s_H, hl);
+        }
+        __syncthreads();
+        for (uint32_t b = t; b < B; b += blockDim.x) {
+            S1[b] = s1[b];
+            S2[b] = s2[b];
+        }
+        if (t == 0) {
+            acc->H = s_H;
+            acc->rows = 0ull;
+            acc->hits[0] = s_hits;
+            acc->retraced[0] = s_retraced;
+            acc->fast[0] = s_fast;
+            if (s_inline) atomicAdd(&L.cnt->inline_retraced, s_inline);
+        }
+        __syncthreads();
+
+        // ---- finalize into the ring entry's result slot (mapped host memory)
+        {
+            LaunchArgs a;
+            memset(&a, 0, sizeof(a));
+            a.designs = &sD;
+            a.acc = acc;
+            a.S1 = S1;
+            a.S2 = S2;
+            a.out = &L.done[slot].o;
+            DesignJob J = sJ;
+            J.acc_off = 0;
+            finalize_design(a, 0u, J, t, blockDim.x, tab, fin_red);
+        }
+        __syncthreads();
+        if (t == 0) {
+            L.done[slot].status = 0u;
+            __threadfence_system();
+            store_release_sys(&L.done[slot].seq, idx + 1ull);
+            atomicAdd(&L.cnt->designs, 1ull);
+        }
+        idle_start = global_ns();
+    }
+}
+
 }  // namespace
 
 // A launch that, with `pdl`, may start before the previous kernel on the stream has
@@ -1349,6 +1664,24 @@ void launch_tp_adaptive(const DevDesign *d, uint32_t B, const double *lambdas, u
 void launch_mufu_peak(float *out, uint32_t iters, int blocks, int threads, cudaStream_t stream)
 {
     mufu_peak_kernel<<<blocks, threads, 0, stream>>>(out, iters);
+}
+
+size_t loop_slab_bytes(uint32_t max_rows, uint32_t max_cells, uint32_t max_B, uint32_t qcap)
+{
+    return slab_layout(max_rows, max_cells, max_B, qcap).bytes;
+}
+
+void launch_loop(const LoopArgs &a, uint32_t grid, cudaStream_t stream)
+{
+    loop_kernel<<<grid, kLoopThreads, 2 * sizeof(unsigned long long) * a.max_B, stream>>>(a);
+}
+
+int loop_ctas_per_sm()
+{
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, loop_kernel, kLoopThreads,
+                                                  2 * sizeof(unsigned long long) * CPD_MAX_BINS);
+    return per_sm < 1 ? 1 : per_sm;
 }
 
 void launch_fma_peak(float *out, uint32_t iters, int blocks, int threads, cudaStream_t stream)

@@ -12,7 +12,7 @@ flags=(-std=c11 -O3 -ffp-contract=off -fno-fast-math -fPIC -shared -pthread)
 if [ "$(uname -m)" = "aarch64" ] && echo 'int main(void){return 0;}' | gcc -mcpu=neoverse-v2 -x c - -o /dev/null 2>/dev/null; then
     flags+=(-mcpu=neoverse-v2)
 fi
-gcc "${flags[@]}" -o "$here/_build/liborc.so.tmp" "$here/cpd_oracle.c" -lm
+gcc "${flags[@]}" -o "$here/_build/liborc.so.tmp" "$here/cpd_oracle.c" "$here/cpd_oracle_toric.c" -lm
 mv "$here/_build/liborc.so.tmp" "$here/_build/liborc.so"
 # the op-counting build of the same model (the frozen per-ray operation table)
 g++ -std=c++17 -O2 -ffp-contract=off -fno-fast-math -fPIC -shared -Wno-class-memaccess \

@@ -49,36 +49,6 @@ void orc_gpu_points(double seed, uint64_t first, size_t n, double *out)
     for (size_t i = 0; i < n; i++) out[i] = fractd(fma((double)(first + i), ORC_ALPHA, seed));
 }
 
-/* Welford, src/spectrometer/welford.rs:5-57. */
-typedef struct { double count, mean, m2; } welford;
-
-static void wf_next(welford *w, double x)
-{
-    w->count += 1.0;
-    double delta = x - w->mean;
-    w->mean += delta / w->count;
-    double delta2 = x - w->mean;
-    w->m2 += delta * delta2;
-}
-
-static void wf_skip(welford *w, double new_count)
-{
-    if (w->count < new_count) {
-        double zero_count = new_count - w->count;
-        double count = new_count;
-        w->mean = (w->count * w->mean) / count;
-        w->m2 += sqr(w->mean) * w->count * zero_count / count;
-        w->count = count;
-    }
-}
-
-static int wf_sem_le(const welford *w, double err2)
-{
-    return w->m2 < err2 * (w->count * (w->count - 1.0));
-}
-
-/* FloatExt::plog2p, src/spectrometer/utils.rs:196-202. */
-static double plog2p(double p) { return p > 0.0 ? p * log2(p) : 0.0; }
 
 int orc_position_detector(const orc_spec *s, double acceptance, double pos_out[2], int32_t *flipped_out)
 {
@@ -250,6 +220,13 @@ int orc_p_dets_l_wavelength(const orc_spec *s, double wavelength, size_t max_m, 
 /* mutual_information + fitness (fitness.rs:79-147). */
 int orc_fitness_adaptive(const orc_spec *s, size_t max_n, size_t max_m, double out[3])
 {
+    return orc_fitness_adaptive_work(s, max_n, max_m, out, NULL, NULL);
+}
+
+int orc_fitness_adaptive_work(const orc_spec *s, size_t max_n, size_t max_m, double out[3], uint64_t *wavelengths_out,
+                              uint64_t *rays_out)
+{
+    uint64_t n_w = 0, n_r = 0;
     spectrometer sp;
     int e = build_spectrometer(s, &sp);
     if (e) return e;
@@ -267,7 +244,8 @@ int orc_fitness_adaptive(const orc_spec *s, size_t max_n, size_t max_m, double o
     for (size_t it = 0; it < max_n; it++) {
         st = fractd(st + ORC_ALPHA);
         double w = sample_wavelength(&sp, st);
-        p_dets_adaptive(&sp, w, max_m, row);
+        n_r += p_dets_adaptive(&sp, w, max_m, row);
+        n_w++;
         double h = 0.0;
         for (uint32_t i = 0; i < nbin; i++) {
             wf_next(&p_dets[i], row[i].mean);
@@ -289,6 +267,8 @@ int orc_fitness_adaptive(const orc_spec *s, size_t max_n, size_t max_m, double o
     out[0] = size;
     out[1] = h_det_l_w.mean - h_det;
     out[2] = dev;
+    if (wavelengths_out) *wavelengths_out = n_w;
+    if (rays_out) *rays_out = n_r;
     free(p_dets);
     free(row);
     return ORC_OK;

@@ -94,6 +94,10 @@ int orc_propagation_path(const orc_spec *s, double wavelength, double initial_y,
 /* fitness() (src/fitness.rs:130-147) with the reference's adaptive SEM stops.
  * out = {size, info, deviation}. */
 int orc_fitness_adaptive(const orc_spec *s, size_t max_n, size_t max_m, double out[3]);
+/* The same, also writing the wavelengths the outer SEM stop let through and the rays
+ * traced over them (the work the reference's estimator did). */
+int orc_fitness_adaptive_work(const orc_spec *s, size_t max_n, size_t max_m, double out[3], uint64_t *wavelengths_out,
+                              uint64_t *rays_out);
 
 /* p_dets_l_wavelength (src/fitness.rs:48-69) for one wavelength: writes bin_count means. */
 int orc_p_dets_l_wavelength(const orc_spec *s, double wavelength, size_t max_m, double *out);
@@ -125,6 +129,37 @@ int orc_fitness_adaptive_points(const orc_spec *s, const double *lam_u, size_t W
  * lambda = wmin + (wmax-wmin)*lam_u[i]; bin_count marks a lost ray. */
 int orc_trace_pairs(const orc_spec *s, const double *lam_u, const double *ray_u, size_t n,
                     uint32_t *bins, double *ts);
+
+/* ------------------------------------------------ 3-D: fiber beam, toric lenses
+ * (cpd_oracle_toric.c). The reference's Dim3 spectrometer: FiberBeam
+ * (src/spectrometer/spectrometer.rs:75-125), CulminatingToricCompoundPrism
+ * (src/spectrometer/ray.rs:112-118, toric.rs:204-262), the 3-D linear detector. */
+typedef struct orc_spec3 {
+    orc_spec base;          /* prism, detector and wavelength fields; base.curvature and the
+                               beam fields are unused */
+    double curv0[2];        /* first toric lens: signed normalized poloidal curvature,
+                               normalized toroidal curvature */
+    double curv1[2];        /* last toric lens */
+    double fiber_radius, fiber_na, fiber_center_y;
+} orc_spec3;
+
+/* approx_cbrt (src/spectrometer/cbrt.rs:49-68). */
+double orc_approx_cbrt(double x);
+/* sympy_soln (src/spectrometer/toric.rs:41-141): roots[0..3] of the ray-torus quartic. */
+void orc_toric_roots(double r_2, double R_2, double dp_magn_sq, double dp_v, double dp_n, double n_v,
+                     double roots[4]);
+/* Qrng<[f64; 4]> from [seed; 4] (qrng.rs:157-255): n points, out[4 i + k]. */
+void orc3_qrng_points(double seed, size_t n, double *out);
+/* detector_array_positioning (spectrometer.rs:322-364) for the 3-D spectrometer. */
+int orc3_position_detector(const orc_spec3 *s, double acceptance, double pos_out[2], int32_t *flipped_out);
+/* One ray per (lam_u[i], q[4 i .. 4 i + 3]): bins[i] (bin_count when lost), ts[i], and optionally
+ * the RayTraceError code, the NaN roots met at the toric faces and the toric faces reached. */
+int orc3_trace_pairs(const orc_spec3 *s, const double *lam_u, const double *q, size_t n, uint32_t *bins,
+                     double *ts, int32_t *status, uint32_t *nan_roots, uint32_t *toric_calls);
+/* Fixed-N estimator on explicit points (W wavelength u-points, R 4-D ray points), as
+ * orc_fitness_points; stats[3] = size. */
+int orc3_fitness_points(const orc_spec3 *s, const double *lam_u, size_t W, const double *q, size_t R,
+                        double *p_out, double stats[4], uint64_t *hits_out);
 
 #ifdef __cplusplus
 }

@@ -83,6 +83,37 @@ static real calc_n_r(const real *c, real w)
     return s;
 }
 
+/* Welford, src/spectrometer/welford.rs:5-57. */
+typedef struct { real count, mean, m2; } welford;
+
+static void wf_next(welford *w, real x)
+{
+    w->count += 1.0;
+    real delta = x - w->mean;
+    w->mean += delta / w->count;
+    real delta2 = x - w->mean;
+    w->m2 += delta * delta2;
+}
+
+static void wf_skip(welford *w, real new_count)
+{
+    if (w->count < new_count) {
+        real zero_count = new_count - w->count;
+        real count = new_count;
+        w->mean = (w->count * w->mean) / count;
+        w->m2 += sqr(w->mean) * w->count * zero_count / count;
+        w->count = count;
+    }
+}
+
+static int wf_sem_le(const welford *w, real err2)
+{
+    return w->m2 < err2 * (w->count * (w->count - 1.0));
+}
+
+/* FloatExt::plog2p, src/spectrometer/utils.rs:196-202. */
+static real plog2p(real p) { return p > 0.0 ? p * log2(p) : 0.0; }
+
 /* FloatExt::euclid_div_rem, utils.rs:177-192. */
 static void euclid_div_rem(real a, real b, real *q, real *r)
 {

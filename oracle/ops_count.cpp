@@ -47,6 +47,7 @@ inline bool operator!=(Cnt a, Cnt b) { tick(CMP); return a.v != b.v; }
 inline Cnt fma(Cnt a, Cnt b, Cnt c) { tick(FMA); return Cnt(std::fma(a.v, b.v, c.v)); }
 inline Cnt sqrt(Cnt a) { tick(SQRT); return Cnt(std::sqrt(a.v)); }
 inline Cnt log(Cnt a) { tick(LOG); return Cnt(std::log(a.v)); }
+inline Cnt log2(Cnt a) { tick(LOG); return Cnt(std::log2(a.v)); }
 inline Cnt cos(Cnt a) { tick(TRIG); return Cnt(std::cos(a.v)); }
 inline Cnt sin(Cnt a) { tick(TRIG); return Cnt(std::sin(a.v)); }
 inline Cnt fabs(Cnt a) { tick(OTHER); return Cnt(std::fabs(a.v)); }
@@ -60,6 +61,7 @@ using orc_ops::copysign;
 using orc_ops::fabs;
 using orc_ops::fma;
 using orc_ops::log;
+using orc_ops::log2;
 using orc_ops::signbit;
 using orc_ops::sin;
 using orc_ops::sqrt;

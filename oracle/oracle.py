@@ -53,7 +53,7 @@ def _stale() -> bool:
     if not os.path.exists(LIB_PATH):
         return True
     t = os.path.getmtime(LIB_PATH)
-    srcs = ("cpd_oracle.c", "cpd_oracle.h", "cpd_oracle_model.h", "ops_count.cpp", "build.sh")
+    srcs = ("cpd_oracle.c", "cpd_oracle_toric.c", "cpd_oracle.h", "cpd_oracle_model.h", "ops_count.cpp", "build.sh")
     return any(os.path.getmtime(os.path.join(HERE, f)) > t for f in srcs)
 
 
@@ -85,6 +85,8 @@ def lib():
         L.orc_design_dump.argtypes = [sp, dp]
         L.orc_propagation_path.argtypes = [sp, C.c_double, C.c_double, dp]
         L.orc_fitness_adaptive.argtypes = [sp, C.c_size_t, C.c_size_t, dp]
+        L.orc_fitness_adaptive_work.argtypes = [sp, C.c_size_t, C.c_size_t, dp, C.POINTER(C.c_uint64),
+                                                C.POINTER(C.c_uint64)]
         L.orc_p_dets_l_wavelength.argtypes = [sp, C.c_double, C.c_size_t, dp]
         L.orc_p_dets_l_wavelength_count.argtypes = [sp, C.c_double, C.c_size_t, dp, C.POINTER(C.c_uint64)]
         L.orc_fitness_points.argtypes = [sp, dp, C.c_size_t, dp, C.c_size_t, C.c_int, dp, dp,
@@ -206,6 +208,16 @@ def fitness_adaptive(d: dict, max_n: int = 16384, max_m: int = 16384):
     return float(out[0]), float(out[1]), float(out[2])
 
 
+def fitness_adaptive_work(d: dict, max_n: int = 16384, max_m: int = 16384):
+    """(size, info, deviation, wavelengths used, rays traced) of the reference CPU fitness."""
+    s = make_spec(d)
+    out = np.zeros(3)
+    nw, nr = C.c_uint64(0), C.c_uint64(0)
+    e = lib().orc_fitness_adaptive_work(C.byref(s), max_n, max_m, _dp(out), C.byref(nw), C.byref(nr))
+    assert e == OK, e
+    return float(out[0]), float(out[1]), float(out[2]), int(nw.value), int(nr.value)
+
+
 def p_dets_l_wavelength(d: dict, wavelength: float, max_m: int = 16384) -> np.ndarray:
     s = make_spec(d)
     out = np.zeros(int(d["bin_count"]))
@@ -294,3 +306,99 @@ def ops_trace(d: dict, lam_u, ray_u):
     assert e == OK, e
     names = ("ray", "lambda", "hit_ray", "beam")
     return {n: dict(zip(OP_KINDS, (int(v) for v in b))) for n, b in zip(names, bufs)}, int(hits.value)
+
+
+class OrcSpec3(C.Structure):
+    _fields_ = [("base", OrcSpec), ("curv0", C.c_double * 2), ("curv1", C.c_double * 2),
+                ("fiber_radius", C.c_double), ("fiber_na", C.c_double), ("fiber_center_y", C.c_double)]
+
+
+def make_spec3(d: dict) -> OrcSpec3:
+    """The 3-D spectrometer: the flat dict of make_spec plus curv0 / curv1 (poloidal, toroidal)
+    and fiber_radius / fiber_na / fiber_center_y."""
+    s = OrcSpec3()
+    base = dict(d)
+    base.setdefault("curvature", 0.0)
+    base.setdefault("beam_width", 0.0)
+    base.setdefault("beam_y_mean", d["fiber_center_y"])
+    s.base = make_spec(base)
+    s.curv0[0], s.curv0[1] = (float(v) for v in d["curv0"])
+    s.curv1[0], s.curv1[1] = (float(v) for v in d["curv1"])
+    s.fiber_radius = float(d["fiber_radius"])
+    s.fiber_na = float(d["fiber_na"])
+    s.fiber_center_y = float(d["fiber_center_y"])
+    return s
+
+
+def _lib3():
+    L = lib()
+    if not getattr(L, "_orc3", False):
+        sp3 = C.POINTER(OrcSpec3)
+        dp = C.POINTER(C.c_double)
+        up = C.POINTER(C.c_uint32)
+        L.orc_approx_cbrt.restype = C.c_double
+        L.orc_approx_cbrt.argtypes = [C.c_double]
+        L.orc_toric_roots.argtypes = [C.c_double] * 6 + [dp]
+        L.orc3_qrng_points.argtypes = [C.c_double, C.c_size_t, dp]
+        L.orc3_position_detector.argtypes = [sp3, C.c_double, dp, C.POINTER(C.c_int32)]
+        L.orc3_trace_pairs.argtypes = [sp3, dp, dp, C.c_size_t, up, dp, C.POINTER(C.c_int32), up, up]
+        L.orc3_fitness_points.argtypes = [sp3, dp, C.c_size_t, dp, C.c_size_t, dp, dp, C.POINTER(C.c_uint64)]
+        L._orc3 = True
+    return L
+
+
+def approx_cbrt(x: float) -> float:
+    return _lib3().orc_approx_cbrt(float(x))
+
+
+def toric_roots(r_2, R_2, dp_magn_sq, dp_v, dp_n, n_v) -> np.ndarray:
+    out = np.zeros(4)
+    _lib3().orc_toric_roots(r_2, R_2, dp_magn_sq, dp_v, dp_n, n_v, _dp(out))
+    return out
+
+
+def qrng3_points(seed: float, n: int) -> np.ndarray:
+    out = np.zeros((n, 4))
+    _lib3().orc3_qrng_points(float(seed), n, _dp(out))
+    return out
+
+
+def position_detector3(d: dict, acceptance: float = 1.0):
+    s = make_spec3(d)
+    pos = np.zeros(2)
+    fl = C.c_int32(0)
+    e = _lib3().orc3_position_detector(C.byref(s), float(acceptance), _dp(pos), C.byref(fl))
+    return e, (float(pos[0]), float(pos[1])), bool(fl.value)
+
+
+def trace_pairs3(d: dict, lam_u, q):
+    """(bins, ts, status, nan_roots, toric_calls) per (lam_u[i], q[i]) ray."""
+    s = make_spec3(d)
+    lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 4)
+    n = lam_u.size
+    bins = np.zeros(n, dtype=np.uint32)
+    ts = np.zeros(n)
+    st = np.zeros(n, dtype=np.int32)
+    nan = np.zeros(n, dtype=np.uint32)
+    calls = np.zeros(n, dtype=np.uint32)
+    u32 = C.POINTER(C.c_uint32)
+    e = _lib3().orc3_trace_pairs(C.byref(s), _dp(lam_u), _dp(q), n, bins.ctypes.data_as(u32), _dp(ts),
+                                 st.ctypes.data_as(C.POINTER(C.c_int32)), nan.ctypes.data_as(u32),
+                                 calls.ctypes.data_as(u32))
+    assert e == OK, e
+    return bins, ts, st, nan, calls
+
+
+def fitness_points3(d: dict, lam_u, q):
+    s = make_spec3(d)
+    lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 4)
+    W, R, B = lam_u.size, q.shape[0], int(d["bin_count"])
+    p = np.zeros((W, B))
+    st = np.zeros(4)
+    hits = C.c_uint64(0)
+    e = _lib3().orc3_fitness_points(C.byref(s), _dp(lam_u), W, _dp(q), R, _dp(p), _dp(st), C.byref(hits))
+    assert e == OK, e
+    return p, {"info": float(st[0]), "h_cond": float(st[1]), "h_det": float(st[2]), "size": float(st[3]),
+               "hits": int(hits.value)}

@@ -72,7 +72,7 @@ def test_static_entry_without_p_output(f1):
     spec = _cases(f1)[1]
     lam_u = O.qrng_points(0.5, 256)
     ray_u = O.qrng_points(0.5, 2048)
-    ref = spec.gpu_fitness_points(lam_u, ray_u)
+    ref, _ = spec.gpu_fitness_points(lam_u, ray_u)
     for _ in range(2):
         rc, f, _ = _static_call(spec, lam_u, ray_u, want_p=False)
         assert rc == N.OK, N.status_string(rc)
