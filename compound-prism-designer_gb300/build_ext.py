@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcpd.so")
-SOURCES = ["cpd_kernels.cu", "cpd_runtime.cu", "cpd_host.cpp", "cpd_static.cu"]
+SOURCES = ["cpd_kernels.cu", "cpd_runtime.cu", "cpd_host.cpp", "cpd_static.cu", "cpd_loop.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
           "-I", os.path.join(HERE, "..", "include")]

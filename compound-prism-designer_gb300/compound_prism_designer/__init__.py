@@ -649,6 +649,82 @@ def _design_array(designs) -> np.ndarray:
     return np.frombuffer(_pack_designs(designs), dtype=N.DESIGN_DTYPE)
 
 
+class LoopServer:
+    """The device-resident serving loop (cpd_loop_*, no reference counterpart).
+
+    One persistent kernel; each CTA owns a histogram slab and evaluates whole designs
+    taken from a ring in mapped host memory, with no host step between designs. A design
+    is admitted when its W x B cells fit a slab (max_cells, max_rows); the GPU memory for
+    histograms is hist_budget_bytes. Fixed N with the hybrid trace. The methods are
+    those of Server; each design's result is bitwise the one it gets alone."""
+
+    def __init__(self, hist_budget_bytes: int = 4 << 30, *, max_cells: int = 0, max_rows: int = 0,
+                 ring_capacity: int = 0, ctas_per_sm: int = 0, idle_ms: int = 0, ray_tile: int = 0,
+                 context: Optional[Context] = None):
+        self._ctx = context or default_context()
+        cfg = N.LoopConfig(int(hist_budget_bytes), int(max_cells), int(max_rows), int(ring_capacity),
+                           int(ctas_per_sm), int(idle_ms), int(ray_tile))
+        h = C.c_void_p()
+        _check(N.lib.cpd_loop_create(self._ctx.handle, C.byref(cfg), C.byref(h)), "cpd_loop_create")
+        self._h = h
+        self._sizes: dict[int, int] = {}
+        self._lock = threading.Lock()
+
+    def submit(self, designs, *, seeds=0.5, max_n=128, max_eval=8192, mode: int = TRACE_HYBRID) -> int:
+        """Queues designs (Spectrometers or an N.DESIGN_DTYPE array); returns the request id."""
+        d = _design_array(designs)
+        n = d.size
+        items = _items(n, seeds, max_n, max_eval)
+        rid = C.c_uint64(0)
+        _check(N.lib.cpd_loop_submit(self._h, d.ctypes.data, items.ctypes.data, n, int(mode), C.byref(rid)),
+               "cpd_loop_submit")
+        with self._lock:
+            self._sizes[rid.value] = n
+        return rid.value
+
+    def wait(self, request_id: int, timeout: Optional[float] = None):
+        """(results, latency_ms) as Server.wait."""
+        with self._lock:
+            n = self._sizes[request_id]
+        outs = np.zeros(n, dtype=N.FITNESS_DTYPE)
+        lat = C.c_double(0.0)
+        remaining = math.inf if timeout is None else float(timeout)
+        while True:
+            step = min(remaining, 1.0)
+            rc = N.lib.cpd_loop_wait(self._h, request_id, outs.ctypes.data, step * 1e3, C.byref(lat))
+            if rc != N.TIMEOUT:
+                break
+            remaining -= step
+            if remaining <= 0:
+                raise TimeoutError(f"request {request_id} not done")
+        with self._lock:
+            del self._sizes[request_id]
+        _check(rc, "cpd_loop_wait")
+        return outs, lat.value
+
+    def stats(self) -> dict:
+        r = N.LoopReport()
+        _check(N.lib.cpd_loop_stats(self._h, C.byref(r)), "cpd_loop_stats")
+        return r.as_dict()
+
+    def close(self):
+        if self._h:
+            N.lib.cpd_loop_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
 class Server:
     """Continuous-batching fitness server on one GPU (no reference counterpart).
 

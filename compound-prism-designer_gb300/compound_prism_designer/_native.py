@@ -119,6 +119,23 @@ class BatchItem(C.Structure):
     _fields_ = [("seed", C.c_double), ("max_n", C.c_uint32), ("max_eval", C.c_uint32)]
 
 
+class LoopConfig(C.Structure):
+    _fields_ = [("hist_budget_bytes", C.c_uint64), ("max_cells", C.c_uint32), ("max_rows", C.c_uint32),
+                ("ring_capacity", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("idle_ms", C.c_uint32),
+                ("ray_tile", C.c_uint32)]
+
+
+class LoopReport(C.Structure):
+    _fields_ = [("designs_done", C.c_uint64), ("device_designs", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("max_designs_in_flight", C.c_uint64), ("pending_designs", C.c_uint64),
+                ("table_resets", C.c_uint64), ("inline_retraced", C.c_uint64), ("slab_bytes", C.c_uint64),
+                ("ctas", C.c_uint32), ("idle_exits", C.c_uint32), ("stop_exits", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 _dp = C.POINTER(C.c_double)
 _up = C.POINTER(C.c_uint32)
 _ctxp = C.c_void_p
@@ -177,6 +194,12 @@ SIGNATURES = [
     ("cpd_server_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                    C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("cpd_server_destroy", None, [C.c_void_p]),
+    ("cpd_loop_create", C.c_int, [_ctxp, C.POINTER(LoopConfig), C.POINTER(C.c_void_p)]),
+    ("cpd_loop_submit", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                  C.POINTER(C.c_uint64)]),
+    ("cpd_loop_wait", C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_double, _dp]),
+    ("cpd_loop_stats", C.c_int, [C.c_void_p, C.POINTER(LoopReport)]),
+    ("cpd_loop_destroy", None, [C.c_void_p]),
 ]
 
 # numpy mirrors of the records, for whole-generation arrays passed by pointer

@@ -170,6 +170,7 @@ struct alignas(16) LoopWork {
     uint32_t ray_tile;
     uint32_t pad[2];
 };
+static_assert(sizeof(LoopWork) % 16 == 0, "ring records are copied in 16-byte words");
 
 // The result slot of a ring entry (mapped host memory): written by the CTA that evaluated
 // the entry, then `seq` = index + 1 after a system-scope fence.
@@ -180,14 +181,11 @@ struct alignas(16) LoopDone {
     uint32_t pad;
 };
 
-// Control words (mapped host memory).
+// Control words (mapped host memory), written by the host.
 struct alignas(16) LoopCtl {
-    unsigned long long published;  // host: ring entries published (monotone)
-    unsigned int stop;             // host: exit once the ring is drained
-    unsigned int idle_exits;       // device: CTAs that left after the idle limit
-    unsigned int stop_exits;       // device: CTAs that left on `stop`
+    unsigned long long published;  // ring entries published (monotone)
+    unsigned int stop;             // the CTAs leave once no published entry is left
     unsigned int pad;
-    unsigned long long designs;    // device: designs evaluated
 };
 
 struct LoopArgs {
@@ -219,6 +217,10 @@ struct LoopCounters {
     unsigned int idle_exits;        // CTAs that left after the idle limit
     unsigned int stop_exits;        // CTAs that left on the host's stop word
 };
+
+// A DesignOut as the cpd_fitness of a fixed-N evaluation of `rays` rays (with the SEM
+// convergence status), as every synchronous entry point fills it.
+void fitness_from_out(const DesignOut &o, uint64_t rays, cpd_fitness &f);
 
 // Bytes of one CTA's slab for designs of up to max_rows rows and max_cells cells.
 size_t loop_slab_bytes(uint32_t max_rows, uint32_t max_cells, uint32_t max_B, uint32_t qcap);

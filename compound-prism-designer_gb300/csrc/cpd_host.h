@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include "../../include/cpd.h"
@@ -20,4 +21,23 @@ void ray_table(const double *ray_u, uint32_t R, std::vector<double> &z64, std::v
                std::vector<uint32_t> *rank = nullptr);
 // u_i = fract(fma(first + i, 1/phi, seed)), i < n.
 void seed_points(double seed, uint32_t first, uint32_t n, double *out);
+
+// A sorted ray table with its f32 split and rank (see ray_table).
+struct RayTable {
+    std::vector<double> z64;
+    std::vector<float> z32;
+    std::vector<uint32_t> rank;  // ray index -> sorted position (adaptive sampling)
+};
+using RayTablePtr = std::shared_ptr<const RayTable>;
+using LamPtr = std::shared_ptr<const std::vector<double>>;
+
+// What other translation units need of a context (cpd_runtime.cu): its device, SM count
+// and float-float log2 table on the device, and its caches of the GPU seed policy's tables
+// (ray tables per (seed, R); wavelength points per seed, max(1024, W rounded up to a power
+// of two) of them).
+int context_device(const cpd_context *ctx);
+int context_sms(const cpd_context *ctx);
+const float *context_logtab(const cpd_context *ctx);
+RayTablePtr context_ray_table(cpd_context *ctx, double seed, uint32_t R);
+LamPtr context_lam_points(cpd_context *ctx, double seed, uint32_t W);
 }  // namespace cpd

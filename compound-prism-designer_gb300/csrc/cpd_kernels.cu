@@ -1219,7 +1219,7 @@ constexpr uint32_t kLoopThreads = 256;
 #endif
 
 struct SlabLayout {
-    size_t hist, lp, lx, queue, s1, s2, acc, bytes;
+    size_t hist, lp, lx, queue, s1, s2, acc, band, bytes;
 };
 
 __host__ __device__ inline SlabLayout slab_layout(uint32_t rows, uint32_t cells, uint32_t maxB, uint32_t qcap)
@@ -1240,6 +1240,8 @@ __host__ __device__ inline SlabLayout slab_layout(uint32_t rows, uint32_t cells,
     o += (8 * (size_t)maxB + 255) & ~size_t(255);
     L.acc = o;
     o += (sizeof(DesignAcc) + 255) & ~size_t(255);
+    L.band = o;
+    o += (4 * ((size_t)rows + 1) + 255) & ~size_t(255);
     L.bytes = o;
     return L;
 }
@@ -1278,8 +1280,9 @@ __device__ __noinline__ uint32_t loop_retrace(const DevDesign &D, const LamDF &E
 
 __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel(const LoopArgs L)
 {
-    __shared__ __align__(16) DevDesign sD;
-    __shared__ __align__(16) DesignJob sJ;
+    __shared__ __align__(16) LoopWork sW;
+    DevDesign &sD = sW.d;
+    DesignJob &sJ = sW.j;
     __shared__ float tab[4 * ff::kLogTable];
     __shared__ FinalizeRed fin_red[kLoopThreads / 32];
     __shared__ unsigned long long s_idx, s_hits, s_retraced, s_fast, s_H, s_inline;
@@ -1296,7 +1299,9 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
     unsigned long long *S1 = reinterpret_cast<unsigned long long *>(slab + SL.s1);
     unsigned long long *S2 = reinterpret_cast<unsigned long long *>(slab + SL.s2);
     DesignAcc *acc = reinterpret_cast<DesignAcc *>(slab + SL.acc);
+    uint32_t *band = reinterpret_cast<uint32_t *>(slab + SL.band);  // exclusive prefix of band rays per row
     unsigned long long *s1 = loop_smem, *s2 = loop_smem + L.max_B;
+    __shared__ uint32_t s_part[kLoopThreads];
     const Guards guards = default_guards();
     // the idle wait: bounded in time and in polls (a poll sleeps about a microsecond)
     const unsigned long long max_polls = L.idle_ns / 500ull + 1000ull;
@@ -1335,19 +1340,16 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
         if (idx == ~0ull) break;
         const uint32_t slot = (uint32_t)(idx % L.capacity);
         {
-            // the record (after thread 0's acquire of `published` and the barrier)
-            const uint32_t *src = reinterpret_cast<const uint32_t *>(&L.ring[slot].d);
-            uint32_t *dst = reinterpret_cast<uint32_t *>(&sD);
-            for (uint32_t i = t; i < sizeof(DevDesign) / 4; i += blockDim.x) dst[i] = src[i];
-            const uint32_t *srcj = reinterpret_cast<const uint32_t *>(&L.ring[slot].j);
-            uint32_t *dstj = reinterpret_cast<uint32_t *>(&sJ);
-            for (uint32_t i = t; i < sizeof(DesignJob) / 4; i += blockDim.x) dstj[i] = srcj[i];
+            // the record (after thread 0's acquire of `published` and the barrier), in 16-byte
+            // words from mapped host memory
+            const uint4 *src = reinterpret_cast<const uint4 *>(&L.ring[slot]);
+            uint4 *dst = reinterpret_cast<uint4 *>(&sW);
+            for (uint32_t i = t; i < sizeof(LoopWork) / 16; i += blockDim.x) dst[i] = __ldcv(src + i);
         }
-        const uint32_t ray_tile = L.ring[slot].ray_tile;
         unsigned long long *accw = reinterpret_cast<unsigned long long *>(acc);
         for (uint32_t i = t; i < sizeof(DesignAcc) / 8; i += blockDim.x) accw[i] = 0ull;
         __syncthreads();
-        const uint32_t W = sJ.W, B = sJ.B, Rz = sJ.Rz;
+        const uint32_t W = sJ.W, B = sJ.B, Rz = sJ.Rz, ray_tile = sW.ray_tile;
         const float *z32 = L.z32 + 2 * sJ.ray_off;
         for (uint32_t b = t; b < B; b += blockDim.x) s1[b] = s2[b] = 0ull;
 
@@ -1430,20 +1432,50 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
         }
         __syncthreads();
 
-        // ---- float-float re-trace: each row's guard bands (a warp per row), then the queue
+        // ---- float-float re-trace of every row's guard bands, spread over all threads (an
+        // exclusive prefix sum of the rows' band rays: rows differ widely), then the queue
+        {
+            // per thread: a contiguous run of rows; its band rays, then a scan over threads
+            const uint32_t per = (W + blockDim.x - 1u) / blockDim.x;
+            const uint32_t k0 = min(t * per, W), k1 = min(k0 + per, W);
+            uint32_t run = 0;
+            for (uint32_t k = k0; k < k1; k++) {
+                const LamParams &P = lp[k];
+                band[k] = run;
+                run += P.all_exact ? P.band_hi - P.band_lo : (P.core_lo - P.band_lo) + (P.band_hi - P.core_hi);
+            }
+            s_part[t] = run;
+            __syncthreads();
+            if (t == 0) {
+                uint32_t acc_n = 0;
+                for (uint32_t i = 0; i < blockDim.x; i++) {
+                    const uint32_t v = s_part[i];
+                    s_part[i] = acc_n;
+                    acc_n += v;
+                }
+                band[W] = acc_n;
+            }
+            __syncthreads();
+            for (uint32_t k = k0; k < k1; k++) band[k] += s_part[t];
+            __syncthreads();
+        }
         {
             unsigned long long hits = 0ull, ret = 0ull;
-            for (uint32_t k = warp; k < W; k += nwarps) {
-                const LamParams &P = lp[k];
-                const uint32_t a0 = P.band_lo, a1 = P.all_exact ? P.band_hi : P.core_lo;
-                const uint32_t b0 = P.all_exact ? P.band_hi : P.core_hi, b1 = P.band_hi;
-                unsigned long long *hrow = hist + (uint64_t)k * B;
-                const uint32_t na = a1 > a0 ? a1 - a0 : 0u, nb = b1 > b0 ? b1 - b0 : 0u;
-                for (uint32_t i = lane; i < na + nb; i += 32u) {
-                    const uint32_t j = i < na ? a0 + i : b0 + (i - na);
-                    hits += loop_retrace(sD, lx[k], z32, j, hrow);
-                    ret++;
+            const uint32_t nband = band[W];
+            for (uint32_t i = t; i < nband; i += blockDim.x) {
+                // the row holding band ray i: the last k with band[k] <= i
+                uint32_t lo = 0, hi = W;
+                while (hi - lo > 1u) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (band[mid] <= i) lo = mid;
+                    else hi = mid;
                 }
+                const uint32_t k = lo, r = i - band[k];
+                const LamParams &P = lp[k];
+                const uint32_t na = P.all_exact ? P.band_hi - P.band_lo : P.core_lo - P.band_lo;
+                const uint32_t j = r < na ? P.band_lo + r : P.core_hi + (r - na);
+                hits += loop_retrace(sD, lx[k], z32, j, hist + (uint64_t)k * B);
+                ret++;
             }
             const uint32_t qn = min(s_qn, L.qcap);
             for (uint32_t i = t; i < qn; i += blockDim.x) {

@@ -88,13 +88,6 @@ struct RayKey {
     bool operator<(const RayKey &o) const { return seed_bits != o.seed_bits ? seed_bits < o.seed_bits : R < o.R; }
 };
 
-struct RayTable {
-    std::vector<double> z64;
-    std::vector<float> z32;
-    std::vector<uint32_t> rank;  // ray index -> sorted position (adaptive sampling)
-};
-using RayTablePtr = std::shared_ptr<const RayTable>;
-
 // The sampling flags a trace mode may carry.
 constexpr uint32_t kSamplingBits = CPD_SAMPLING_ADAPTIVE | CPD_SAMPLING_EXACT;
 
@@ -216,7 +209,6 @@ RayTablePtr ray_table_cached(cpd_context *ctx, double seed, uint32_t R)
 // wavelengths are the first W of any longer table of the same seed, so one table of
 // max(1024, W rounded up to a power of two) points serves every W up to its length:
 // the designs of a batch with mixed W share a few tables.
-using LamPtr = std::shared_ptr<const std::vector<double>>;
 LamPtr lam_points_cached(cpd_context *ctx, double seed, uint32_t W)
 {
     uint64_t bits;
@@ -687,6 +679,15 @@ void batch_inputs(cpd_context *ctx, const cpd_design *designs, const cpd_batch_i
 }
 
 }  // namespace
+
+namespace cpd {
+int context_device(const cpd_context *ctx) { return ctx->device; }
+int context_sms(const cpd_context *ctx) { return ctx->num_sms; }
+const float *context_logtab(const cpd_context *ctx) { return ctx->logtab.as<float>(); }
+RayTablePtr context_ray_table(cpd_context *ctx, double seed, uint32_t R) { return ray_table_cached(ctx, seed, R); }
+LamPtr context_lam_points(cpd_context *ctx, double seed, uint32_t W) { return lam_points_cached(ctx, seed, W); }
+void fitness_from_out(const DesignOut &o, uint64_t rays, cpd_fitness &f) { fill_fitness(o, rays, f, true, false); }
+}  // namespace cpd
 
 // ------------------------------------------------------------------ the server
 

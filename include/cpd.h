@@ -381,6 +381,54 @@ int cpd_server_stats(cpd_server *sv, uint64_t *designs_done, uint64_t *passes,
 /* Finishes every queued design, then stops the worker and frees the slots. */
 void cpd_server_destroy(cpd_server *sv);
 
+/* ---------------------------------------------------------------- device-resident loop */
+
+/* No reference counterpart (the reference's optimizer calls gpu_fitness once per design,
+ * designer.py:267-300, through a process-wide lock, src/cuda_fitness.rs:322-362): a
+ * serving loop that lives on the GPU. One persistent kernel; each of its CTAs owns a
+ * histogram slab and evaluates whole designs, taking them from a ring of records in
+ * mapped host memory, with no host step between designs. The host queues requests and
+ * feeds the ring; completions are read from mapped memory. The GPU memory for histograms
+ * is hist_budget_bytes split into slabs of max_cells cells (8 bytes each), one per
+ * resident CTA: a design is admitted when W * bin_count <= max_cells and W <= max_rows,
+ * else cpd_loop_submit returns CPD_NO_CAPACITY. A CTA with no work waits at most idle_ms,
+ * then leaves; the loop relaunches the kernel when new work arrives. Fixed N with the
+ * hybrid trace (CPD_TRACE_HYBRID) only. Each design's result is bitwise its result from
+ * cpd_fitness_gpu_batch with n = 1 (integer accumulation, the same device code). */
+typedef struct cpd_loop cpd_loop;
+typedef struct cpd_loop_config {
+    uint64_t hist_budget_bytes;  /* 0: 4 GiB */
+    uint32_t max_cells;          /* W * bin_count a slab holds; 0: 2^20 */
+    uint32_t max_rows;           /* wavelengths a slab holds; 0: 8192 */
+    uint32_t ring_capacity;      /* designs published and not yet completed; 0: 16384 */
+    uint32_t ctas_per_sm;        /* 0: as many as fit */
+    uint32_t idle_ms;            /* a CTA's longest wait for work; 0: 200 */
+    uint32_t ray_tile;           /* rays per lane per trace work item; 0: 64 */
+} cpd_loop_config;
+typedef struct cpd_loop_report {
+    uint64_t designs_done;           /* completions read by the host */
+    uint64_t device_designs;         /* designs the CTAs evaluated */
+    uint64_t kernel_launches;        /* launches of the loop kernel (after idle exits) */
+    uint64_t max_designs_in_flight;  /* published and not yet completed, at most */
+    uint64_t pending_designs;        /* queued on the host, not yet published */
+    uint64_t table_resets;           /* times the device table arena was emptied */
+    uint64_t inline_retraced;        /* flagged rays re-traced inline (a slab queue was full) */
+    uint64_t slab_bytes;             /* device bytes per CTA */
+    uint32_t ctas;                   /* CTAs of the loop kernel */
+    uint32_t idle_exits;             /* CTAs that left after idle_ms without work */
+    uint32_t stop_exits;             /* CTAs that left on cpd_loop_destroy */
+    uint32_t reserved;
+} cpd_loop_report;
+int cpd_loop_create(cpd_context *ctx, const cpd_loop_config *cfg, cpd_loop **out);
+/* Queues n designs (trace mode CPD_TRACE_HYBRID); returns a request id at once. */
+int cpd_loop_submit(cpd_loop *loop, const cpd_design *designs, const cpd_batch_item *items, uint32_t n,
+                    uint32_t trace_mode, uint64_t *request_id);
+/* As cpd_server_wait. */
+int cpd_loop_wait(cpd_loop *loop, uint64_t request_id, cpd_fitness *outs, double timeout_ms, double *latency_ms);
+int cpd_loop_stats(cpd_loop *loop, cpd_loop_report *out);
+/* Finishes every queued design, lets the CTAs leave, frees the loop. */
+void cpd_loop_destroy(cpd_loop *loop);
+
 #ifdef __cplusplus
 }
 #endif
