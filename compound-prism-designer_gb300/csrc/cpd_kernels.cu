@@ -1278,6 +1278,101 @@ __device__ __noinline__ uint32_t loop_retrace(const DevDesign &D, const LamDF &E
     return 0u;
 }
 
+// The loop's per-wavelength setup: rows t, t + nthr, ... (out of line, so that its
+// float-float program does not set the register budget of the trace loop).
+__device__ __noinline__ void loop_setup(const DevDesign &D, const double *lam, const float *z32, uint32_t Rz, uint32_t W,
+                                        LamParams *lp, LamDF *lx, uint32_t t, uint32_t nthr)
+{
+    for (uint32_t k = t; k < W; k += nthr) {
+        LamParams P;
+        lambda_setup_df(D, lam[k], z32, Rz, P, kYGuardRel, lx + k, false);
+        if (P.all_exact) {
+            // no reference ray: every ray of the band is re-traced
+            P.core_lo = P.core_hi = 0;
+        }
+        lp[k] = P;
+    }
+}
+
+// Counters of one design in the loop (shared memory).
+struct LoopTally {
+    unsigned long long hits, retraced, fast, H, inl;
+    uint32_t item, qn;
+};
+
+// The loop's FP32 trace of the core rays by one warp: items of 32 rows x a ray chunk,
+// claimed from the shared counter; hits as run-length fixed-point sums into the slab's
+// histogram; flagged rays to the slab's queue, or re-traced here when it is full.
+__device__ __noinline__ void loop_trace(const DevDesign &D, const LamParams *lp, const LamDF *lx, const float *z32,
+                                        uint32_t W, uint32_t B, uint32_t Rz, uint32_t ray_tile,
+                                        unsigned long long *hist, QEntry *queue, uint32_t qcap, LoopTally *tally,
+                                        uint32_t lane)
+{
+    const uint32_t nblk = (W + 31u) / 32u;
+    const uint32_t nchunk = Rz ? (Rz + ray_tile - 1u) / ray_tile : 1u;
+    const uint32_t total = nblk * nchunk;
+    const FastConst &C = D.fc;
+    const Guards guards = default_guards();
+    for (;;) {
+        uint32_t item = 0;
+        if (lane == 0) item = atomicAdd(&tally->item, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        const uint32_t blk = item / nchunk, chunk = item - blk * nchunk;
+        const uint32_t k = blk * 32u + lane;
+        LamParams P;
+        uint32_t lo = 0, hi = 0;
+        if (k < W) {
+            P = lp[k];
+            const uint32_t j0 = chunk * ray_tile;
+            const uint32_t j1 = min(j0 + ray_tile, Rz);
+            lo = max(j0, P.core_lo);
+            hi = min(j1, P.core_hi);
+        }
+        const float2 *__restrict__ zt = reinterpret_cast<const float2 *>(z32);
+        unsigned long long *hrow = hist + (uint64_t)k * B;
+        uint32_t cur = 0xffffffffu;
+        unsigned long long sum = 0ull;
+        uint32_t nhit = 0, ninl = 0;
+        for (uint32_t j = lo; j < hi; ++j) {
+            const float2 z = __ldg(zt + j);
+            uint32_t bin = 0;
+            float tt = 0.f;
+            const int r = fast_ray(C, P, guards, z.x, z.y, bin, tt);
+            if (r == RAY_HIT) {
+                if (bin != cur) {
+                    if (sum) atomicAdd(hrow + cur, sum);
+                    cur = bin;
+                    sum = 0ull;
+                }
+                sum += t_fixed(tt);
+                nhit++;
+            } else if (r == RAY_FLAG) {
+                const uint32_t pos = atomicAdd(&tally->qn, 1u);
+                if (pos < qcap) {
+                    queue[pos] = QEntry{0u, k, j, 0u};
+                } else {
+                    // the queue is full: re-trace here (counted as re-traced, as queued)
+                    nhit += loop_retrace(D, lx[k], z32, j, hrow);
+                    ninl++;
+                }
+            }
+        }
+        if (sum) atomicAdd(hrow + cur, sum);
+        nhit = __reduce_add_sync(0xffffffffu, nhit);
+        ninl = __reduce_add_sync(0xffffffffu, ninl);
+        const uint32_t nfast = __reduce_add_sync(0xffffffffu, hi > lo ? hi - lo : 0u);
+        if (lane == 0) {
+            if (nhit) atomicAdd(&tally->hits, (unsigned long long)nhit);
+            if (nfast) atomicAdd(&tally->fast, (unsigned long long)nfast);
+            if (ninl) {
+                atomicAdd(&tally->retraced, (unsigned long long)ninl);
+                atomicAdd(&tally->inl, (unsigned long long)ninl);
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel(const LoopArgs L)
 {
     __shared__ __align__(16) LoopWork sW;
@@ -1285,8 +1380,8 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
     DesignJob &sJ = sW.j;
     __shared__ float tab[4 * ff::kLogTable];
     __shared__ FinalizeRed fin_red[kLoopThreads / 32];
-    __shared__ unsigned long long s_idx, s_hits, s_retraced, s_fast, s_H, s_inline;
-    __shared__ uint32_t s_item, s_qn;
+    __shared__ unsigned long long s_idx;
+    __shared__ LoopTally tally;
     extern __shared__ __align__(16) unsigned long long loop_smem[];  // per-bin s1, s2 (max_B each)
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5, nwarps = blockDim.x >> 5;
     for (uint32_t i = t; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = L.logtab[i];
@@ -1302,7 +1397,6 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
     uint32_t *band = reinterpret_cast<uint32_t *>(slab + SL.band);  // exclusive prefix of band rays per row
     unsigned long long *s1 = loop_smem, *s2 = loop_smem + L.max_B;
     __shared__ uint32_t s_part[kLoopThreads];
-    const Guards guards = default_guards();
     // the idle wait: bounded in time and in polls (a poll sleeps about a microsecond)
     const unsigned long long max_polls = L.idle_ns / 500ull + 1000ull;
     unsigned long long idle_start = global_ns();
@@ -1331,9 +1425,7 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
                 __nanosleep(1000);
             }
             s_idx = got;
-            s_item = 0u;
-            s_qn = 0u;
-            s_hits = s_retraced = s_fast = s_H = s_inline = 0ull;
+            tally = LoopTally{0ull, 0ull, 0ull, 0ull, 0ull, 0u, 0u};
         }
         __syncthreads();
         const unsigned long long idx = s_idx;
@@ -1354,82 +1446,11 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
         for (uint32_t b = t; b < B; b += blockDim.x) s1[b] = s2[b] = 0ull;
 
         // ---- per-wavelength setup
-        for (uint32_t k = t; k < W; k += blockDim.x) {
-            LamParams P;
-            lambda_setup_df(sD, L.lam[sJ.lam_off + k], z32, Rz, P, kYGuardRel, lx + k, false);
-            if (P.all_exact) {
-                // no reference ray: every ray of the band is re-traced
-                P.core_lo = P.core_hi = 0;
-            }
-            lp[k] = P;
-        }
+        loop_setup(sD, L.lam + sJ.lam_off, z32, Rz, W, lp, lx, t, blockDim.x);
         __syncthreads();
 
         // ---- FP32 trace of the core rays
-        {
-            const uint32_t nblk = (W + 31u) / 32u;
-            const uint32_t nchunk = Rz ? (Rz + ray_tile - 1u) / ray_tile : 1u;
-            const uint32_t total = nblk * nchunk;
-            const FastConst &C = sD.fc;
-            for (;;) {
-                uint32_t item = 0;
-                if (lane == 0) item = atomicAdd(&s_item, 1u);
-                item = __shfl_sync(0xffffffffu, item, 0);
-                if (item >= total) break;
-                const uint32_t blk = item / nchunk, chunk = item - blk * nchunk;
-                const uint32_t k = blk * 32u + lane;
-                LamParams P;
-                uint32_t lo = 0, hi = 0;
-                if (k < W) {
-                    P = lp[k];
-                    const uint32_t j0 = chunk * ray_tile;
-                    const uint32_t j1 = min(j0 + ray_tile, Rz);
-                    lo = max(j0, P.core_lo);
-                    hi = min(j1, P.core_hi);
-                }
-                const float2 *__restrict__ zt = reinterpret_cast<const float2 *>(z32);
-                unsigned long long *hrow = hist + (uint64_t)k * B;
-                uint32_t cur = 0xffffffffu;
-                unsigned long long sum = 0ull;
-                uint32_t nhit = 0, ninl = 0;
-                for (uint32_t j = lo; j < hi; ++j) {
-                    const float2 z = __ldg(zt + j);
-                    uint32_t bin = 0;
-                    float tt = 0.f;
-                    const int r = fast_ray(C, P, guards, z.x, z.y, bin, tt);
-                    if (r == RAY_HIT) {
-                        if (bin != cur) {
-                            if (sum) atomicAdd(hrow + cur, sum);
-                            cur = bin;
-                            sum = 0ull;
-                        }
-                        sum += t_fixed(tt);
-                        nhit++;
-                    } else if (r == RAY_FLAG) {
-                        const uint32_t pos = atomicAdd(&s_qn, 1u);
-                        if (pos < L.qcap) {
-                            queue[pos] = QEntry{0u, k, j, 0u};
-                        } else {
-                            // the queue is full: re-trace here (counted as re-traced, as queued)
-                            nhit += loop_retrace(sD, lx[k], z32, j, hrow);
-                            ninl++;
-                        }
-                    }
-                }
-                if (sum) atomicAdd(hrow + cur, sum);
-                nhit = __reduce_add_sync(0xffffffffu, nhit);
-                ninl = __reduce_add_sync(0xffffffffu, ninl);
-                const uint32_t nfast = __reduce_add_sync(0xffffffffu, hi > lo ? hi - lo : 0u);
-                if (lane == 0) {
-                    if (nhit) atomicAdd(&s_hits, (unsigned long long)nhit);
-                    if (nfast) atomicAdd(&s_fast, (unsigned long long)nfast);
-                    if (ninl) {
-                        atomicAdd(&s_retraced, (unsigned long long)ninl);
-                        atomicAdd(&s_inline, (unsigned long long)ninl);
-                    }
-                }
-            }
-        }
+        loop_trace(sD, lp, lx, z32, W, B, Rz, ray_tile, hist, queue, L.qcap, &tally, lane);
         __syncthreads();
 
         // ---- float-float re-trace of every row's guard bands, spread over all threads (an
@@ -1477,7 +1498,7 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
                 hits += loop_retrace(sD, lx[k], z32, j, hist + (uint64_t)k * B);
                 ret++;
             }
-            const uint32_t qn = min(s_qn, L.qcap);
+            const uint32_t qn = min(tally.qn, L.qcap);
             for (uint32_t i = t; i < qn; i += blockDim.x) {
                 const QEntry e = queue[i];
                 hits += loop_retrace(sD, lx[e.k], z32, e.j, hist + (uint64_t)e.k * B);
@@ -1486,8 +1507,8 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
             hits = warp_sum_u64(hits);
             ret = warp_sum_u64(ret);
             if (lane == 0) {
-                if (hits) atomicAdd(&s_hits, hits);
-                if (ret) atomicAdd(&s_retraced, ret);
+                if (hits) atomicAdd(&tally.hits, hits);
+                if (ret) atomicAdd(&tally.retraced, ret);
             }
         }
         __syncthreads();
@@ -1510,7 +1531,7 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
                 }
             }
             hl = warp_sum_u64(hl);
-            if (lane == 0 && hl) atomicAdd(&s_H, hl);
+            if (lane == 0 && hl) atomicAdd(&tally.H, hl);
         }
         __syncthreads();
         for (uint32_t b = t; b < B; b += blockDim.x) {
@@ -1518,12 +1539,12 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
             S2[b] = s2[b];
         }
         if (t == 0) {
-            acc->H = s_H;
+            acc->H = tally.H;
             acc->rows = 0ull;
-            acc->hits[0] = s_hits;
-            acc->retraced[0] = s_retraced;
-            acc->fast[0] = s_fast;
-            if (s_inline) atomicAdd(&L.cnt->inline_retraced, s_inline);
+            acc->hits[0] = tally.hits;
+            acc->retraced[0] = tally.retraced;
+            acc->fast[0] = tally.fast;
+            if (tally.inl) atomicAdd(&L.cnt->inline_retraced, tally.inl);
         }
         __syncthreads();
 
