@@ -255,11 +255,36 @@ def cpu_oracle_rate(d, W, R, target_s=10.0, nthreads=None, gpu_info=None):
     out = {"value": done / dt, "unit": "designs/s", "cores": nthreads, "kind": "port",
            "sample": f"{done} whole designs of the benchmark workload ({W} wavelengths x {R} rays each, "
                      f"{done * W * R} rays, {dt:.1f} s, {nthreads} threads, fixed N on the GPU call's points)",
-           "reference_adaptive": reference_adaptive_rate(d, W, R, nthreads)}
+           "reference_adaptive": reference_adaptive_rate(d, W, R, nthreads),
+           "config0": config0_rates(nthreads)}
     if gpu_info is not None:
         out["mi_check"] = {"gpu_mi": gpu_info, "oracle_mi": st["info"],
                            "rel_err": abs(gpu_info - st["info"]) / abs(st["info"]), "tolerance": 1e-4}
     return out
+
+
+def config0_rates(nthreads, target_s=2.0):
+    """The reference's CPU-runnable case (3 prisms, 32 bins, 64 wavelengths x 256 rays, the
+    reference CPU point set from 0.5): the oracle's fixed-N rate, one design per thread, and
+    the reference's adaptive fitness with max_n = 64, max_m = 256."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import numpy as np
+    import oracle as O
+    from compound_prism_designer import synth
+
+    _, d, _ = synth.random_design(np.random.default_rng(20261203), 3, 32)
+    lam, ray_u = O.qrng_points(0.5, 64), O.qrng_points(0.5, 256)
+    _, st = O.fitness_points(d, lam, ray_u)
+    done, t0 = 0, time.perf_counter()
+    with ThreadPoolExecutor(nthreads) as ex:
+        while done == 0 or time.perf_counter() - t0 < target_s:
+            list(ex.map(lambda _: O.fitness_points(d, lam, ray_u, want_p=False), range(nthreads * 8)))
+            done += nthreads * 8
+    fixed = done / (time.perf_counter() - t0)
+    ad = reference_adaptive_rate(d, 64, 256, nthreads, target_s=target_s)
+    return {"workload": "3 prisms, 32 bins, 64 wavelengths x 256 rays (reference CPU points from 0.5)",
+            "fixed_n_designs_per_s": fixed, "fixed_n_mi": st["info"], "reference_adaptive": ad, "cores": nthreads}
 
 
 def reference_adaptive_rate(d, max_n, max_m, nthreads, target_s=3.0):

@@ -8,7 +8,11 @@ through the C ABI of libcpd.so (include/cpd.h); gpu_fitness runs the
 sm_103a kernels and has no CPU fallback.
 
 Out of scope (they raise NotImplementedError): the 3-D FiberBeam/toric-lens
-variant on the GPU and the matplotlib drawing helpers (polygons, surfaces).
+variant and the matplotlib drawing helpers (polygons, surfaces). The reference's 3-D
+ray-torus intersection (src/spectrometer/toric.rs:41-201) takes the square root of a
+negative discriminant whenever a ray meets the torus four times, so in the reference
+optimizer's fiber configuration no design can be positioned and every ray is lost at the
+first toric lens; the 3-D path is not reproduced on the GPU.
 """
 from __future__ import annotations
 
@@ -233,7 +237,10 @@ class CompoundPrism:
         if len(glasses) != len(lengths):
             raise ValueError("len(glasses) != len(lengths)")
         if isinstance(curvature, (tuple, list)):
-            raise NotImplementedError("the 3-D toric-lens compound prism is not built")
+            raise NotImplementedError(
+                "the 3-D toric-lens compound prism is not built: the reference's closed-form ray-torus "
+                "intersection (toric.rs:41-141) yields NaN whenever a ray meets the torus four times, so no "
+                "design of its fiber configuration can be positioned")
         self.glasses = glasses
         self.angles = angles
         self.lengths = lengths
