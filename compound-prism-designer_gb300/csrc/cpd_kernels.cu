@@ -767,6 +767,9 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
     const bool active = grp < groups;
     const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
     unsigned long long *base = a.hist + J.hist_off;
+    // the f64 scale of the optional p(d|lambda) output, formed only when it is written
+    // (an f64 division issues to the FP64 unit, ~64 cycles per warp instruction here)
+    const double pscale = a.p_out ? kTScaleInv / (double)J.R : 0.0;
     for (uint32_t bg = 0; bg < B; bg += 32u * NB) {
         unsigned long long c1[NB], q2[NB];
 #pragma unroll
@@ -801,8 +804,7 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
                             c1[ii] += cv;
                         }
                 }
-                if (a.p_out && active && rw < r1 && b < B)
-                    a.p_out[(uint64_t)rw * B + b] = (double)cv * (kTScaleInv / (double)J.R);
+                if (a.p_out && active && rw < r1 && b < B) a.p_out[(uint64_t)rw * B + b] = (double)cv * pscale;
             }
         }
 #pragma unroll
@@ -880,6 +882,7 @@ __global__ void __launch_bounds__(kEntropyThreads, 4) entropy_block_kernel(const
         __syncthreads();
         const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
         unsigned long long *base = a.hist + J.hist_off;
+        const double pscale = a.p_out ? kTScaleInv / (double)J.R : 0.0;  // see entropy_tile
         const uint32_t cells = (r1 - r0) * B;
         const uint32_t db = (uint32_t)kEntropyThreads % B, dr = (uint32_t)kEntropyThreads / B;
         uint32_t b = t % B, row = r0 + t / B;
@@ -896,7 +899,7 @@ __global__ void __launch_bounds__(kEntropyThreads, 4) entropy_block_kernel(const
                 idx[k] = (uint64_t)row * B + b;
                 bc[k] = b;
                 cv[k] = in ? base[idx[k]] : 0ull;
-                if (in && a.p_out) a.p_out[idx[k]] = (double)cv[k] * (kTScaleInv / (double)J.R);
+                if (in && a.p_out) a.p_out[idx[k]] = (double)cv[k] * pscale;
                 b += db;
                 row += dr;
                 if (b >= B) {

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <iterator>
 #include <array>
 #include <chrono>
 #include <cmath>
@@ -106,7 +107,18 @@ struct PassSlot {
     size_t ctl_off = 0;
     bool hist_dirty = true;
     uint32_t qcap = 1u << 18;
-    std::vector<uint8_t> graph_key;
+    // Captured passes, most recently used first: a caller that alternates between a few
+    // launch signatures (designs of different detector sizes, say) replays each one's
+    // graph instead of capturing anew. The key holds every pointer and size the graph
+    // bakes in, plus buf_gen, which changes whenever a buffer of the slot is reallocated.
+    struct CachedGraph {
+        std::vector<uint8_t> key;
+        cudaGraphExec_t exec;
+        int launches;
+    };
+    std::vector<CachedGraph> graphs;
+    static constexpr size_t kGraphCache = 8;
+    uint64_t buf_gen = 0;
     // The wavelength-point and ray tables (the arena after the designs and jobs) of the
     // last pass, when they came from the context's caches: identity of each table in
     // upload order, and references that keep those tables (and so their addresses)
@@ -114,8 +126,6 @@ struct PassSlot {
     // jobs only.
     std::vector<const void *> tables_key;
     std::vector<std::shared_ptr<const void>> tables_refs;
-    cudaGraphExec_t graph_exec = nullptr;
-    int graph_launches = 0;
     // the pass in flight / last finished
     uint32_t n = 0;
     uint64_t hist_cells = 0;
@@ -138,8 +148,8 @@ struct PassSlot {
     void destroy()
     {
         if (stream) cudaStreamSynchronize(stream);
-        if (graph_exec) cudaGraphExecDestroy(graph_exec);
-        graph_exec = nullptr;
+        for (CachedGraph &c : graphs) cudaGraphExecDestroy(c.exec);
+        graphs.clear();
         for (DevBuf *b : {&in, &lp, &lx, &hist, &S1, &S2, &acc, &queue, &pout}) b->release();
         for (HostBuf *b : {&h_in, &h_outs}) b->release();
         for (cudaEvent_t *ev : {&ev0, &ev1, &done, &kev[0], &kev[1], &kev[2], &kev[3], &kev[4]})
@@ -384,7 +394,8 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         S.tables_key.clear();
         S.tables_refs.clear();
     }
-    // device buffers
+    // device buffers (a reallocation retires the captured graphs that hold the old addresses)
+    const void *bufs_before[] = {S.lp.p, S.lx.p, S.hist.p, S.S1.p, S.S2.p, S.acc.p, S.queue.p, S.h_in.p, S.h_outs.p, in_before};
     const size_t hist_bytes = sizeof(unsigned long long) * std::max<uint64_t>(hist, 1);
     const size_t old_hist = S.hist.cap;
     CPD_TRY(S.lp.ensure(sizeof(LamParams) * std::max<uint64_t>(rows, 1)));
@@ -397,6 +408,10 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     CPD_TRY(S.queue.ensure(sizeof(QEntry) * S.qcap));
     if (p_out_host) CPD_TRY(S.pout.ensure(hist_bytes));
     S.ctl_off = ctl_off;
+    {
+        const void *after[] = {S.lp.p, S.lx.p, S.hist.p, S.S1.p, S.S2.p, S.acc.p, S.queue.p, S.h_in.p, S.h_outs.p, S.in.p};
+        if (!std::equal(std::begin(after), std::end(after), std::begin(bufs_before))) S.buf_gen++;
+    }
 
     cudaStream_t s = S.stream;
     if (S.hist_dirty) {
@@ -453,10 +468,10 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     // The device work of a pass, captured once per signature and replayed.
     // The whole pass -- input upload, accumulator clears, kernels, read-back, and the two
     // timing events around the kernels -- is one graph, captured once per signature.
-    std::vector<uint8_t> key(sizeof(a) + 6 * sizeof(uint64_t));
+    std::vector<uint8_t> key(sizeof(a) + 8 * sizeof(uint64_t));
     std::memcpy(key.data(), &a, sizeof(a));
-    const uint64_t extra[6] = {n, ctx->warps_per_cta, (uint64_t)ctx->num_sms, (in_bytes << 1) | (resident ? 1u : 0u),
-                               out_bytes, fresh ? accc + 1 : 0};
+    const uint64_t extra[8] = {n, ctx->warps_per_cta, (uint64_t)ctx->num_sms, (in_bytes << 1) | (resident ? 1u : 0u),
+                               out_bytes, fresh ? accc + 1 : 0, S.buf_gen, (uint64_t)(uintptr_t)S.h_in.p};
     std::memcpy(key.data() + sizeof(a), extra, sizeof(extra));
     auto record = [&](cudaStream_t st, bool capturing) -> int {
         const unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
@@ -471,20 +486,27 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         return l;
     };
     if (use_graph && !profile) {
-        if (!S.graph_exec || key != S.graph_key) {
-            if (S.graph_exec) cudaGraphExecDestroy(S.graph_exec);
-            S.graph_exec = nullptr;
+        auto hit = std::find_if(S.graphs.begin(), S.graphs.end(),
+                                [&](const PassSlot::CachedGraph &c) { return c.key == key; });
+        if (hit == S.graphs.end()) {
             cudaGraph_t g = nullptr;
             CPD_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            S.graph_launches = record(s, true);
+            const int launches = record(s, true);
             CPD_TRY(cudaStreamEndCapture(s, &g));
-            const cudaError_t e = cudaGraphInstantiate(&S.graph_exec, g, 0);
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
             cudaGraphDestroy(g);
             CPD_TRY(e);
-            S.graph_key = key;
+            if (S.graphs.size() >= PassSlot::kGraphCache) {
+                cudaGraphExecDestroy(S.graphs.back().exec);
+                S.graphs.pop_back();
+            }
+            S.graphs.insert(S.graphs.begin(), PassSlot::CachedGraph{key, exec, launches});
+        } else if (hit != S.graphs.begin()) {
+            std::rotate(S.graphs.begin(), hit, hit + 1);  // most recently used first
         }
-        CPD_TRY(cudaGraphLaunch(S.graph_exec, s));
-        S.launches = S.graph_launches;
+        CPD_TRY(cudaGraphLaunch(S.graphs.front().exec, s));
+        S.launches = S.graphs.front().launches;
     } else {
         S.launches = record(s, false);
         CPD_TRY(cudaGetLastError());
