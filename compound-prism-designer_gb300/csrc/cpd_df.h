@@ -331,27 +331,34 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
     if (lost) return false;
     // Sorted-ray index ranges: y_j = bym - bw z_j is monotone in z, so the index of a
     // height threshold T is the number of z_j below (bym - T)/bw, counted on the (hi,
-    // lo) table; the four counts are searched in lockstep.
+    // lo) table. The four counts are branch-free lower bounds stepping together: the
+    // interval lengths depend on R alone, so every lane runs the same iterations and the
+    // four table reads of an iteration are independent (a branchy bisection per key took
+    // ~6k cycles at R = 1024, its steps serialised behind their branches).
     auto ycount4 = [&](const F2 thr[4], uint32_t out[4]) {
         F2 key[4];
-        uint32_t lo[4], hi[4];
         const F2 ibw = rcp(C.bw);
+#pragma unroll
         for (int i = 0; i < 4; i++) {
             key[i] = fabsf(thr[i].hi) >= kBig ? c(((thr[i].hi > 0.f) == (C.bw.hi > 0.f)) ? -INFINITY : INFINITY)
                                               : mul(sub(C.bym, thr[i]), ibw);
-            lo[i] = 0;
-            hi[i] = R;
+            out[i] = 0u;
         }
-        while (lo[0] < hi[0] || lo[1] < hi[1] || lo[2] < hi[2] || lo[3] < hi[3]) {
+        if (R == 0u) return;
+        // invariant: the count lies in [base, base + n]; z[base + n/2] < key moves base up
+        uint32_t base[4] = {0u, 0u, 0u, 0u};
+        for (uint32_t n = R; n > 1u;) {
+            const uint32_t half = n >> 1;
+#pragma unroll
             for (int i = 0; i < 4; i++) {
-                if (lo[i] < hi[i]) {
-                    const uint32_t mid = (lo[i] + hi[i]) >> 1;
-                    if (lt(F2{z32[2 * mid], z32[2 * mid + 1]}, key[i])) lo[i] = mid + 1;
-                    else hi[i] = mid;
-                }
+                const uint32_t m = base[i] + half;
+                base[i] = lt(F2{z32[2 * m], z32[2 * m + 1]}, key[i]) ? m : base[i];
             }
+            n -= half;
         }
-        for (int i = 0; i < 4; i++) out[i] = lo[i];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+            out[i] = base[i] + (lt(F2{z32[2 * base[i]], z32[2 * base[i] + 1]}, key[i]) ? 1u : 0u);
     };
     if (C.bw.hi == 0.f) {
         // every ray starts at the same height

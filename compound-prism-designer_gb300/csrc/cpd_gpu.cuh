@@ -29,6 +29,9 @@ struct alignas(16) DesignJob {
     uint32_t pad;
     float unit_hi, unit_lo;  // p per count unit, 2^-31 / R, float-float
     float lu_hi, lu_lo;      // log2 of that unit, float-float
+    double pscale;           // 2^-31 / R in f64, for the optional p(d|lambda) output (set on the host:
+                             // an f64 division on the device issues to the slow FP64 unit)
+    double pad2;
 };
 
 // A ray whose FP32 result fell inside a guard band: (design, wavelength row, ray). In

@@ -52,6 +52,22 @@ __device__ __forceinline__ void push_ray(const LaunchArgs &a, uint32_t d, uint32
     else atomicOr(&a.ctl->overflow, 1u);
 }
 
+// The rays [j0, j1) and [j2, j3) of row k, queued with one atomic for the whole run (a row's
+// guard bands can hold dozens of rays; one round trip to the queue counter per ray made a
+// serial chain on the setup's critical path).
+__device__ __forceinline__ void push_ranges(const LaunchArgs &a, uint32_t d, uint32_t k, uint32_t j0, uint32_t j1,
+                                            uint32_t j2, uint32_t j3)
+{
+    const uint32_t na = j1 > j0 ? j1 - j0 : 0u, nb = j3 > j2 ? j3 - j2 : 0u;
+    if (na + nb == 0u) return;
+    const unsigned long long pos = atomicAdd(&a.ctl->queue_count, (unsigned long long)(na + nb));
+    if (pos + na + nb > a.qcap) atomicOr(&a.ctl->overflow, 1u);
+    for (uint32_t i = 0; i < na + nb; i++) {
+        if (pos + i >= a.qcap) break;
+        a.queue[pos + i] = QEntry{d, k, i < na ? j0 + i : j2 + (i - na), 0u};
+    }
+}
+
 // Designs built on the device from parameter records (CPD_BUILD_ON_DEVICE): one thread
 // per design, the f64 construction of cpd_build.h (positioning first when the pass's
 // acceptance is positive), written straight into the pass's design records. A design whose
@@ -152,14 +168,13 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     if (a.adaptive) {
         // the adaptive rounds trace every ray of the band themselves
     } else if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
-        for (uint32_t j = P.band_lo; j < P.band_hi; j++) push_ray(a, d, k, j);
+        push_ranges(a, d, k, P.band_lo, P.band_hi, 0u, 0u);
         P.core_lo = P.core_hi = 0;
     } else if (P.all_exact) {
         // FP32-only study mode without a reference ray: these rays are counted as lost
         P.core_lo = P.core_hi = 0;
     } else {
-        for (uint32_t j = P.band_lo; j < P.core_lo; j++) push_ray(a, d, k, j);
-        for (uint32_t j = P.core_hi; j < P.band_hi; j++) push_ray(a, d, k, j);
+        push_ranges(a, d, k, P.band_lo, P.core_lo, P.core_hi, P.band_hi);
     }
     a.lp[row] = P;
 }
@@ -767,9 +782,7 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
     const bool active = grp < groups;
     const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
     unsigned long long *base = a.hist + J.hist_off;
-    // the f64 scale of the optional p(d|lambda) output, formed only when it is written
-    // (an f64 division issues to the FP64 unit, ~64 cycles per warp instruction here)
-    const double pscale = a.p_out ? kTScaleInv / (double)J.R : 0.0;
+    const double pscale = J.pscale;  // p per count unit, for the optional p(d|lambda) output
     for (uint32_t bg = 0; bg < B; bg += 32u * NB) {
         unsigned long long c1[NB], q2[NB];
 #pragma unroll
@@ -882,7 +895,7 @@ __global__ void __launch_bounds__(kEntropyThreads, 4) entropy_block_kernel(const
         __syncthreads();
         const ff::F2 unit{J.unit_hi, J.unit_lo}, lu{J.lu_hi, J.lu_lo};
         unsigned long long *base = a.hist + J.hist_off;
-        const double pscale = a.p_out ? kTScaleInv / (double)J.R : 0.0;  // see entropy_tile
+        const double pscale = J.pscale;
         const uint32_t cells = (r1 - r0) * B;
         const uint32_t db = (uint32_t)kEntropyThreads % B, dr = (uint32_t)kEntropyThreads / B;
         uint32_t b = t % B, row = r0 + t / B;
@@ -1386,7 +1399,7 @@ __global__ void __launch_bounds__(kLoopThreads, CPD_LOOP_MIN_BLOCKS) loop_kernel
     __shared__ unsigned long long s_idx;
     __shared__ LoopTally tally;
     extern __shared__ __align__(16) unsigned long long loop_smem[];  // per-bin s1, s2 (max_B each)
-    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5, nwarps = blockDim.x >> 5;
+    const uint32_t t = threadIdx.x, lane = t & 31u;
     for (uint32_t i = t; i < 4u * ff::kLogTable; i += blockDim.x) tab[i] = L.logtab[i];
     const SlabLayout SL = slab_layout(L.max_rows, L.max_cells, L.max_B, L.qcap);
     unsigned char *slab = L.slabs + (size_t)blockIdx.x * L.slab_bytes;
@@ -1608,7 +1621,8 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         launches++;
     }
     if (a.total_rows) {
-        // one warp per block: f64-pipe bound, so spreading rows over every SM matters
+        // one warp per block: each row is one thread's latency-bound float-float chain,
+        // so spreading the rows over every SM matters
         const uint32_t blocks = (uint32_t)((a.total_rows + 31) / 32);
         launch_k(setup_kernel, blocks, 32, 2 * kStageRays * sizeof(float), stream, false, a);
         launches++;

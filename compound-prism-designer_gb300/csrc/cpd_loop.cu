@@ -247,6 +247,7 @@ void loop_feeder(cpd_loop *L)
                 J.ray_off = ray_o;
                 ff::split(kTScaleInv / (double)J.R, J.unit_hi, J.unit_lo);
                 ff::split(-31.0 - std::log2((double)J.R), J.lu_hi, J.lu_lo);
+                J.pscale = kTScaleInv / (double)J.R;
                 w.mode = CPD_TRACE_HYBRID;
                 w.ray_tile = L->ray_tile;
                 L->owner[slot] = Owner{rid, idx, true};

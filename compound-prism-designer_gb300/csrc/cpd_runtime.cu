@@ -326,6 +326,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         J.ntiles = (J.W + J.tile_rows - 1) / J.tile_rows;
         ff::split(kTScaleInv / (double)J.R, J.unit_hi, J.unit_lo);
         ff::split(-31.0 - std::log2((double)J.R), J.lu_hi, J.lu_lo);
+        J.pscale = kTScaleInv / (double)J.R;
         rows += J.W;
         hist += (uint64_t)J.W * J.B;
         if (owns_rays[i]) {

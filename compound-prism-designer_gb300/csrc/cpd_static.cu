@@ -139,6 +139,7 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     J.ntiles = (W + J.tile_rows - 1) / J.tile_rows;
     ff::split(kTScaleInv / (double)R, J.unit_hi, J.unit_lo);
     ff::split(-31.0 - std::log2((double)R), J.lu_hi, J.lu_lo);
+    J.pscale = kTScaleInv / (double)R;
     ff::make_log_table(reinterpret_cast<float *>(st.head + kOffLog));
 
     // The array keeps the previous call's contents: everything that must start at zero is
