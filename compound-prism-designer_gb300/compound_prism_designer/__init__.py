@@ -70,7 +70,9 @@ def _dp(a: np.ndarray):
 def _seed_array(seeds):
     """A few seeds as a ctypes double array (the per-call path: a numpy pointer costs
     several microseconds, a small ctypes array well under one)."""
-    if isinstance(seeds, np.ndarray):
+    if type(seeds) is list and all(type(v) is float for v in seeds):
+        vals = seeds  # the common per-call form, without a numpy round trip
+    elif isinstance(seeds, np.ndarray):
         vals = seeds.ravel().tolist()
     elif isinstance(seeds, (float, int)):
         vals = [seeds]
