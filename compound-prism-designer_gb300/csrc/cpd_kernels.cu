@@ -335,6 +335,13 @@ static_assert(sizeof(RoundSlot) % 16 == 0, "bin states follow the slots 16-byte 
 constexpr size_t adapt_smem_bytes(uint32_t KW, uint32_t B) { return KW * sizeof(RoundSlot) + bin_state_bytes(B); }
 static_assert(adapt_smem_bytes(kMaxAdaptWarps, CPD_MAX_BINS) <= 227u * 1024u, "shared memory per block");
 
+// Dynamic shared memory of the one-warp form (adaptive_row1): the row's LamParams and
+// FastConst, one slot, the bin states.
+constexpr size_t adapt1_smem_bytes(uint32_t B)
+{
+    return sizeof(LamParams) + sizeof(FastConst) + adapt_smem_bytes(1, B);
+}
+
 // Byte v of a bin's group lane table (v = the round within the group).
 __device__ __forceinline__ uint32_t lane_entry(const uint4 &w, uint32_t v)
 {
@@ -554,8 +561,161 @@ __device__ bool adaptive_row(const LaunchArgs &a, uint64_t row, unsigned long lo
     return false;
 }
 
+// One wavelength row under adaptive sampling by a single warp (the form for passes with
+// many rows, where the rows themselves fill the GPU): the same rounds and decisions as
+// adaptive_row, one round after another. Each bin's exact integer Welford sums are kept
+// cumulatively in shared memory; a round's hit lanes add their sums into the slot of their
+// bin's leader (the lowest lane that hit it), the leader adds them to the bin's state and
+// tests the state through the round, and the round stops the row when it hit some bin and
+// every bin it hit passes. No lane tables, no barriers: one warp decides each round alone.
+template <bool kExact>
+__device__ bool adaptive_row1(const LaunchArgs &a, uint64_t row, unsigned long long *smem, uint32_t lane)
+{
+    const uint32_t d = find_job<F_ROW>(a.jobs, a.njobs, row);
+    const DesignJob &J = a.jobs[d];
+    const uint32_t k = (uint32_t)(row - J.row_off);
+    const uint32_t B = J.B, R = J.R;
+    const DevDesign &D = a.designs[d];
+    if (!kExact && a.adaptive == 2u) {
+        // verification mode: every row on the exact path
+        if (lane == 0) {
+            const unsigned long long pos = atomicAdd(&a.ctl->queue_count, 1ull);
+            if (pos < a.qcap) a.queue[pos] = QEntry{d, k, 0u, 0u};
+            else atomicOr(&a.ctl->overflow, 1u);
+        }
+        return false;
+    }
+    // the row's constants are the same in every lane: they live in shared memory (read
+    // where they are used), which leaves the registers to more resident warps
+    LamParams &P = *reinterpret_cast<LamParams *>(smem);
+    FastConst &C = *reinterpret_cast<FastConst *>(reinterpret_cast<char *>(smem) + sizeof(LamParams));
+    RoundSlot &my = *reinterpret_cast<RoundSlot *>(reinterpret_cast<char *>(smem) + sizeof(LamParams) + sizeof(FastConst));
+    const LamDF &E = a.lx[row];
+    const BinStates st(&my + 1, B);
+    static_assert(sizeof(LamParams) % 16 == 0 && sizeof(FastConst) % 16 == 0, "16-byte copies");
+    if (lane < sizeof(LamParams) / 16)
+        reinterpret_cast<uint4 *>(&P)[lane] = reinterpret_cast<const uint4 *>(a.lp + row)[lane];
+    else if (lane < (sizeof(LamParams) + sizeof(FastConst)) / 16)
+        reinterpret_cast<uint4 *>(&C)[lane - sizeof(LamParams) / 16] =
+            reinterpret_cast<const uint4 *>(&D.fc)[lane - sizeof(LamParams) / 16];
+    for (uint32_t b = lane; b < B; b += 32u) {
+        st.s1[b] = st.q1[b] = st.q2[b] = 0ull;
+        st.n[b] = st.h[b] = 0u;
+    }
+    __syncwarp();
+    const uint32_t *rank = a.rank + J.rank_off;
+    const float2 *zt = reinterpret_cast<const float2 *>(a.z32) + J.ray_off;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint32_t count = 0, flag = 0, hits = 0, ndf = 0;  // the same in every lane
+    // no ray clears the flat faces: every round runs without a hit
+    const uint32_t g_start = P.band_lo >= P.band_hi ? R : 0u;
+    if (g_start == R) count = R;
+    // the ray this lane traces in the next round, loaded while the current one is decided
+    uint32_t s_nx = 0xffffffffu;
+    float2 z_nx = make_float2(0.f, 0.f);
+    const auto fetch = [&](uint32_t g) {
+        const uint32_t j = g + lane;
+        s_nx = j < R ? rank[j] : 0xffffffffu;
+        if (s_nx >= P.band_lo && s_nx < P.band_hi) z_nx = zt[s_nx];
+    };
+    if (g_start < R) fetch(g_start);
+    for (uint32_t g0 = g_start; g0 < R; g0 += kRoundRays) {
+        uint32_t bin = 0xffffffffu, tf = 0u;
+        bool used_df = false;
+        {
+            const uint32_t s = s_nx;
+            if (s >= P.band_lo && s < P.band_hi) {
+                const float2 z = z_nx;
+                int res = RAY_FLAG;
+                if (!kExact && !P.all_exact && s >= P.core_lo && s < P.core_hi) {
+                    uint32_t b = 0;
+                    float t = 0.f;
+                    res = fast_ray(C, P, a.guards, z.x, z.y, b, t);
+                    if (res == RAY_HIT) {
+                        bin = b;
+                        tf = t_fixed(t);
+                    }
+                }
+                if (res == RAY_FLAG) {
+                    const uint2 r = trace_df_exact_call(D, E, z.x, z.y);
+                    bin = r.x;
+                    tf = r.y;
+                    used_df = true;
+                }
+            }
+        }
+        if (g0 + kRoundRays < R) fetch(g0 + kRoundRays);
+        const bool hit = bin != 0xffffffffu;
+        const uint32_t hm = __ballot_sync(0xffffffffu, hit);
+        const uint32_t dfb = __ballot_sync(0xffffffffu, used_df);
+        const uint32_t grp = __match_any_sync(0xffffffffu, bin);
+        const bool leader = hit && (grp & lt_mask) == 0u;
+        const uint32_t rn = min(kRoundRays, R - g0);  // samples of this round
+        // the round's sums per bin, in 32-bit pieces (as adaptive_row): into the leader's slot
+        my.p[0][lane] = my.p[1][lane] = my.p[2][lane] = my.p[3][lane] = my.p[4][lane] = 0u;
+        __syncwarp();
+        if (hit) {
+            const uint32_t ld = (uint32_t)__ffs(grp) - 1u, q = tf >> kTqShift;
+            const uint32_t qh = q >> 10, ql = q & 0x3ffu;
+            atomicAdd(&my.p[0][ld], q);
+            atomicAdd(&my.p[1][ld], tf & 0x7ffu);
+            atomicAdd(&my.p[2][ld], qh * qh);
+            atomicAdd(&my.p[3][ld], qh * ql);
+            atomicAdd(&my.p[4][ld], ql * ql);
+        }
+        __syncwarp();
+        int verdict = SEM_PASS;
+        uint32_t cn = 0, ch = 0;
+        unsigned long long cq1 = 0, cq2 = 0;
+        if (leader) {
+            const uint32_t sq = my.p[0][lane];
+            st.s1[bin] += ((unsigned long long)sq << kTqShift) + my.p[1][lane];
+            cq1 = st.q1[bin] + sq;
+            cq2 = st.q2[bin] + ((unsigned long long)my.p[2][lane] << 20) +
+                  ((unsigned long long)my.p[3][lane] << 11) + my.p[4][lane];
+            cn = st.n[bin] + rn;
+            ch = st.h[bin] + (uint32_t)__popc(grp);
+            st.q1[bin] = cq1;
+            st.q2[bin] = cq2;
+            st.n[bin] = cn;
+            st.h[bin] = ch;
+            verdict = sem_quick(cn, ch, cq1, cq2, kExact ? 0u : kTqDelta);
+        }
+        if (__any_sync(0xffffffffu, verdict < 0) && verdict < 0)
+            verdict = sem_test(cn, ch, cq1, cq2, kExact ? 0u : kTqDelta);
+        const bool fail = __any_sync(0xffffffffu, verdict == SEM_FAIL);
+        const bool unsure = __any_sync(0xffffffffu, verdict == SEM_UNSURE);
+        count += rn;
+        hits += (uint32_t)__popc(hm);
+        ndf += (uint32_t)__popc(dfb);
+        if (hm && !fail) {
+            flag = (!kExact && unsure) ? 2u : 1u;
+            break;
+        }
+        if (g0 + kRoundRays >= R) {
+            flag = 1u;  // out of rays
+            break;
+        }
+    }
+    __syncwarp();
+    if (flag == 2u) return true;  // the caller redoes the row on the exact path at once
+    unsigned long long *hrow = a.hist + J.hist_off + (uint64_t)k * B;
+    for (uint32_t b = lane; b < B; b += 32u) {
+        const unsigned long long s1 = st.s1[b];
+        if (s1) hrow[b] = rescale_cell(s1, R, count);
+    }
+    if (lane == 0) {
+        const uint32_t sp = (uint32_t)(row % (uint64_t)kSpread);
+        atomicAdd(&a.acc[d].fast[sp], (unsigned long long)count);
+        if (hits) atomicAdd(&a.acc[d].hits[sp], (unsigned long long)hits);
+        if (ndf) atomicAdd(&a.acc[d].retraced[sp], (unsigned long long)ndf);
+    }
+    __syncwarp();  // the slot and bin states are reused by the next row
+    return false;
+}
+
 #ifndef CPD_ADAPT_KW_MANY
-#define CPD_ADAPT_KW_MANY 2  // warps per row when at least 8 rows per SM
+#define CPD_ADAPT_KW_MANY 1  // warps per row when at least 8 rows per SM (1: adaptive1_kernel)
 #endif
 #ifndef CPD_ADAPT_KW_SOME
 #define CPD_ADAPT_KW_SOME 4  // warps per row at 2 to 7 rows per SM
@@ -577,6 +737,19 @@ __global__ void __launch_bounds__(32 * kMaxAdaptWarps, CPD_ADAPT_MIN_BLOCKS) ada
         adaptive_row<true>(a, blockIdx.x, adapt_smem, kw, warp, lane);
 }
 
+#ifndef CPD_ADAPT1_MIN_BLOCKS
+#define CPD_ADAPT1_MIN_BLOCKS 32
+#endif
+// The many-rows form: one row per one-warp block (adaptive_row1).
+__global__ void __launch_bounds__(32, CPD_ADAPT1_MIN_BLOCKS) adaptive1_kernel(const LaunchArgs a)
+{
+    extern __shared__ __align__(16) unsigned long long adapt_smem[];
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();  // the setup's LamParams and LamDF
+    if (adaptive_row1<false>(a, blockIdx.x, adapt_smem, threadIdx.x))
+        adaptive_row1<true>(a, blockIdx.x, adapt_smem, threadIdx.x);
+}
+
 // The queued rows: the float-float path from the first round on, one row per block of
 // blockDim.x / 32 warps (as many as the rounds kernel used: a queued row of a plain call
 // is on the pass's critical path).
@@ -590,8 +763,9 @@ __global__ void __launch_bounds__(32 * kMaxAdaptWarps, 1) adaptive_exact_kernel(
     const uint64_t n = qn < a.qcap ? qn : a.qcap;
     for (uint64_t i = blockIdx.x; i < n; i += gridDim.x) {
         const QEntry e = a.queue[i];
-        adaptive_row<true>(a, a.jobs[e.design].row_off + e.k, adapt_smem, blockDim.x >> 5, threadIdx.x >> 5,
-                           threadIdx.x & 31u);
+        const uint64_t row = a.jobs[e.design].row_off + e.k;
+        if (blockDim.x == 32u) adaptive_row1<true>(a, row, adapt_smem, threadIdx.x);
+        else adaptive_row<true>(a, row, adapt_smem, blockDim.x >> 5, threadIdx.x >> 5, threadIdx.x & 31u);
     }
 }
 
@@ -1636,13 +1810,14 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
             // decide that many rounds at once
             const uint64_t per_sm = a.total_rows / (uint64_t)num_sms;
             const uint32_t kw = per_sm >= 8 ? CPD_ADAPT_KW_MANY : per_sm >= 2 ? CPD_ADAPT_KW_SOME : kMaxAdaptWarps;
-            launch_k(adaptive_kernel, (unsigned)a.total_rows, 32 * kw, adapt_smem_bytes(kw, maxB), stream, pdl, a);
+            launch_k(kw == 1u ? adaptive1_kernel : adaptive_kernel, (unsigned)a.total_rows, 32 * kw,
+                     kw == 1u ? adapt1_smem_bytes(maxB) : adapt_smem_bytes(kw, maxB), stream, pdl, a);
             launches++;
         }
         if (ev) cudaEventRecord(ev[2], stream);
         const uint32_t kwe = a.total_rows / (uint64_t)num_sms >= 8 ? 1u : kMaxAdaptWarps;
-        launch_k(adaptive_exact_kernel, (unsigned)(num_sms * (kwe == 1u ? 8 : 1)), 32 * kwe, adapt_smem_bytes(kwe, maxB),
-                 stream, pdl, a);
+        launch_k(adaptive_exact_kernel, (unsigned)(num_sms * (kwe == 1u ? 8 : 1)), 32 * kwe,
+                 kwe == 1u ? adapt1_smem_bytes(maxB) : adapt_smem_bytes(kwe, maxB), stream, pdl, a);
         launches++;
     } else {
     if (ev) cudaEventRecord(ev[1], stream);
@@ -1697,6 +1872,9 @@ cudaError_t configure_kernels()
 {
     const int bytes = (int)adapt_smem_bytes(kMaxAdaptWarps, CPD_MAX_BINS);
     cudaError_t e = cudaFuncSetAttribute(adaptive_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(adaptive1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)adapt1_smem_bytes(CPD_MAX_BINS));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(adaptive_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
