@@ -173,8 +173,14 @@ CPD_HDN inline bool reference_ray_df(const DevDesign &D, const float *z32, LamPa
         const F2 ps = add(gu, mul(du, T));
         P.zref_hi = z.hi;
         P.zref_lo = z.lo;
-        P.dlx2 = 2.f * ex.hi;
-        P.dly2 = 2.f * ey.hi;
+        // the exit-face terms as polynomials in dz = zref - z: the point on the last flat
+        // face moves by wz dz, wz = (bx, by) bw
+        const F2 wzx = mul(bx, C.bw), wzy = mul(by, C.bw);
+        P.wzx = wzx.hi;
+        P.wzy = wzy.hi;
+        P.uz = dot(dx, dy, wzx, wzy).hi;
+        P.ca = 2.f * dot(ex, ey, wzx, wzy).hi;
+        P.cb = dot(wzx, wzy, wzx, wzy).hi;
         P.ud2 = 2.f * ud.hi;
         P.disc = disc.hi;
         P.sd = sd.hi;
@@ -388,8 +394,6 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
     if (P.core_hi < P.core_lo) P.core_hi = P.core_lo;
     if (P.band_hi < P.core_hi) P.band_hi = P.core_hi;
     if (P.band_lo > P.core_lo) P.band_lo = P.core_lo;
-    P.w1x = bx.hi;
-    P.w1y = by.hi;
     P.dx = dx.hi;
     P.dy = dy.hi;
     P.ts = ts.hi;

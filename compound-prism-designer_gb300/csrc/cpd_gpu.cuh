@@ -107,6 +107,16 @@ struct LaunchArgs {
     QEntry *queue;
     uint32_t qcap;
     uint32_t ray_tile;
+    // Single-design passes: per 32-row block, [min core_lo, max core_hi) over its rows,
+    // written by the setup (which also adds the block's length to ctl->item_counter). The
+    // trace then splits the sum of those lengths into equal shares, one per resident warp,
+    // instead of handing out work items from the counter. nullptr: work items.
+    uint2 *spans;
+    // The design's fast-path constants and thresholds when `spans` is set: read by the
+    // trace as kernel parameters (constant-bank operands), which leaves their registers to
+    // the ray loop.
+    FastConst fc;
+    FastLimits fl;
     uint32_t mode;        // CPD_TRACE_*
     uint32_t adaptive;    // per-wavelength SEM stop: 1, or 2 with every row on the exact path
     uint32_t max_B;       // widest detector of the launch
@@ -243,6 +253,10 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
                 cudaEvent_t *ev = nullptr, bool pdl = false);
 
 // Warps of the trace kernel resident at once with this block shape.
+// The kernel of a single-design pass's trace (its graph node's parameters carry the
+// design's constants and are updated per call).
+const void *trace_spans_kernel_fn();
+
 uint64_t trace_resident_warps(int num_sms, uint32_t warps_per_cta);
 
 // cpd_design records built on the device from n parameter records (one thread each).

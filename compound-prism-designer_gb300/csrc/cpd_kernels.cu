@@ -105,6 +105,43 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
 }
 
+// The setup of one wavelength row (below): LamParams and LamDF, and the row's guard-band
+// rays queued. Returns the row's fast-path range [core_lo, core_hi) (empty: hi <= lo).
+__device__ __forceinline__ uint2 setup_row(const LaunchArgs &a, uint64_t row, uint32_t d, double u,
+                                           const DevDesign &sD, uint32_t d0, bool stage_z, const float *sz)
+{
+    const DesignJob &J = a.jobs[d];
+    const uint32_t k = (uint32_t)(row - J.row_off);
+    const bool staged = d == d0;
+    const DevDesign &D = staged ? sD : a.designs[d];
+    const float *z32 = staged && stage_z ? sz : a.z32 + 2 * J.ray_off;
+    LamParams P;
+    if (D.status) {
+        // a design whose device build failed: every ray of it is lost
+        uint32_t *w = reinterpret_cast<uint32_t *>(&P);
+        for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
+        LamDF *E = a.lx + row;
+        memset(E, 0, sizeof(LamDF));
+        E->lost = 1u;
+        a.lp[row] = P;
+        return make_uint2(0u, 0u);
+    }
+    lambda_setup_df(D, u, z32, J.Rz, P, a.yguard_rel, a.lx + row, a.adaptive != 0);
+    if (a.adaptive) {
+        // the adaptive rounds trace every ray of the band themselves
+    } else if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
+        push_ranges(a, d, k, P.band_lo, P.band_hi, 0u, 0u);
+        P.core_lo = P.core_hi = 0;
+    } else if (P.all_exact) {
+        // FP32-only study mode without a reference ray: these rays are counted as lost
+        P.core_lo = P.core_hi = 0;
+    } else {
+        push_ranges(a, d, k, P.band_lo, P.core_lo, P.core_hi, P.band_hi);
+    }
+    a.lp[row] = P;
+    return make_uint2(P.core_lo, P.core_hi);
+}
+
 // One warp per block of 32 rows. The block first copies its design record and, for
 // tables of up to kStageRays rays, its sorted z table into shared memory with
 // asynchronous 16-byte copies that are all in flight at once (one memory latency
@@ -133,6 +170,15 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     const uint32_t d0 = find_job<F_ROW>(a.jobs, a.njobs, row0);
     const DesignJob &J0 = a.jobs[d0];
     const bool stage_z = J0.Rz <= kStageRays;
+    // the row's design and wavelength point, loaded while the copies below are in flight
+    // (the point is not in L2 when the previous pass's tables were evicted)
+    uint32_t d = 0;
+    double u = 0.0;
+    if (row < a.total_rows) {
+        d = find_job<F_ROW>(a.jobs, a.njobs, row);
+        const DesignJob &J = a.jobs[d];
+        u = a.lam_u[J.lam_off + (row - J.row_off)];
+    }
     {
         const char *src = reinterpret_cast<const char *>(a.designs + d0);
         char *dst = reinterpret_cast<char *>(&sD);
@@ -146,42 +192,143 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
         asm volatile("cp.async.wait_all;" ::: "memory");
     }
     __syncthreads();
-    if (row >= a.total_rows) return;
-    const uint32_t d = find_job<F_ROW>(a.jobs, a.njobs, row);
-    const DesignJob &J = a.jobs[d];
-    const uint32_t k = (uint32_t)(row - J.row_off);
-    const bool staged = d == d0;
-    const DevDesign &D = staged ? sD : a.designs[d];
-    const float *z32 = staged && stage_z ? sz : a.z32 + 2 * J.ray_off;
-    LamParams P;
-    if (D.status) {
-        // a design whose device build failed: every ray of it is lost
-        uint32_t *w = reinterpret_cast<uint32_t *>(&P);
-        for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
-        LamDF *E = a.lx + row;
-        memset(E, 0, sizeof(LamDF));
-        E->lost = 1u;
-        a.lp[row] = P;
-        return;
+    uint2 core = make_uint2(0u, 0u);
+    if (row < a.total_rows) core = setup_row(a, row, d, u, sD, d0, stage_z, sz);
+    if (a.spans) {
+        // single-design pass: this block's 32 rows are the trace's block blockIdx.x
+        const bool any = core.y > core.x;
+        const uint32_t lo = __reduce_min_sync(0xffffffffu, any ? core.x : 0xffffffffu);
+        const uint32_t hi = __reduce_max_sync(0xffffffffu, any ? core.y : 0u);
+        if (threadIdx.x == 0) {
+            const uint2 s = hi > lo ? make_uint2(lo, hi) : make_uint2(0u, 0u);
+            a.spans[blockIdx.x] = s;
+            if (s.y > s.x) atomicAdd(&a.ctl->item_counter, (unsigned long long)(s.y - s.x));
+        }
     }
-    lambda_setup_df(D, a.lam_u[J.lam_off + k], z32, J.Rz, P, a.yguard_rel, a.lx + row, a.adaptive != 0);
-    if (a.adaptive) {
-        // the adaptive rounds trace every ray of the band themselves
-    } else if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
-        push_ranges(a, d, k, P.band_lo, P.band_hi, 0u, 0u);
-        P.core_lo = P.core_hi = 0;
-    } else if (P.all_exact) {
-        // FP32-only study mode without a reference ray: these rays are counted as lost
-        P.core_lo = P.core_hi = 0;
-    } else {
-        push_ranges(a, d, k, P.band_lo, P.core_lo, P.core_hi, P.band_hi);
-    }
-    a.lp[row] = P;
 }
 
 #ifndef CPD_TRACE_MIN_BLOCKS
 #define CPD_TRACE_MIN_BLOCKS 3
 #endif
+
+// The rays [j0, j1) of the 32-row block blk of design d (lane = row), each lane clamped
+// to its row's fast-path range: FP32 fast path, hits as run-length fixed-point sums
+// flushed with one 64-bit atomic per run, guard-band rays queued for the re-trace.
+template <bool PARAM_FC>
+__device__ __forceinline__ void trace_block_rays(const LaunchArgs &a, uint32_t d, const DesignJob &J, uint32_t blk,
+                                                 uint32_t j0, uint32_t j1, uint32_t lane)
+{
+    const uint32_t k = blk * 32u + lane;
+    // the design's constants: kernel parameters (constant-bank operands, no registers)
+    // for a single-design pass, else a copy in registers
+    const FastConst Cd = PARAM_FC ? FastConst{} : a.designs[d].fc;
+    const FastConst &C = PARAM_FC ? a.fc : Cd;
+    const FastLimits Ld = PARAM_FC ? FastLimits{} : fast_limits(Cd, a.guards);
+    const FastLimits &Lm = PARAM_FC ? a.fl : Ld;
+    LamParams P;
+    uint32_t lo = 0, hi = 0;
+    if (k < J.W) {
+        P = a.lp[J.row_off + k];
+        lo = max(j0, P.core_lo);
+        hi = min(j1, P.core_hi);
+    }
+    const float2 *__restrict__ zt = reinterpret_cast<const float2 *>(a.z32) + J.ray_off;
+    unsigned long long *hrow = a.hist + J.hist_off + (uint64_t)k * J.B;
+    uint32_t cur = 0xffffffffu;
+    unsigned long long sum = 0ull;
+    uint32_t nhit = 0;
+    for (uint32_t j = lo; j < hi; ++j) {
+        const float2 z = __ldg(zt + j);
+        uint32_t bin = 0;
+        float t = 0.f;
+        const int r = fast_ray(C, Lm, P, a.guards, z.x, z.y, bin, t);
+        if (r == RAY_HIT) {
+            if (bin != cur) {
+                if (sum) atomicAdd(hrow + cur, sum);
+                cur = bin;
+                sum = 0ull;
+            }
+            sum += t_fixed(t);
+            nhit++;
+        } else if (r == RAY_FLAG) {
+            push_ray(a, d, k, j);
+        }
+    }
+    if (sum) atomicAdd(hrow + cur, sum);
+    nhit = __reduce_add_sync(0xffffffffu, nhit);
+    const uint32_t nfast = __reduce_add_sync(0xffffffffu, hi > lo ? hi - lo : 0u);
+    const uint32_t sp = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % (uint32_t)kSpread;
+    if (lane == 0 && nhit) atomicAdd(&a.acc[d].hits[sp], (unsigned long long)nhit);
+    if (lane == 0 && nfast) atomicAdd(&a.acc[d].fast[sp], (unsigned long long)nfast);
+}
+
+// The trace of a single-design pass whose setup wrote the blocks' spans (a.spans). Its
+// design constants are kernel parameters (constant-bank operands), which takes the ray
+// loop from 80 to 71 registers. Measured on the 4096 x 1024 plain pass: at 64 registers
+// (4 blocks of 256 per SM, 32 warps, no spill) the trace issues 68% of the slots against
+// 62%, but fills the register file, so the re-trace and entropy blocks can no longer
+// become resident while it runs, and the pass is ~1.5 us slower than at 3 blocks per SM.
+#ifndef CPD_TRACE_SPANS_MIN_BLOCKS
+#define CPD_TRACE_SPANS_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(256, CPD_TRACE_SPANS_MIN_BLOCKS) trace_spans_kernel(const LaunchArgs a)
+{
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();  // setup's LamParams and queue
+    const uint32_t lane = threadIdx.x & 31u;
+    // Equal shares of the design's fast-path ray slots: the blocks' spans laid end to
+    // end (U slots in all), warp w taking [U w / nw, U (w + 1) / nw). A warp's lanes
+    // step through a block's span together, so a span costs its length whatever the
+    // rows' own ranges; every warp gets the same work and no warp waits on a counter.
+    // Nothing stays live in registers across a segment's ray loop (which needs every
+    // register it can get): the cursor waits in shared memory, and the share's end and the
+    // prefix over the spans are found again from the pass's words for each segment.
+    __shared__ volatile unsigned long long s_cur[8];  // per warp of the block (<= 256 threads)
+    {
+        const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+        const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+        s_cur[threadIdx.x >> 5] = a.ctl->item_counter * w / nw;  // the next slot of this warp's share
+    }
+    for (;;) {
+        __syncwarp();
+        uint64_t cur = s_cur[threadIdx.x >> 5];
+        const uint64_t end = a.ctl->item_counter * (((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) + 1u) /
+                             (((uint64_t)gridDim.x * blockDim.x) >> 5);
+        if (cur >= end) break;
+        const uint32_t nb = (a.jobs[0].W + 31u) / 32u;
+        uint64_t pre = 0;  // slots of the blocks before group c
+        uint32_t c = 0, sx, len, incl;
+        for (;;) {
+            const uint32_t b = c + lane;
+            const uint2 s = b < nb ? a.spans[b] : make_uint2(0u, 0u);
+            sx = s.x;
+            len = s.y - s.x;
+            incl = len;  // inclusive scan over the group
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += v;
+            }
+            const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+            if (pre + tot > cur) break;
+            pre += tot;
+            c += 32u;
+        }
+        // the block holding the cursor: the first whose end lies past it (nonempty)
+        const int l = __ffs(__ballot_sync(0xffffffffu, pre + incl > cur)) - 1;
+        const uint32_t bx = __shfl_sync(0xffffffffu, sx, l);
+        const uint32_t ln = __shfl_sync(0xffffffffu, len, l);
+        const uint64_t e0 = pre + __shfl_sync(0xffffffffu, incl, l) - ln;
+        const uint64_t rem = end - e0;
+        const uint32_t stop = rem < ln ? (uint32_t)rem : ln;
+        const uint32_t r0 = bx + (uint32_t)(cur - e0);
+        __syncwarp();
+        s_cur[threadIdx.x >> 5] = e0 + stop;
+        const DesignJob J = a.jobs[0];
+        trace_block_rays<true>(a, 0u, J, c + (uint32_t)l, r0, bx + stop, lane);
+    }
+}
+
 __global__ void __launch_bounds__(256, CPD_TRACE_MIN_BLOCKS) trace_kernel(const LaunchArgs a)
 {
     cudaTriggerProgrammaticLaunchCompletion();
@@ -197,45 +344,8 @@ __global__ void __launch_bounds__(256, CPD_TRACE_MIN_BLOCKS) trace_kernel(const 
         const uint64_t local = item - J.item_off;
         const uint32_t blk = (uint32_t)(local / J.nchunk);
         const uint32_t chunk = (uint32_t)(local - (uint64_t)blk * J.nchunk);
-        const uint32_t k = blk * 32u + lane;
-        const FastConst C = a.designs[d].fc;
-        LamParams P;
-        uint32_t lo = 0, hi = 0;
-        if (k < J.W) {
-            P = a.lp[J.row_off + k];
-            const uint32_t j0 = chunk * a.ray_tile;
-            const uint32_t j1 = min(j0 + a.ray_tile, J.Rz);
-            lo = max(j0, P.core_lo);
-            hi = min(j1, P.core_hi);
-        }
-        const float2 *__restrict__ zt = reinterpret_cast<const float2 *>(a.z32) + J.ray_off;
-        unsigned long long *hrow = a.hist + J.hist_off + (uint64_t)k * J.B;
-        uint32_t cur = 0xffffffffu;
-        unsigned long long sum = 0ull;
-        uint32_t nhit = 0;
-        for (uint32_t j = lo; j < hi; ++j) {
-            const float2 z = __ldg(zt + j);
-            uint32_t bin = 0;
-            float t = 0.f;
-            const int r = fast_ray(C, P, a.guards, z.x, z.y, bin, t);
-            if (r == RAY_HIT) {
-                if (bin != cur) {
-                    if (sum) atomicAdd(hrow + cur, sum);
-                    cur = bin;
-                    sum = 0ull;
-                }
-                sum += t_fixed(t);
-                nhit++;
-            } else if (r == RAY_FLAG) {
-                push_ray(a, d, k, j);
-            }
-        }
-        if (sum) atomicAdd(hrow + cur, sum);
-        nhit = __reduce_add_sync(0xffffffffu, nhit);
-        const uint32_t nfast = __reduce_add_sync(0xffffffffu, hi > lo ? hi - lo : 0u);
-        const uint32_t sp = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % (uint32_t)kSpread;
-        if (lane == 0 && nhit) atomicAdd(&a.acc[d].hits[sp], (unsigned long long)nhit);
-        if (lane == 0 && nfast) atomicAdd(&a.acc[d].fast[sp], (unsigned long long)nfast);
+        const uint32_t j0 = chunk * a.ray_tile;
+        trace_block_rays<false>(a, d, J, blk, j0, min(j0 + a.ray_tile, J.Rz), lane);
     }
 }
 
@@ -1824,12 +1934,14 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
     if (a.mode != CPD_TRACE_FP64 && a.total_items) {
         int per_sm = 0;
         const int threads = (int)warps_per_cta * 32;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel, threads, 0);
+        auto k = a.spans ? trace_spans_kernel : trace_kernel;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, 0);
         if (per_sm < 1) per_sm = 1;
         uint64_t grid = (uint64_t)num_sms * per_sm;
+        // equal shares: every resident warp; work items: no more warps than items
         const uint64_t need = (a.total_items + warps_per_cta - 1) / warps_per_cta;
-        if (grid > need) grid = need;
-        launch_k(trace_kernel, (unsigned)grid, threads, 0, stream, pdl, a);
+        if (!a.spans && grid > need) grid = need;
+        launch_k(k, (unsigned)grid, threads, 0, stream, pdl, a);
         launches++;
     }
     if (ev) cudaEventRecord(ev[2], stream);
@@ -1879,6 +1991,8 @@ cudaError_t configure_kernels()
         e = cudaFuncSetAttribute(adaptive_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
 }
+
+const void *trace_spans_kernel_fn() { return reinterpret_cast<const void *>(trace_spans_kernel); }
 
 uint64_t trace_resident_warps(int num_sms, uint32_t warps_per_cta)
 {

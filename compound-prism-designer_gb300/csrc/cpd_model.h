@@ -127,10 +127,10 @@ struct alignas(16) DevDesign {
 // distance to the detector.
 struct alignas(16) LamParams {
     float zref_hi, zref_lo;     // z of the reference ray (f32 hi + lo parts)
-    float w1x, w1y;             // d(position on the last flat face)/dy
+    float wzx, wzy;             // d(position on the last flat face)/d(zref - z) = (dw/dy) bw
     float dx, dy;               // direction entering the exit face (same for every ray)
     float ts, tp;               // s/p transmittance entering the exit face
-    float dlx2, dly2;           // 2 (w_ref - c): ray point on the last face relative to the centre
+    float ca, cb;               // d(cq) = dz (ca + cb dz): ca = 2 (w_ref - c).wz, cb = |wz|^2
     float ud2, disc, sd;        // reference: 2 d.(w - c), discriminant, its square root
     float sigma;                // root sign: s = -ud + sigma*sd
     float s, px2, py2, mb;      // reference root, 2 p_ref (rel. bound centre), |p|^2 - rho^2
@@ -141,7 +141,8 @@ struct alignas(16) LamParams {
     uint32_t core_lo, core_hi;  // sorted-ray range that clears every flat face (fast path)
     uint32_t band_lo, band_hi;  // [band_lo, core_lo) and [core_hi, band_hi): guard bands
     uint32_t all_exact;         // no usable reference ray: every core ray is re-traced exactly
-    uint32_t pad[3];
+    float uz;                   // d(ud) = uz dz: d.wz
+    uint32_t pad[2];
 };
 
 
@@ -570,30 +571,45 @@ CPD_HD float mulr(float a, float b) { return ff::mul_rn(a, b); }
 CPD_HD float addr(float a, float b) { return ff::add_rn(a, b); }
 CPD_HD float subr(float a, float b) { return ff::sub_rn(a, b); }
 
-CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, float zhi, float zlo, uint32_t &bin,
-                    float &t)
+// The fast path's thresholds that combine a design constant with a guard, rounded once
+// (the same operations wherever they are formed: per work item on the device, or on the
+// host for a pass whose design constants are kernel parameters).
+struct FastLimits {
+    float rho101;  // 1.01 rho: a root whose other root may lie inside the bound
+    float rho2g;   // guard on |p|^2 - rho^2
+    float ci_lo;   // min_ci - cosine guard
+    float ci_hi;   // min_ci + cosine guard
+};
+CPD_HD FastLimits fast_limits(const FastConst &D, const Guards &g)
 {
-    // start-height difference from the reference ray: y = bym - bw z
+    return FastLimits{mulr(1.01f, D.rho), mulr(g.rel, D.rho2), subr(D.min_ci, g.cosine), addr(D.min_ci, g.cosine)};
+}
+
+CPD_HD int fast_ray(const FastConst &D, const FastLimits &Lm, const LamParams &P, const Guards &g, float zhi,
+                    float zlo, uint32_t &bin, float &t)
+{
+    // start-height difference from the reference ray (y = bym - bw z): the point on the
+    // last flat face moves by dw = wz dz
     const float dz = addr(subr(P.zref_hi, zhi), subr(P.zref_lo, zlo));
-    const float dyy = mulr(D.bw, dz);
-    const float dwx = mulr(P.w1x, dyy), dwy = mulr(P.w1y, dyy);
-    // exit face: s^2 + 2 ud s + cq = 0, ud = d.(w - c), cq = |w - c|^2 - Rc^2
-    const float dud = fmaf(P.dx, dwx, mulr(P.dy, dwy));
-    const float dcq = fmaf(dwx, addr(P.dlx2, dwx), mulr(dwy, addr(P.dly2, dwy)));
+    const float dwx = mulr(P.wzx, dz), dwy = mulr(P.wzy, dz);
+    // exit face: s^2 + 2 ud s + cq = 0, ud = d.(w - c), cq = |w - c|^2 - Rc^2; both change
+    // by polynomials in dz whose coefficients the setup formed in float-float
+    const float dud = mulr(P.uz, dz);
+    const float dcq = mulr(dz, fmaf(P.cb, dz, P.ca));
     const float ddisc = fmaf(dud, addr(P.ud2, dud), -dcq);
     const float disc = addr(P.disc, ddisc);
     const float gdisc = mulr(g.rel, P.disc);
     if (disc <= gdisc) return disc > -gdisc ? RAY_FLAG : RAY_LOST;
     const float sd = sqrt_fast(disc);
     // the other root is 2 sd away along the ray: outside the bound when sd > rho
-    bool flag = sd < mulr(1.01f, D.rho);
+    bool flag = sd < Lm.rho101;
     const float dsd = div_fast(ddisc, addr(sd, P.sd));
     const float ds = fmaf(P.sigma, dsd, -dud);
     const float s = addr(P.s, ds);
     flag |= fabs_f(s) < g.dist;
     const float dpx = fmaf(P.dx, ds, dwx), dpy = fmaf(P.dy, ds, dwy);
     const float mb = addr(P.mb, fmaf(dpx, addr(P.px2, dpx), mulr(dpy, addr(P.py2, dpy))));
-    flag |= fabs_f(mb) < mulr(g.rel, D.rho2);
+    flag |= fabs_f(mb) < Lm.rho2g;
     if ((s < 0.f) | (mb > 0.f)) return flag ? RAY_FLAG : RAY_LOST;
     // refraction into air at the exit face, normal n = (c - p)/Rc
     const float dnx = -mulr(dpx, D.inv_rc), dny = -mulr(dpy, D.inv_rc);
@@ -607,24 +623,24 @@ CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, flo
     const float dkk = fmaf(P.r, dci, -dcr);
     const float nx = addr(P.nx, dnx), ny = addr(P.ny, dny);
     const float dex = fmaf(P.kk, dnx, mulr(dkk, nx)), dey = fmaf(P.kk, dny, mulr(dkk, ny));
-    float ts = P.ts, tp = P.tp;
+    // the ray's transmittance t = (ts + tp) / 2 after the exit face
+    float tr;
     if (D.ar) flag |= fabs_f(subr(ci, 0.5f)) < g.cosine;
     if (D.ar && ci > 0.5f) {
-        ts = mulr(ts, 0.99f);
-        tp = mulr(tp, 0.99f);
+        tr = mulr(addr(P.ts, P.tp), 0.495f);  // 0.99 (ts + tp) / 2
     } else {
-        // 1 - Rs = 4 n1 n2 ci cr / (n1 ci + n2 cr)^2, 1 - Rp likewise with ci<->cr (n2 = 1)
+        // 1 - Rs = 4 n1 n2 ci cr / a^2, 1 - Rp = 4 n1 n2 ci cr / b^2 (n2 = 1), a = r ci + cr,
+        // b = r cr + ci: t = 2 r ci cr (ts b^2 + tp a^2) / (a^2 b^2)
         const float r = P.r;
         const float a = fmaf(r, ci, cr), b = fmaf(r, cr, ci);
         const float a2 = mulr(a, a), b2 = mulr(b, b);
-        const float inv = div_fast(mulr(mulr(mulr(4.f, r), ci), cr), mulr(a2, b2));
-        ts = mulr(ts, mulr(b2, inv));
-        tp = mulr(tp, mulr(a2, inv));
+        const float q = div_fast(mulr(mulr(mulr(2.f, r), ci), cr), mulr(a2, b2));
+        tr = mulr(q, fmaf(P.ts, b2, mulr(P.tp, a2)));
     }
     // detector line
     const float dcid = -fmaf(dex, D.dnfx, mulr(dey, D.dnfy));
     const float cid = addr(P.cid, dcid);
-    if (cid <= addr(D.min_ci, g.cosine)) return cid > subr(D.min_ci, g.cosine) ? RAY_FLAG : RAY_LOST;
+    if (cid <= Lm.ci_hi) return cid > Lm.ci_lo ? RAY_FLAG : RAY_LOST;
     const float dgn = fmaf(dpx, D.dnfx, mulr(dpy, D.dnfy));
     const float dgu = fmaf(dpx, D.dufx, mulr(dpy, D.dufy));
     const float ddu = fmaf(dex, D.dufx, mulr(dey, D.dufy));
@@ -634,8 +650,8 @@ CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, flo
     const float pos = addr(P.pos, dpos);
     // The position is the one unbounded quantity (a reference ray can land metres from
     // the detector): its guard grows with the magnitudes it was summed from.
-    const float mag = addr(addr(addr(fabs_f(P.pos), fabs_f(tu)), fabs_f(tt)), fabs_f(dgu));
-    const float gp = fmaf(g.pos_rel, mag, g.pos);
+    const float gp = fmaf(g.pos_rel, addr(addr(fabs_f(tu), fabs_f(tt)), fabs_f(dgu)),
+                          fmaf(g.pos_rel, fabs_f(P.pos), g.pos));
     // 0 <= pos <= L, as a distance from the detector's middle
     const float dm = fabs_f(subr(pos, D.hL));
     if (dm > addr(D.hL, gp)) return RAY_LOST;
@@ -654,10 +670,15 @@ CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, flo
 #endif
     if ((b < D.B) & (rem < D.bin_size)) {
         bin = b;
-        t = mulr(addr(ts, tp), 0.5f);
+        t = tr;
         return RAY_HIT;
     }
     return RAY_LOST;
+}
+CPD_HD int fast_ray(const FastConst &D, const LamParams &P, const Guards &g, float zhi, float zlo, uint32_t &bin,
+                    float &t)
+{
+    return fast_ray(D, fast_limits(D, g), P, g, zhi, zlo, bin, t);
 }
 
 }  // namespace cpd

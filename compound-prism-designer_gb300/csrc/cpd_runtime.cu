@@ -91,6 +91,28 @@ struct RayKey {
 
 // The sampling flags a trace mode may carry.
 constexpr uint32_t kSamplingBits = CPD_SAMPLING_ADAPTIVE | CPD_SAMPLING_EXACT;
+// Most rows of a pass whose trace takes equal shares of span slots: every warp scans the
+// blocks' spans (32 per step) to find its share.
+constexpr uint64_t kBalancedMaxRows = 16384;
+#ifndef CPD_TRACE_SPANS
+#define CPD_TRACE_SPANS 1  // 0: single-design passes take work items from the counter too
+#endif
+
+// The kernel node of `fn` in a captured graph (nullptr if none).
+cudaGraphNode_t find_kernel_node(cudaGraph_t g, const void *fn)
+{
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return nullptr;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return nullptr;
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams kp{};
+        if (cudaGraphKernelNodeGetParams(nd, &kp) == cudaSuccess && kp.func == fn) return nd;
+    }
+    return nullptr;
+}
 
 // Everything one pass needs on the device, plus its staging and its captured graph.
 // A context owns one slot (the synchronous calls); a server owns several, so that
@@ -115,6 +137,12 @@ struct PassSlot {
         std::vector<uint8_t> key;
         cudaGraphExec_t exec;
         int launches;
+        // a single-design pass: the captured graph (kept: its node handle addresses the
+        // exec's node), the trace node, and the launch arguments it holds, whose design
+        // constants (fc, fl) change from call to call while the key stays the same
+        cudaGraph_t graph = nullptr;
+        cudaGraphNode_t trace_node = nullptr;
+        LaunchArgs args{};
     };
     std::vector<CachedGraph> graphs;
     static constexpr size_t kGraphCache = 8;
@@ -148,7 +176,10 @@ struct PassSlot {
     void destroy()
     {
         if (stream) cudaStreamSynchronize(stream);
-        for (CachedGraph &c : graphs) cudaGraphExecDestroy(c.exec);
+        for (CachedGraph &c : graphs) {
+            cudaGraphExecDestroy(c.exec);
+            if (c.graph) cudaGraphDestroy(c.graph);
+        }
         graphs.clear();
         for (DevBuf *b : {&in, &lp, &lx, &hist, &S1, &S2, &acc, &queue, &pout}) b->release();
         for (HostBuf *b : {&h_in, &h_outs}) b->release();
@@ -399,7 +430,8 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     const void *bufs_before[] = {S.lp.p, S.lx.p, S.hist.p, S.S1.p, S.S2.p, S.acc.p, S.queue.p, S.h_in.p, S.h_outs.p, in_before};
     const size_t hist_bytes = sizeof(unsigned long long) * std::max<uint64_t>(hist, 1);
     const size_t old_hist = S.hist.cap;
-    CPD_TRY(S.lp.ensure(sizeof(LamParams) * std::max<uint64_t>(rows, 1)));
+    // the LamParams, then (single-design passes) one span per 32-row block
+    CPD_TRY(S.lp.ensure(sizeof(LamParams) * std::max<uint64_t>(rows, 1) + sizeof(uint2) * ((rows + 31) / 32)));
     CPD_TRY(S.lx.ensure(sizeof(LamDF) * std::max<uint64_t>(rows, 1)));
     CPD_TRY(S.hist.ensure(hist_bytes));
     if (S.hist.cap != old_hist) S.hist_dirty = true;
@@ -459,6 +491,16 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         a.guards = default_guards();
         a.yguard_rel = kYGuardRel;
     }
+    // One host-built design with a fixed ray count: the trace splits its rays into equal
+    // shares per warp (no work-item counter, no tail of unequal items) and reads the
+    // design's constants as kernel parameters. The bound on rows x rays keeps each warp's
+    // share arithmetic in range.
+    if (CPD_TRACE_SPANS && n == 1 && !on_device && !adaptive && mode != CPD_TRACE_FP64 &&
+        rows <= kBalancedMaxRows && rows * (uint64_t)jobs[0].Rz <= (1ull << 31)) {
+        a.spans = reinterpret_cast<uint2 *>(S.lp.as<LamParams>() + rows);
+        a.fc = ds[0].dev->fc;
+        a.fl = fast_limits(a.fc, a.guards);
+    }
     a.p_out = p_out_host ? S.pout.as<double>() : nullptr;
     a.logtab = ctx->logtab.as<float>();
     if (on_device) {
@@ -469,8 +511,15 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     // The device work of a pass, captured once per signature and replayed.
     // The whole pass -- input upload, accumulator clears, kernels, read-back, and the two
     // timing events around the kernels -- is one graph, captured once per signature.
+    // The design constants of a single-design pass are not part of the key: the cached
+    // graph's trace node gets them per call.
     std::vector<uint8_t> key(sizeof(a) + 8 * sizeof(uint64_t));
-    std::memcpy(key.data(), &a, sizeof(a));
+    {
+        LaunchArgs ka = a;
+        std::memset(&ka.fc, 0, sizeof(ka.fc));
+        std::memset(&ka.fl, 0, sizeof(ka.fl));
+        std::memcpy(key.data(), &ka, sizeof(ka));
+    }
     const uint64_t extra[8] = {n, ctx->warps_per_cta, (uint64_t)ctx->num_sms, (in_bytes << 1) | (resident ? 1u : 0u),
                                out_bytes, fresh ? accc + 1 : 0, S.buf_gen, (uint64_t)(uintptr_t)S.h_in.p};
     std::memcpy(key.data() + sizeof(a), extra, sizeof(extra));
@@ -496,18 +545,43 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
             CPD_TRY(cudaStreamEndCapture(s, &g));
             cudaGraphExec_t exec = nullptr;
             const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
-            cudaGraphDestroy(g);
+            if (e != cudaSuccess) cudaGraphDestroy(g);
             CPD_TRY(e);
+            PassSlot::CachedGraph c{key, exec, launches};
+            c.args = a;
+            if (a.spans) {
+                c.graph = g;
+                c.trace_node = find_kernel_node(g, trace_spans_kernel_fn());
+                if (!c.trace_node) {
+                    cudaGraphExecDestroy(exec);
+                    cudaGraphDestroy(g);
+                    return CPD_CUDA_ERROR;
+                }
+            } else {
+                cudaGraphDestroy(g);
+            }
             if (S.graphs.size() >= PassSlot::kGraphCache) {
                 cudaGraphExecDestroy(S.graphs.back().exec);
+                if (S.graphs.back().graph) cudaGraphDestroy(S.graphs.back().graph);
                 S.graphs.pop_back();
             }
-            S.graphs.insert(S.graphs.begin(), PassSlot::CachedGraph{key, exec, launches});
+            S.graphs.insert(S.graphs.begin(), c);
         } else if (hit != S.graphs.begin()) {
             std::rotate(S.graphs.begin(), hit, hit + 1);  // most recently used first
         }
-        CPD_TRY(cudaGraphLaunch(S.graphs.front().exec, s));
-        S.launches = S.graphs.front().launches;
+        PassSlot::CachedGraph &cg = S.graphs.front();
+        if (cg.trace_node && (std::memcmp(&cg.args.fc, &a.fc, sizeof(a.fc)) != 0 ||
+                              std::memcmp(&cg.args.fl, &a.fl, sizeof(a.fl)) != 0)) {
+            cudaKernelNodeParams kp{};
+            CPD_TRY(cudaGraphKernelNodeGetParams(cg.trace_node, &kp));
+            void *args[] = {&a};
+            kp.kernelParams = args;
+            kp.extra = nullptr;
+            CPD_TRY(cudaGraphExecKernelNodeSetParams(cg.exec, cg.trace_node, &kp));
+            cg.args = a;
+        }
+        CPD_TRY(cudaGraphLaunch(cg.exec, s));
+        S.launches = cg.launches;
     } else {
         S.launches = record(s, false);
         CPD_TRY(cudaGetLastError());

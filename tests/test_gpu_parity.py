@@ -204,6 +204,25 @@ def test_repeat_calls_identical(designs):
     assert a.as_dict() == b.as_dict()
 
 
+def test_alternating_designs_reuse_the_pass_graph():
+    """Designs of one shape share a captured pass graph; the single-design trace reads
+    each design's constants from that graph's kernel parameters, which every call
+    updates. Alternating designs on one context must give each design the bits it gets
+    on a context of its own, and agree with the oracle."""
+    rng = np.random.default_rng(515)
+    cases = [synth.random_design(rng, 6, 64)[:2] for _ in range(3)]
+    lam_u, ray_u = O.qrng_points(0.5, 256), O.qrng_points(0.5, 1024)
+    fresh = [s.gpu_fitness_points(lam_u, ray_u, want_p=True, context=cpd.Context(0)) for s, _ in cases]
+    ctx = cpd.Context(0)
+    for _ in range(2):
+        for (s, d), (f0, p0) in zip(cases, fresh):
+            f, p = s.gpu_fitness_points(lam_u, ray_u, want_p=True, context=ctx)
+            assert f.info == f0.info and f.hits == f0.hits and np.array_equal(p, p0)
+    for (s, d), (f0, p0) in zip(cases, fresh):
+        po, st = O.fitness_points(d, lam_u, ray_u, nthreads=NTHREADS)
+        assert np.abs(p0 - po).max() <= 1e-6 and f0.hits == st["hits"]
+
+
 @pytest.mark.parametrize("B", [1, 1024])
 def test_detector_size_extremes(B):
     """One bin, and the largest detector the ABI accepts (CPD_MAX_BINS = 1024 bins, the
