@@ -189,8 +189,8 @@ CPD_HDN inline bool reference_ray_df(const DevDesign &D, const float *z32, LamPa
         P.px2 = 2.f * px.hi;
         P.py2 = 2.f * py.hi;
         P.mb = mb.hi;
-        P.nx = nx.hi;
-        P.ny = ny.hi;
+        P.nf = dot(nx, ny, C.dnx, C.dny).hi;
+        P.nu = dot(nx, ny, C.dux, C.duy).hi;
         P.ci = ci.hi;
         P.ci2 = 2.f * ci.hi;
         P.crsq = crsq.hi;
@@ -199,7 +199,6 @@ CPD_HDN inline bool reference_ray_df(const DevDesign &D, const float *z32, LamPa
         P.r2 = sqr(r).hi;
         P.kk = kk.hi;
         P.cid = cid.hi;
-        P.gn = gn.hi;
         P.T = T.hi;
         P.du = du.hi;
         P.pos = ps.hi;

@@ -134,15 +134,15 @@ struct alignas(16) LamParams {
     float ud2, disc, sd;        // reference: 2 d.(w - c), discriminant, its square root
     float sigma;                // root sign: s = -ud + sigma*sd
     float s, px2, py2, mb;      // reference root, 2 p_ref (rel. bound centre), |p|^2 - rho^2
-    float nx, ny;               // reference exit-face normal (c - p)/Rc
+    float nf, nu;               // reference exit-face normal (c - p)/Rc . detector normal, . direction
     float ci, ci2, crsq, cr;    // reference cosines (ci2 = 2 ci)
     float r, r2, kk;            // n_last, n_last^2, r ci - cr
-    float cid, gn, T, du, pos;  // reference detector cosine, (p - P).N, gn/cid, d'.u, position
+    float cid, T, du, pos;      // reference detector cosine, distance (p - P).N / cid, d'.u, position
     uint32_t core_lo, core_hi;  // sorted-ray range that clears every flat face (fast path)
     uint32_t band_lo, band_hi;  // [band_lo, core_lo) and [core_hi, band_hi): guard bands
     uint32_t all_exact;         // no usable reference ray: every core ray is re-traced exactly
     float uz;                   // d(ud) = uz dz: d.wz
-    uint32_t pad[2];
+    uint32_t pad[3];
 };
 
 
@@ -611,9 +611,9 @@ CPD_HD int fast_ray(const FastConst &D, const FastLimits &Lm, const LamParams &P
     const float mb = addr(P.mb, fmaf(dpx, addr(P.px2, dpx), mulr(dpy, addr(P.py2, dpy))));
     flag |= fabs_f(mb) < Lm.rho2g;
     if ((s < 0.f) | (mb > 0.f)) return flag ? RAY_FLAG : RAY_LOST;
-    // refraction into air at the exit face, normal n = (c - p)/Rc
-    const float dnx = -mulr(dpx, D.inv_rc), dny = -mulr(dpy, D.inv_rc);
-    const float dci = -fmaf(P.dx, dnx, mulr(P.dy, dny));
+    // refraction into air at the exit face, normal n = (c - p)/Rc, so dn = -dp/Rc and
+    // dci = -d.dn = (d.dp)/Rc = (ds + dud)/Rc (|d| = 1)
+    const float dci = mulr(addr(ds, dud), D.inv_rc);
     const float ci = addr(P.ci, dci);
     const float dcr2 = mulr(mulr(P.r2, dci), addr(P.ci2, dci));
     const float crsq = addr(P.crsq, dcr2);
@@ -621,8 +621,6 @@ CPD_HD int fast_ray(const FastConst &D, const FastLimits &Lm, const LamParams &P
     const float cr = sqrt_fast(crsq);
     const float dcr = div_fast(dcr2, addr(cr, P.cr));
     const float dkk = fmaf(P.r, dci, -dcr);
-    const float nx = addr(P.nx, dnx), ny = addr(P.ny, dny);
-    const float dex = fmaf(P.kk, dnx, mulr(dkk, nx)), dey = fmaf(P.kk, dny, mulr(dkk, ny));
     // the ray's transmittance t = (ts + tp) / 2 after the exit face
     float tr;
     if (D.ar) flag |= fabs_f(subr(ci, 0.5f)) < g.cosine;
@@ -637,14 +635,18 @@ CPD_HD int fast_ray(const FastConst &D, const FastLimits &Lm, const LamParams &P
         const float q = div_fast(mulr(mulr(mulr(2.f, r), ci), cr), mulr(a2, b2));
         tr = mulr(q, fmaf(P.ts, b2, mulr(P.tp, a2)));
     }
-    // detector line
-    const float dcid = -fmaf(dex, D.dnfx, mulr(dey, D.dnfy));
-    const float cid = addr(P.cid, dcid);
-    if (cid <= Lm.ci_hi) return cid > Lm.ci_lo ? RAY_FLAG : RAY_LOST;
+    // detector line (normal N, direction U). The exit direction e = r d + kk n changes by
+    // de = kk_ref dn + dkk n; with dn = -dp/Rc its components along N and U follow from
+    // dgn = dp.N and dgu = dp.U: de.N = dkk nf - (kk_ref + dkk) dgn/Rc, likewise for U
     const float dgn = fmaf(dpx, D.dnfx, mulr(dpy, D.dnfy));
     const float dgu = fmaf(dpx, D.dufx, mulr(dpy, D.dufy));
-    const float ddu = fmaf(dex, D.dufx, mulr(dey, D.dufy));
-    const float dT = div_fast(fmaf(dgn, P.cid, -mulr(P.gn, dcid)), mulr(cid, P.cid));
+    const float kn = mulr(addr(P.kk, dkk), D.inv_rc);
+    const float dcid = fmaf(dgn, kn, -mulr(dkk, P.nf));  // cid = -e.N
+    const float cid = addr(P.cid, dcid);
+    if (cid <= Lm.ci_hi) return cid > Lm.ci_lo ? RAY_FLAG : RAY_LOST;
+    const float ddu = fmaf(-dgu, kn, mulr(dkk, P.nu));
+    // T = gn / cid: dT = (dgn - T_ref dcid) / cid
+    const float dT = div_fast(fmaf(-P.T, dcid, dgn), cid);
     const float tu = mulr(ddu, addr(P.T, dT)), tt = mulr(P.du, dT);
     const float dpos = addr(tu, addr(tt, dgu));
     const float pos = addr(P.pos, dpos);
