@@ -214,9 +214,30 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
 // The rays [j0, j1) of the 32-row block blk of design d (lane = row), each lane clamped
 // to its row's fast-path range: FP32 fast path, hits as run-length fixed-point sums
 // flushed with one 64-bit atomic per run, guard-band rays queued for the re-trace.
+// Flagged rays a warp of the single-design trace keeps for its own re-trace.
+constexpr uint32_t kWarpFlags = 32;
+
+// The float-float re-trace of one queued ray (k, j) of design d, counted in copy sp of
+// the design's counters.
+__device__ __forceinline__ void retrace_ray(const LaunchArgs &a, uint32_t d, uint32_t k, uint32_t j, uint32_t sp)
+{
+    const DesignJob &J = a.jobs[d];
+    const float *z = a.z32 + 2 * (J.ray_off + j);
+    uint32_t bin = 0;
+    float t = 0.f;
+    if (trace_df(a.designs[d], a.lx[J.row_off + k], z[0], z[1], bin, t)) {
+        atomicAdd(a.hist + J.hist_off + (uint64_t)k * J.B + bin, (unsigned long long)t_fixed(t));
+        atomicAdd(&a.acc[d].hits[sp], 1ull);
+    }
+    atomicAdd(&a.acc[d].retraced[sp], 1ull);
+}
+
+// PARAM_FC: the single-design trace, whose constants are kernel parameters and whose
+// flagged rays go to the warp's list (wlist, *wcount; the global queue once it is full).
 template <bool PARAM_FC>
 __device__ __forceinline__ void trace_block_rays(const LaunchArgs &a, uint32_t d, const DesignJob &J, uint32_t blk,
-                                                 uint32_t j0, uint32_t j1, uint32_t lane)
+                                                 uint32_t j0, uint32_t j1, uint32_t lane, uint2 *wlist = nullptr,
+                                                 uint32_t *wcount = nullptr)
 {
     const uint32_t k = blk * 32u + lane;
     // the design's constants: kernel parameters (constant-bank operands, no registers)
@@ -251,7 +272,13 @@ __device__ __forceinline__ void trace_block_rays(const LaunchArgs &a, uint32_t d
             sum += t_fixed(t);
             nhit++;
         } else if (r == RAY_FLAG) {
-            push_ray(a, d, k, j);
+            if (PARAM_FC) {
+                const uint32_t pos = atomicAdd(wcount, 1u);
+                if (pos < kWarpFlags) wlist[pos] = make_uint2(k, j);
+                else push_ray(a, d, k, j);
+            } else {
+                push_ray(a, d, k, j);
+            }
         }
     }
     if (sum) atomicAdd(hrow + cur, sum);
@@ -283,11 +310,18 @@ __global__ void __launch_bounds__(256, CPD_TRACE_SPANS_MIN_BLOCKS) trace_spans_k
     // Nothing stays live in registers across a segment's ray loop (which needs every
     // register it can get): the cursor waits in shared memory, and the share's end and the
     // prefix over the spans are found again from the pass's words for each segment.
+    // A warp's flagged rays wait in its list and are re-traced by the warp after its share
+    // (rays past kWarpFlags go to the global queue and the re-trace kernel): the re-trace
+    // of the pass then overlaps the trace instead of following it.
     __shared__ volatile unsigned long long s_cur[8];  // per warp of the block (<= 256 threads)
+    __shared__ uint2 s_flags[8][kWarpFlags];
+    __shared__ uint32_t s_nflags[8];
+    const uint32_t wib = threadIdx.x >> 5;
     {
         const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
         const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-        s_cur[threadIdx.x >> 5] = a.ctl->item_counter * w / nw;  // the next slot of this warp's share
+        s_cur[wib] = a.ctl->item_counter * w / nw;  // the next slot of this warp's share
+        if (lane == 0) s_nflags[wib] = 0u;
     }
     for (;;) {
         __syncwarp();
@@ -325,8 +359,12 @@ __global__ void __launch_bounds__(256, CPD_TRACE_SPANS_MIN_BLOCKS) trace_spans_k
         __syncwarp();
         s_cur[threadIdx.x >> 5] = e0 + stop;
         const DesignJob J = a.jobs[0];
-        trace_block_rays<true>(a, 0u, J, c + (uint32_t)l, r0, bx + stop, lane);
+        trace_block_rays<true>(a, 0u, J, c + (uint32_t)l, r0, bx + stop, lane, s_flags[wib], &s_nflags[wib]);
     }
+    __syncwarp();
+    const uint32_t nf = min(s_nflags[wib], kWarpFlags);
+    const uint32_t sp = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % (uint32_t)kSpread;
+    for (uint32_t i = lane; i < nf; i += 32u) retrace_ray(a, 0u, s_flags[wib][i].x, s_flags[wib][i].y, sp);
 }
 
 __global__ void __launch_bounds__(256, CPD_TRACE_MIN_BLOCKS) trace_kernel(const LaunchArgs a)
@@ -370,15 +408,7 @@ __global__ void __launch_bounds__(32) retrace_kernel(const LaunchArgs a)
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const QEntry e = a.queue[i];
-        const DesignJob &J = a.jobs[e.design];
-        const float *z = a.z32 + 2 * (J.ray_off + e.j);
-        uint32_t bin = 0;
-        float t = 0.f;
-        if (trace_df(a.designs[e.design], a.lx[J.row_off + e.k], z[0], z[1], bin, t)) {
-            atomicAdd(a.hist + J.hist_off + (uint64_t)e.k * J.B + bin, (unsigned long long)t_fixed(t));
-            atomicAdd(&a.acc[e.design].hits[i % kSpread], 1ull);
-        }
-        atomicAdd(&a.acc[e.design].retraced[i % kSpread], 1ull);
+        retrace_ray(a, e.design, e.k, e.j, (uint32_t)(i % kSpread));
     }
 }
 
@@ -1945,8 +1975,11 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         launches++;
     }
     if (ev) cudaEventRecord(ev[2], stream);
-    launch_k(a.mode == CPD_TRACE_FP64 ? retrace_exact_kernel : retrace_kernel, (unsigned)(num_sms * 8), 32, 0, stream,
-             pdl, a);
+    // the single-design trace re-traces its own flagged rays; what reaches the queue there
+    // (the setup's guard bands, a warp's flags past kWarpFlags) is usually little, and a
+    // grid of one block per SM is resident beside the trace, ready when it completes
+    launch_k(a.mode == CPD_TRACE_FP64 ? retrace_exact_kernel : retrace_kernel,
+             (unsigned)(num_sms * (a.spans ? 1 : 8)), 32, 0, stream, pdl, a);
     launches++;
     }
     if (ev) cudaEventRecord(ev[3], stream);
