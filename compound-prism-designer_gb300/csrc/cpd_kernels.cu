@@ -232,12 +232,12 @@ __device__ __forceinline__ void retrace_ray(const LaunchArgs &a, uint32_t d, uin
     atomicAdd(&a.acc[d].retraced[sp], 1ull);
 }
 
-// PARAM_FC: the single-design trace, whose constants are kernel parameters and whose
-// flagged rays go to the warp's list (wlist, *wcount; the global queue once it is full).
+// PARAM_FC: the single-design trace, whose constants are kernel parameters. Flagged rays
+// go to the warp's list (wlist, *wcount: design, row, ray), the global queue once it is full.
 template <bool PARAM_FC>
 __device__ __forceinline__ void trace_block_rays(const LaunchArgs &a, uint32_t d, const DesignJob &J, uint32_t blk,
-                                                 uint32_t j0, uint32_t j1, uint32_t lane, uint2 *wlist = nullptr,
-                                                 uint32_t *wcount = nullptr)
+                                                 uint32_t j0, uint32_t j1, uint32_t lane, uint3 *wlist,
+                                                 uint32_t *wcount)
 {
     const uint32_t k = blk * 32u + lane;
     // the design's constants: kernel parameters (constant-bank operands, no registers)
@@ -272,13 +272,9 @@ __device__ __forceinline__ void trace_block_rays(const LaunchArgs &a, uint32_t d
             sum += t_fixed(t);
             nhit++;
         } else if (r == RAY_FLAG) {
-            if (PARAM_FC) {
-                const uint32_t pos = atomicAdd(wcount, 1u);
-                if (pos < kWarpFlags) wlist[pos] = make_uint2(k, j);
-                else push_ray(a, d, k, j);
-            } else {
-                push_ray(a, d, k, j);
-            }
+            const uint32_t pos = atomicAdd(wcount, 1u);
+            if (pos < kWarpFlags) wlist[pos] = make_uint3(d, k, j);
+            else push_ray(a, d, k, j);
         }
     }
     if (sum) atomicAdd(hrow + cur, sum);
@@ -314,7 +310,7 @@ __global__ void __launch_bounds__(256, CPD_TRACE_SPANS_MIN_BLOCKS) trace_spans_k
     // (rays past kWarpFlags go to the global queue and the re-trace kernel): the re-trace
     // of the pass then overlaps the trace instead of following it.
     __shared__ volatile unsigned long long s_cur[8];  // per warp of the block (<= 256 threads)
-    __shared__ uint2 s_flags[8][kWarpFlags];
+    __shared__ uint3 s_flags[8][kWarpFlags];
     __shared__ uint32_t s_nflags[8];
     const uint32_t wib = threadIdx.x >> 5;
     {
@@ -364,7 +360,7 @@ __global__ void __launch_bounds__(256, CPD_TRACE_SPANS_MIN_BLOCKS) trace_spans_k
     __syncwarp();
     const uint32_t nf = min(s_nflags[wib], kWarpFlags);
     const uint32_t sp = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % (uint32_t)kSpread;
-    for (uint32_t i = lane; i < nf; i += 32u) retrace_ray(a, 0u, s_flags[wib][i].x, s_flags[wib][i].y, sp);
+    for (uint32_t i = lane; i < nf; i += 32u) retrace_ray(a, 0u, s_flags[wib][i].y, s_flags[wib][i].z, sp);
 }
 
 __global__ void __launch_bounds__(256, CPD_TRACE_MIN_BLOCKS) trace_kernel(const LaunchArgs a)
@@ -372,6 +368,13 @@ __global__ void __launch_bounds__(256, CPD_TRACE_MIN_BLOCKS) trace_kernel(const 
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();  // setup's LamParams and queue
     const uint32_t lane = threadIdx.x & 31u;
+    // a warp's flagged rays wait in its list; the warp re-traces them once half of the
+    // list is taken, and at its end (rays past kWarpFlags go to the global queue)
+    __shared__ uint3 s_flags[8][kWarpFlags];
+    __shared__ uint32_t s_nflags[8];
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint32_t sp = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % (uint32_t)kSpread;
+    if (lane == 0) s_nflags[wib] = 0u;
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(&a.ctl->item_counter, 1ull);
@@ -383,8 +386,20 @@ __global__ void __launch_bounds__(256, CPD_TRACE_MIN_BLOCKS) trace_kernel(const 
         const uint32_t blk = (uint32_t)(local / J.nchunk);
         const uint32_t chunk = (uint32_t)(local - (uint64_t)blk * J.nchunk);
         const uint32_t j0 = chunk * a.ray_tile;
-        trace_block_rays<false>(a, d, J, blk, j0, min(j0 + a.ray_tile, J.Rz), lane);
+        trace_block_rays<false>(a, d, J, blk, j0, min(j0 + a.ray_tile, J.Rz), lane, s_flags[wib], &s_nflags[wib]);
+        __syncwarp();
+        const uint32_t nf = s_nflags[wib];
+        if (nf >= kWarpFlags / 2u) {
+            const uint32_t n = min(nf, kWarpFlags);
+            if (lane < n) retrace_ray(a, s_flags[wib][lane].x, s_flags[wib][lane].y, s_flags[wib][lane].z, sp);
+            __syncwarp();
+            if (lane == 0) s_nflags[wib] = 0u;
+            __syncwarp();
+        }
     }
+    __syncwarp();
+    const uint32_t n = min(s_nflags[wib], kWarpFlags);
+    if (lane < n) retrace_ray(a, s_flags[wib][lane].x, s_flags[wib][lane].y, s_flags[wib][lane].z, sp);
 }
 
 // The queued rays, hybrid mode: the float-float re-trace.
