@@ -207,9 +207,6 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
     }
 }
 
-#ifndef CPD_TRACE_MIN_BLOCKS
-#define CPD_TRACE_MIN_BLOCKS 3
-#endif
 
 // The rays [j0, j1) of the 32-row block blk of design d (lane = row), each lane clamped
 // to its row's fast-path range: FP32 fast path, hits as run-length fixed-point sums
@@ -363,7 +360,13 @@ __global__ void __launch_bounds__(256, CPD_TRACE_SPANS_MIN_BLOCKS) trace_spans_k
     for (uint32_t i = lane; i < nf; i += 32u) retrace_ray(a, 0u, s_flags[wib][i].y, s_flags[wib][i].z, sp);
 }
 
-__global__ void __launch_bounds__(256, CPD_TRACE_MIN_BLOCKS) trace_kernel(const LaunchArgs a)
+// 72 registers: 28 resident warps per SM (blocks of 2 or 4 warps) against 24 at 80, for a
+// 24-byte spill; measured on the 1024-design batched pass: 12.82 -> 12.33 ms (64 registers
+// spill 88 bytes: 16.4 ms)
+#ifndef CPD_TRACE_MAXNREG
+#define CPD_TRACE_MAXNREG 72
+#endif
+__global__ void __maxnreg__(CPD_TRACE_MAXNREG) trace_kernel(const LaunchArgs a)
 {
     cudaTriggerProgrammaticLaunchCompletion();
     cudaGridDependencySynchronize();  // setup's LamParams and queue
