@@ -51,17 +51,19 @@ PLAIN_SEED = 20261203 + 1
 OPS_TABLE = os.path.join(ROOT, "roofline", "ops_per_ray.json")
 # FP32 arithmetic of fast_ray on its full path for an anti-reflection-coated design (exit
 # face, refraction, detector, binning and the guard-band thresholds): adds/muls count 1,
-# FMAs 2; the 5 hardware estimates (2 sqrt, 3 reciprocals) and the floor are not counted.
-# Rays lost early execute fewer, so this is an upper bound per evaluated ray.
-FLOP_PER_FAST_RAY = 102
+# FMAs 2, comparisons 0; the 5 hardware estimates (2 sqrt, 3 reciprocals) and the floor
+# are not counted. Rays lost early execute fewer, so this is an upper bound per evaluated
+# ray. (102 before the exit-face terms became polynomials in dz and the exit direction was
+# taken along the detector from dp.)
+FLOP_PER_FAST_RAY = 82
 # Special-function-unit results of fast_ray's full path: 2 square-root and 3 reciprocal
 # estimates.
 SFU_PER_FAST_RAY = 5
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one trace_kernel launch of
-# this workload, from the ncu capture summarised in
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one trace_spans_kernel
+# launch of this workload, from the ncu capture summarised in
 # profiles/fitness_pass_plain_g6_b64_w4096_r1024.md (the figure is copied here when the
 # kernel is re-profiled; bench.py reads no profile file).
-TRACE_TRAFFIC_BYTES = 2726656
+TRACE_TRAFFIC_BYTES = 3045376
 
 
 def dist_info():
@@ -690,9 +692,9 @@ def main():
             extras["roofline"] = {
                 "bound": "fp32", "achieved": alg, "peak": peak, "unit": "TFLOP/s", "frac": alg / peak,
                 "traffic": TRACE_TRAFFIC_BYTES,
-                "traffic_source": "ncu capture of trace_kernel on this workload (dram__bytes_read.sum + "
+                "traffic_source": "ncu capture of trace_spans_kernel on this workload (dram__bytes_read.sum + "
                                   "dram__bytes_write.sum), profiles/fitness_pass_plain_g6_b64_w4096_r1024.md",
-                "kernel": "trace_kernel", "kernel_ms": kt,
+                "kernel": "trace_spans_kernel", "kernel_ms": kt,
                 "frac_algorithmic": alg / peak,
                 "frac_algorithmic_pass": alg_pass / peak,
                 "frac_executed": executed / peak,

@@ -283,8 +283,9 @@ __device__ __forceinline__ void trace_block_rays(const LaunchArgs &a, uint32_t d
 }
 
 // The trace of a single-design pass whose setup wrote the blocks' spans (a.spans). Its
-// design constants are kernel parameters (constant-bank operands), which takes the ray
-// loop from 80 to 71 registers. Measured on the 4096 x 1024 plain pass: at 64 registers
+// design constants are kernel parameters (constant-bank operands), which frees the ~17
+// registers a copy of them takes (75 registers with the re-trace list, no spill). Measured
+// on the 4096 x 1024 plain pass: at 64 registers
 // (4 blocks of 256 per SM, 32 warps, no spill) the trace issues 68% of the slots against
 // 62%, but fills the register file, so the re-trace and entropy blocks can no longer
 // become resident while it runs, and the pass is ~1.5 us slower than at 3 blocks per SM.
