@@ -1103,7 +1103,7 @@ __device__ __forceinline__ bool last_tile_of_design(const LaunchArgs &a, const D
 // lanes split into 32/B row phases of one bin each; for wider detectors a lane owns bins
 // lane, lane+32, ... of every row, NB of them per sweep. Each step reads 8/NB rows x NB
 // bins, so eight loads per lane are in flight.
-template <int NB>
+template <int NB, bool WITH_P>
 __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJob &J, uint32_t r0, uint32_t r1,
                                              uint32_t lane, const float *tab, unsigned long long &hl)
 {
@@ -1150,7 +1150,7 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
                             c1[ii] += cv;
                         }
                 }
-                if (a.p_out && active && rw < r1 && b < B) a.p_out[(uint64_t)rw * B + b] = (double)cv * pscale;
+                if (WITH_P && active && rw < r1 && b < B) a.p_out[(uint64_t)rw * B + b] = (double)cv * pscale;
             }
         }
 #pragma unroll
@@ -1165,6 +1165,9 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
 }
 
 // One warp per tile.
+// WITH_P: the pass also writes p(d|lambda) (a.p_out); a kernel of its own, so that the
+// f64 conversion of every cell is not issued when nobody reads it.
+template <bool WITH_P>
 __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_warp_kernel(const LaunchArgs a)
 {
     __shared__ float tab[4 * ff::kLogTable];
@@ -1184,9 +1187,9 @@ __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_warp_kernel(const 
         const uint32_t r1 = min(r0 + J.tile_rows, J.W);
         const uint32_t nb = (J.B + 31u) / 32u;  // bins per lane
         unsigned long long hl = 0ull;
-        if (nb >= 3u) entropy_tile<4>(a, J, r0, r1, lane, tab, hl);
-        else if (nb == 2u) entropy_tile<2>(a, J, r0, r1, lane, tab, hl);
-        else entropy_tile<1>(a, J, r0, r1, lane, tab, hl);
+        if (nb >= 3u) entropy_tile<4, WITH_P>(a, J, r0, r1, lane, tab, hl);
+        else if (nb == 2u) entropy_tile<2, WITH_P>(a, J, r0, r1, lane, tab, hl);
+        else entropy_tile<1, WITH_P>(a, J, r0, r1, lane, tab, hl);
         hl = warp_sum_u64(hl);
         if (lane == 0 && hl) atomicAdd(&a.acc[d].H, hl);
         if (a.njobs == 1 && last_tile_of_design(a, J, lane)) finalize_design(a, d, J, lane, 32u, tab, nullptr);
@@ -1201,6 +1204,7 @@ __global__ void __launch_bounds__(kEntropyThreads, 2) entropy_warp_kernel(const 
 // every sum is independent of the grouping of cells into threads, tiles and launches,
 // and each nonzero cell is zeroed after it is read, which leaves the histogram clear for
 // the next pass.
+template <bool WITH_P>
 __global__ void __launch_bounds__(kEntropyThreads, 4) entropy_block_kernel(const LaunchArgs a)
 {
     __shared__ float tab[4 * ff::kLogTable];
@@ -1245,7 +1249,7 @@ __global__ void __launch_bounds__(kEntropyThreads, 4) entropy_block_kernel(const
                 idx[k] = (uint64_t)row * B + b;
                 bc[k] = b;
                 cv[k] = in ? base[idx[k]] : 0ull;
-                if (in && a.p_out) a.p_out[idx[k]] = (double)cv[k] * pscale;
+                if (WITH_P && in) a.p_out[idx[k]] = (double)cv[k] * pscale;
                 b += db;
                 row += dr;
                 if (b >= B) {
@@ -2008,19 +2012,21 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
             // few tiles: one block per tile
             const size_t smem = 2u * sizeof(unsigned long long) * (a.max_B ? a.max_B : (uint32_t)CPD_MAX_BINS);
             int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, entropy_block_kernel, kEntropyThreads, smem);
+            auto k = a.p_out ? entropy_block_kernel<true> : entropy_block_kernel<false>;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kEntropyThreads, smem);
             if (per_sm < 1) per_sm = 1;
             uint64_t grid = a.total_tiles;
             if (grid > (uint64_t)num_sms * per_sm) grid = (uint64_t)num_sms * per_sm;
-            launch_k(entropy_block_kernel, (unsigned)grid, kEntropyThreads, smem, stream, pdl, a);
+            launch_k(k, (unsigned)grid, kEntropyThreads, smem, stream, pdl, a);
         } else {
             // one warp per tile, as many blocks as are resident at once
             int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, entropy_warp_kernel, kEntropyThreads, 0);
+            auto k = a.p_out ? entropy_warp_kernel<true> : entropy_warp_kernel<false>;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kEntropyThreads, 0);
             if (per_sm < 1) per_sm = 1;
             uint64_t grid = (a.total_tiles + wpb - 1) / wpb;
             if (grid > (uint64_t)num_sms * per_sm) grid = (uint64_t)num_sms * per_sm;
-            launch_k(entropy_warp_kernel, (unsigned)grid, kEntropyThreads, 0, stream, pdl, a);
+            launch_k(k, (unsigned)grid, kEntropyThreads, 0, stream, pdl, a);
         }
         launches++;
     }
