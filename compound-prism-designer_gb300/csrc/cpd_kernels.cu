@@ -1664,8 +1664,11 @@ __device__ __noinline__ void loop_trace(const DevDesign &D, const LamParams *lp,
     const uint32_t nblk = (W + 31u) / 32u;
     const uint32_t nchunk = Rz ? (Rz + ray_tile - 1u) / ray_tile : 1u;
     const uint32_t total = nblk * nchunk;
-    const FastConst &C = D.fc;
+    // the design's constants in registers (read from shared memory at every use, they cost
+    // more than the registers: loop alone 171 -> 172 k designs/s)
+    const FastConst C = D.fc;
     const Guards guards = default_guards();
+    const FastLimits Lm = fast_limits(C, guards);
     for (;;) {
         uint32_t item = 0;
         if (lane == 0) item = atomicAdd(&tally->item, 1u);
@@ -1691,7 +1694,7 @@ __device__ __noinline__ void loop_trace(const DevDesign &D, const LamParams *lp,
             const float2 z = __ldg(zt + j);
             uint32_t bin = 0;
             float tt = 0.f;
-            const int r = fast_ray(C, P, guards, z.x, z.y, bin, tt);
+            const int r = fast_ray(C, Lm, P, guards, z.x, z.y, bin, tt);
             if (r == RAY_HIT) {
                 if (bin != cur) {
                     if (sum) atomicAdd(hrow + cur, sum);
