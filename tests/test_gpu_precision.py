@@ -57,6 +57,29 @@ def test_fp64_trace_equals_oracle_on_near_critical_designs(population):
         assert f.hits == st["hits"]
 
 
+def test_single_design_trace_with_overflowing_flag_lists():
+    """The largest single-design pass whose trace takes equal shares of the ray slots
+    (16384 wavelengths x 8192 rays): each warp's share holds ~37 k rays, and at this
+    design's flag rate (1.3e-3 of the core rays in the host check) many warps flag more rays
+    than their 32-entry lists hold, so the rest go through the global queue and its kernel.
+    The result must equal the multi-design trace's (work items, every flagged ray queued)
+    bit for bit, and the oracle on the same points within the parity bounds."""
+    spec = P.study_population(314, n=8, B=128)[7][0]
+    W, R, seed = 16384, 8192, 0.3
+    single = spec.gpu_fitness_full([seed], max_n=W, max_eval=R)
+    for o in cpd.fitness_batch([spec, spec], seeds=seed, max_n=W, max_eval=R):
+        assert o.info == single.info and o.hits == single.hits and o.retraced == single.retraced
+    assert single.retraced > 0
+    lam_u, ray_u = O.gpu_points(seed, W), O.gpu_points(seed, R, first=1)
+    f, p = spec.gpu_fitness_points(lam_u, ray_u, want_p=True)
+    assert f.info == single.info and f.hits == single.hits
+    po, st = O.fitness_points(synth.spec_dict(spec), lam_u, ray_u, nthreads=NTHREADS)
+    assert np.abs(p - po).max() <= 1e-6
+    assert abs(f.info - st["info"]) <= 1e-4 * abs(st["info"]) + 1e-9
+    assert f.hits == st["hits"]
+    print(f"retraced {f.retraced} of {f.rays} rays, MI rel err {abs(f.info - st['info']) / abs(st['info']):.2e}")
+
+
 def test_summary_counts_classes(population):
     rows = []
     lam_u = P.synth_points(0.5, 64)
