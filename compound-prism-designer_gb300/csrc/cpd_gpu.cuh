@@ -40,6 +40,9 @@ struct alignas(16) QEntry {
     uint32_t design, k, j, pad;
 };
 
+// Sorted-ray tables up to this many rays can be staged in shared memory by the setup.
+constexpr uint32_t kStageRays = 2048;
+
 // Per-launch control words (zeroed before every pass).
 struct Control {
     unsigned long long item_counter;
@@ -117,6 +120,11 @@ struct LaunchArgs {
     // the ray loop.
     FastConst fc;
     FastLimits fl;
+    // The setup stages a design's sorted z table in shared memory when it has at most
+    // stage_cap rays (at most kStageRays; 0: none); the setup's blocks get
+    // 8 * even(stage_cap) bytes, so a pass whose tables are small or not staged at all does
+    // not hold shared memory it does not use.
+    uint32_t stage_cap;
     uint32_t mode;        // CPD_TRACE_*
     uint32_t adaptive;    // per-wavelength SEM stop: 1, or 2 with every row on the exact path
     uint32_t max_B;       // widest detector of the launch

@@ -96,8 +96,6 @@ __global__ void __launch_bounds__(32) build_records_kernel(const cpd_spectromete
     out[i] = d;
 }
 
-// Sorted-ray tables up to this many rays are staged in shared memory by the setup.
-constexpr uint32_t kStageRays = 2048;
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
@@ -143,7 +141,7 @@ __device__ __forceinline__ uint2 setup_row(const LaunchArgs &a, uint64_t row, ui
 }
 
 // One warp per block of 32 rows. The block first copies its design record and, for
-// tables of up to kStageRays rays, its sorted z table into shared memory with
+// tables of up to a.stage_cap rays, its sorted z table into shared memory with
 // asynchronous 16-byte copies that are all in flight at once (one memory latency
 // instead of a chain of dependent loads), so the per-wavelength program and its binary
 // searches run on shared-memory operands. Ray tables start 16-byte aligned (the host
@@ -164,12 +162,12 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
         for (uint64_t i = gt; i < words; i += nt) acc[i] = 0ull;
     }
     __shared__ __align__(16) DevDesign sD;
-    extern __shared__ __align__(16) float sz[];  // 2 kStageRays floats
+    extern __shared__ __align__(16) float sz[];  // 2 even(stage_cap) floats
     const uint64_t row0 = blockIdx.x * (uint64_t)blockDim.x;
     const uint64_t row = row0 + threadIdx.x;
     const uint32_t d0 = find_job<F_ROW>(a.jobs, a.njobs, row0);
     const DesignJob &J0 = a.jobs[d0];
-    const bool stage_z = J0.Rz <= kStageRays;
+    const bool stage_z = J0.Rz <= a.stage_cap;
     // the row's design and wavelength point, loaded while the copies below are in flight
     // (the point is not in L2 when the previous pass's tables were evicted)
     uint32_t d = 0;
@@ -1964,7 +1962,8 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         // one warp per block: each row is one thread's latency-bound float-float chain,
         // so spreading the rows over every SM matters
         const uint32_t blocks = (uint32_t)((a.total_rows + 31) / 32);
-        launch_k(setup_kernel, blocks, 32, 2 * kStageRays * sizeof(float), stream, false, a);
+        const uint32_t cap = a.stage_cap < kStageRays ? a.stage_cap : kStageRays;
+        launch_k(setup_kernel, blocks, 32, 2 * ((cap + 1u) & ~1u) * sizeof(float), stream, false, a);
         launches++;
     }
     if (a.adaptive) {

@@ -483,6 +483,8 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     a.queue = S.queue.as<QEntry>();
     a.qcap = S.qcap;
     a.ray_tile = ctx->ray_tile;
+    for (uint32_t i = 0; i < n; i++)
+        if (jobs[i].Rz <= kStageRays && jobs[i].Rz > a.stage_cap) a.stage_cap = jobs[i].Rz;
     a.mode = mode;
     if (mode == CPD_TRACE_FP32) {
         a.guards = no_guards();

@@ -175,6 +175,7 @@ extern "C" int cpd_fitness_gpu_points_static(const cpd_design *d, const double *
     a.queue = reinterpret_cast<QEntry *>(b + kOffQueue);
     a.qcap = kStaticQueue;
     a.ray_tile = ray_tile;
+    a.stage_cap = Rz <= kStageRays ? Rz : 0u;
     a.mode = trace_mode;
     a.max_B = J.B;
     if (trace_mode == CPD_TRACE_FP32) {
