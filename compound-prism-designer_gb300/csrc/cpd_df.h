@@ -207,130 +207,152 @@ CPD_HDN inline bool reference_ray_df(const DevDesign &D, const float *z32, LamPa
     return false;
 }
 
-// Per-wavelength setup in float-float. u is the wavelength's u-point (lambda = wmin +
-// (wmax - wmin) u); z32 the sorted ray table as (hi, lo) float pairs, R entries. Fills P
-// (fast-path constants and the band / core ranges of sorted rays) and, if given, E.
-// Returns false if no ray of this wavelength clears the flat faces. The face loop is
-// kept rolled: one warp runs this program once per wavelength, so instruction fetch,
-// not scheduling freedom, is what a longer unrolled body would cost.
-// With df_fresnel the Fresnel factors of the flat faces are formed in float-float too,
-// so that E's transmittances match the f64 trace to ~2^-44 (the adaptive mode's exact
-// path needs them); otherwise each factor is an FP32 value (~1e-7).
-CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z32, uint32_t R, LamParams &P,
-                                    double yguard_rel = kYGuardRel, LamDF *E = nullptr, bool df_fresnel = false)
+// The state a wavelength's setup carries through the flat faces. Direction part: the
+// direction d entering the next face, the index n1 of the glass it leaves, the s/p
+// transmittance products. Position part: the affine point a + b y on the last face, and
+// the tightest bounds y >= -L0/L1 (L1 > 0) and y <= U0/U1 (U1 > 0), compared by
+// cross-multiplication so that only the two winners are divided.
+struct SetupDir {
+    ff::F2 dx, dy, n1, ts, tp;
+};
+struct SetupPos {
+    ff::F2 ax, ay, bx, by, L0, L1, U0, U1;
+    float Lg, Ug;
+    bool lost;  // a bound independent of y excludes every ray
+};
+CPD_HD SetupDir setup_dir_init()
 {
-    const int G = D.G;
+    return SetupDir{df::c(1.f), df::c(0.f), df::c(1.f), df::c(1.f), df::c(1.f)};
+}
+CPD_HD SetupPos setup_pos_init()
+{
+    using df::c;
+    return SetupPos{c(0.f), c(0.f), c(0.f), c(1.f), c(0.f), c(0.f), c(0.f), c(0.f), 0.f, 0.f, false};
+}
+// The wavelength of u-point u.
+CPD_HDN inline ff::F2 setup_lambda(const DevDesign &D, double u)
+{
+    return df::add(D.dc.wmin, df::mul(D.dc.wspan, df::from_d(u)));
+}
+// The cosine d.N at flat face k (the same value for both parts of the face).
+CPD_HDN inline ff::F2 face_cos(const DevDesign &D, int k, ff::F2 dx, ff::F2 dy)
+{
+    return df::dot(dx, dy, D.dc.pnx[k], D.dc.pny[k]);
+}
+
+// The position part of flat face k (ci = its cosine, nonzero; dx, dy = the direction that
+// enters it): the distance to the face e0 + e1 y, the three bounds it puts on y, and the
+// point on the face.
+CPD_HDN inline void face_position(const DevDesign &D, int k, ff::F2 ci, ff::F2 dx, ff::F2 dy, SetupPos &S,
+                                  float yg)
+{
     using namespace df;
     const DFConst &C = D.dc;
-    {
-        uint32_t *w = reinterpret_cast<uint32_t *>(&P);
-        for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
-    }
-    const F2 lambda = add(C.wmin, mul(C.wspan, from_d(u)));
-    F2 dx = c(1.f), dy = c(0.f), ax = c(0.f), ay = c(0.f), bx = c(0.f), by = c(1.f), n1 = c(1.f);
-    // s/p transmittance products in float-float: the AR factor 0.99 is not a float, and
-    // six float roundings would bias every ray of the wavelength by ~6e-8
-    F2 ts = c(1.f), tp = c(1.f);
-    const F2 ar99{0.99f, -9.5367431640625e-09f};  // 0.99 = hi + lo to ~1e-17
-    // tightest bounds y >= -L0/L1 (L1 > 0) and y <= U0/U1 (U1 > 0), compared by
-    // cross-multiplication so that only the two winners are divided
-    F2 L0 = c(0.f), L1 = c(0.f), U0 = c(0.f), U1 = c(0.f);
-    float Lg = 0.f, Ug = 0.f;
-    bool lost = false;
-    const float yg = (float)yguard_rel;
     auto constrain = [&](F2 c0, F2 c1, float scale) {
         // c0 + c1 y >= 0
         const float g = yg * (scale + 1.f);
         if (c1.hi == 0.f) {
-            if (neg_(c0)) lost = true;  // independent of y: decided here for every ray
+            if (neg_(c0)) S.lost = true;  // independent of y: decided here for every ray
         } else if (c1.hi > 0.f) {
-            if (L1.hi == 0.f || lt(mul(c0, L1), mul(L0, c1))) {
-                L0 = c0;
-                L1 = c1;
-                Lg = g;
+            if (S.L1.hi == 0.f || lt(mul(c0, S.L1), mul(S.L0, c1))) {
+                S.L0 = c0;
+                S.L1 = c1;
+                S.Lg = g;
             }
         } else {
             const F2 u1 = neg(c1);
-            if (U1.hi == 0.f || lt(mul(c0, U1), mul(U0, u1))) {
-                U0 = c0;
-                U1 = u1;
-                Ug = g;
+            if (S.U1.hi == 0.f || lt(mul(c0, S.U1), mul(S.U0, u1))) {
+                S.U0 = c0;
+                S.U1 = u1;
+                S.Ug = g;
             }
         }
     };
-#pragma unroll 1
-    for (int k = 0; k < G; k++) {
-        if (lost) break;
-        F2 n2 = C.glass[k][0];  // Glass::calc_n (Horner, glasscat.rs:17-22)
+    const F2 nx = C.pnx[k], ny = C.pny[k];
+    // dist(y) = ((P - o(y)).N)/ci = e0 + e1 y; hit y = hy0 + hy1 y
+    const F2 inv = rcp(ci);
+    const F2 e0 = mul(dot(sub(C.ppx[k], S.ax), sub(C.ppy[k], S.ay), nx, ny), inv);
+    const F2 e1 = neg(mul(dot(S.bx, S.by, nx, ny), inv));
+    const float sc = fabsf(e0.hi) + 30.f * fabsf(e1.hi) + C.height.hi;
+    constrain(e0, e1, sc);
+    const F2 hy0 = add(S.ay, mul(dy, e0)), hy1 = add(S.by, mul(dy, e1));
+    constrain(hy0, hy1, sc);
+    constrain(sub(C.height, hy0), neg(hy1), sc);
+    S.ax = add(S.ax, mul(dx, e0));
+    S.ay = hy0;
+    S.bx = add(S.bx, mul(dx, e1));
+    S.by = hy1;
+}
+
+// The direction part of flat face k: Ray::refract (ray.rs:309-367), the same for every ray
+// of the wavelength, and the face's Fresnel factors. Returns false on total internal
+// reflection (the state is then left as it was).
+CPD_HDN inline bool face_direction(const DevDesign &D, int k, ff::F2 lambda, ff::F2 ci, SetupDir &S,
+                                   bool df_fresnel)
+{
+    using namespace df;
+    const DFConst &C = D.dc;
+    const F2 ar99{0.99f, -9.5367431640625e-09f};  // 0.99 = hi + lo to ~1e-17
+    F2 n2 = C.glass[k][0];  // Glass::calc_n (Horner, glasscat.rs:17-22)
 #pragma unroll
-        for (int i = 1; i < 6; i++) n2 = add(mul(n2, lambda), C.glass[k][i]);
-        const F2 nx = C.pnx[k], ny = C.pny[k];
-        const F2 ci = dot(dx, dy, nx, ny);
-        if (ci.hi == 0.f) {  // parallel to the face: no ray meets it
-            lost = true;
-            break;
-        }
-        // dist(y) = ((P - o(y)).N)/ci = e0 + e1 y; hit y = hy0 + hy1 y
-        const F2 inv = rcp(ci);
-        const F2 e0 = mul(dot(sub(C.ppx[k], ax), sub(C.ppy[k], ay), nx, ny), inv);
-        const F2 e1 = neg(mul(dot(bx, by, nx, ny), inv));
-        const float sc = fabsf(e0.hi) + 30.f * fabsf(e1.hi) + C.height.hi;
-        constrain(e0, e1, sc);
-        const F2 hy0 = add(ay, mul(dy, e0)), hy1 = add(by, mul(dy, e1));
-        constrain(hy0, hy1, sc);
-        constrain(sub(C.height, hy0), neg(hy1), sc);
-        ax = add(ax, mul(dx, e0));
-        ay = hy0;
-        bx = add(bx, mul(dx, e1));
-        by = hy1;
-        // Ray::refract (ray.rs:309-367): the same for every ray of the wavelength
-        const F2 ci_r = neg(ci);
-        const F2 rr = div(n1, n2);
-        const F2 cr_sq = sub(c(1.f), mul(sqr(rr), sub(c(1.f), sqr(ci_r))));
-        if (neg_(cr_sq)) {  // total internal reflection
-            lost = true;
-            break;
-        }
-        const F2 cr = sqrt(cr_sq);
-        const F2 kq = sub(mul(rr, ci_r), cr);
-        const F2 vx = add(mul(dx, rr), mul(nx, kq)), vy = add(mul(dy, rr), mul(ny, kq));
-        if (D.ar && lt(c(0.5f), ci_r)) {
-            ts = mul(ts, ar99);
-            tp = mul(tp, ar99);
-        } else if (df_fresnel) {
-            const F2 a = add(mul(n1, ci_r), mul(n2, cr)), b = add(mul(n1, cr), mul(n2, ci_r));
-            const F2 k4 = mulf(mul(mul(n1, n2), mul(ci_r, cr)), 4.f);
-            ts = mul(ts, div(k4, sqr(a)));
-            tp = mul(tp, div(k4, sqr(b)));
-        } else {
-            // 1 - R without cancellation: 4 n1 n2 ci cr / (n1 ci + n2 cr)^2 (s), ci <-> cr (p)
-            const float f1 = n1.hi, f2 = n2.hi, fc = ci_r.hi, fr = cr.hi;
-            const float a = f1 * fc + f2 * fr, b = f1 * fr + f2 * fc;
-            const float k4 = 4.f * f1 * f2 * fc * fr;
-            ts = mulf(ts, k4 / (a * a));
-            tp = mulf(tp, k4 / (b * b));
-        }
-        dx = vx;
-        dy = vy;
-        n1 = n2;
+    for (int i = 1; i < 6; i++) n2 = add(mul(n2, lambda), C.glass[k][i]);
+    const F2 nx = C.pnx[k], ny = C.pny[k];
+    const F2 ci_r = neg(ci);
+    const F2 n1 = S.n1;
+    const F2 rr = div(n1, n2);
+    const F2 cr_sq = sub(c(1.f), mul(sqr(rr), sub(c(1.f), sqr(ci_r))));
+    if (neg_(cr_sq)) return false;  // total internal reflection
+    const F2 cr = sqrt(cr_sq);
+    const F2 kq = sub(mul(rr, ci_r), cr);
+    const F2 vx = add(mul(S.dx, rr), mul(nx, kq)), vy = add(mul(S.dy, rr), mul(ny, kq));
+    // s/p transmittance products in float-float: the AR factor 0.99 is not a float, and
+    // six float roundings would bias every ray of the wavelength by ~6e-8
+    if (D.ar && lt(c(0.5f), ci_r)) {
+        S.ts = mul(S.ts, ar99);
+        S.tp = mul(S.tp, ar99);
+    } else if (df_fresnel) {
+        const F2 a = add(mul(n1, ci_r), mul(n2, cr)), b = add(mul(n1, cr), mul(n2, ci_r));
+        const F2 k4 = mulf(mul(mul(n1, n2), mul(ci_r, cr)), 4.f);
+        S.ts = mul(S.ts, div(k4, sqr(a)));
+        S.tp = mul(S.tp, div(k4, sqr(b)));
+    } else {
+        // 1 - R without cancellation: 4 n1 n2 ci cr / (n1 ci + n2 cr)^2 (s), ci <-> cr (p)
+        const float f1 = n1.hi, f2 = n2.hi, fc = ci_r.hi, fr = cr.hi;
+        const float a = f1 * fc + f2 * fr, b = f1 * fr + f2 * fc;
+        const float k4 = 4.f * f1 * f2 * fc * fr;
+        S.ts = mulf(S.ts, k4 / (a * a));
+        S.tp = mulf(S.tp, k4 / (b * b));
     }
+    S.dx = vx;
+    S.dy = vy;
+    S.n1 = n2;
+    return true;
+}
+
+// After the flat faces: the y interval, E, the sorted-ray ranges and the reference ray.
+CPD_HDN inline bool setup_tail(const DevDesign &D, const float *z32, uint32_t R, LamParams &P, LamDF *E,
+                               const SetupDir &Sd, const SetupPos &Sp, bool lost)
+{
+    using namespace df;
+    const DFConst &C = D.dc;
+    const F2 L0 = Sp.L0, L1 = Sp.L1, U0 = Sp.U0, U1 = Sp.U1;
     const F2 ylo = L1.hi > 0.f ? neg(div(L0, L1)) : c(-kBig), yhi = U1.hi > 0.f ? div(U0, U1) : c(kBig);
-    const float glo = L1.hi > 0.f ? Lg / L1.hi : 0.f, ghi = U1.hi > 0.f ? Ug / U1.hi : 0.f;
+    const float glo = L1.hi > 0.f ? Sp.Lg / L1.hi : 0.f, ghi = U1.hi > 0.f ? Sp.Ug / U1.hi : 0.f;
     if (E) {
         E->ylo = ylo;
         E->yhi = yhi;
-        E->ax = ax;
-        E->ay = ay;
-        E->bx = bx;
-        E->by = by;
-        E->dx = dx;
-        E->dy = dy;
-        E->n = n1;
-        E->ts = ts.hi;
-        E->tp = tp.hi;
+        E->ax = Sp.ax;
+        E->ay = Sp.ay;
+        E->bx = Sp.bx;
+        E->by = Sp.by;
+        E->dx = Sd.dx;
+        E->dy = Sd.dy;
+        E->n = Sd.n1;
+        E->ts = Sd.ts.hi;
+        E->tp = Sd.tp.hi;
         E->lost = lost ? 1u : 0u;
-        E->ts_lo = ts.lo;
-        E->tp_lo = tp.lo;
+        E->ts_lo = Sd.ts.lo;
+        E->tp_lo = Sd.tp.lo;
         E->pad = 0u;
     }
     if (lost) return false;
@@ -393,14 +415,57 @@ CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z
     if (P.core_hi < P.core_lo) P.core_hi = P.core_lo;
     if (P.band_hi < P.core_hi) P.band_hi = P.core_hi;
     if (P.band_lo > P.core_lo) P.band_lo = P.core_lo;
-    P.dx = dx.hi;
-    P.dy = dy.hi;
-    P.ts = ts.hi;
-    P.tp = tp.hi;
-    if (P.core_hi > P.core_lo && !reference_ray_df(D, z32, P, ax, ay, bx, by, dx, dy, n1)) P.all_exact = 1;
+    P.dx = Sd.dx.hi;
+    P.dy = Sd.dy.hi;
+    P.ts = Sd.ts.hi;
+    P.tp = Sd.tp.hi;
+    if (P.core_hi > P.core_lo &&
+        !reference_ray_df(D, z32, P, Sp.ax, Sp.ay, Sp.bx, Sp.by, Sd.dx, Sd.dy, Sd.n1))
+        P.all_exact = 1;
     return P.band_hi > P.band_lo;
 }
 
+CPD_HD void zero_lam_params(LamParams &P)
+{
+    uint32_t *w = reinterpret_cast<uint32_t *>(&P);
+    for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
+}
+
+// Per-wavelength setup in float-float. u is the wavelength's u-point (lambda = wmin +
+// (wmax - wmin) u); z32 the sorted ray table as (hi, lo) float pairs, R entries. Fills P
+// (fast-path constants and the band / core ranges of sorted rays) and, if given, E.
+// Returns false if no ray of this wavelength clears the flat faces. The face loop is
+// kept rolled: one warp runs this program once per wavelength, so instruction fetch,
+// not scheduling freedom, is what a longer unrolled body would cost.
+// With df_fresnel the Fresnel factors of the flat faces are formed in float-float too,
+// so that E's transmittances match the f64 trace to ~2^-44 (the adaptive mode's exact
+// path needs them); otherwise each factor is an FP32 value (~1e-7).
+CPD_HDN inline bool lambda_setup_df(const DevDesign &D, double u, const float *z32, uint32_t R, LamParams &P,
+                                    double yguard_rel = kYGuardRel, LamDF *E = nullptr, bool df_fresnel = false)
+{
+    const int G = D.G;
+    zero_lam_params(P);
+    const ff::F2 lambda = setup_lambda(D, u);
+    SetupDir Sd = setup_dir_init();
+    SetupPos Sp = setup_pos_init();
+    const float yg = (float)yguard_rel;
+    bool lost = false;
+#pragma unroll 1
+    for (int k = 0; k < G; k++) {
+        if (Sp.lost) break;
+        const ff::F2 ci = face_cos(D, k, Sd.dx, Sd.dy);
+        if (ci.hi == 0.f) {  // parallel to the face: no ray meets it
+            lost = true;
+            break;
+        }
+        face_position(D, k, ci, Sd.dx, Sd.dy, Sp, yg);
+        if (!face_direction(D, k, lambda, ci, Sd, df_fresnel)) {
+            lost = true;
+            break;
+        }
+    }
+    return setup_tail(D, z32, R, P, E, Sd, Sp, lost || Sp.lost);
+}
 
 // The float-float re-trace of one ray (start height from z = zh + zl): the flat faces
 // through the wavelength's y interval and affine position, then the curved exit face

@@ -105,26 +105,22 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 
 // The setup of one wavelength row (below): LamParams and LamDF, and the row's guard-band
 // rays queued. Returns the row's fast-path range [core_lo, core_hi) (empty: hi <= lo).
-__device__ __forceinline__ uint2 setup_row(const LaunchArgs &a, uint64_t row, uint32_t d, double u,
-                                           const DevDesign &sD, uint32_t d0, bool stage_z, const float *sz)
+// A row whose design failed its device build: every ray of it is lost.
+__device__ __forceinline__ uint2 setup_failed_row(const LaunchArgs &a, uint64_t row)
 {
-    const DesignJob &J = a.jobs[d];
-    const uint32_t k = (uint32_t)(row - J.row_off);
-    const bool staged = d == d0;
-    const DevDesign &D = staged ? sD : a.designs[d];
-    const float *z32 = staged && stage_z ? sz : a.z32 + 2 * J.ray_off;
     LamParams P;
-    if (D.status) {
-        // a design whose device build failed: every ray of it is lost
-        uint32_t *w = reinterpret_cast<uint32_t *>(&P);
-        for (unsigned i = 0; i < sizeof(LamParams) / 4; i++) w[i] = 0u;
-        LamDF *E = a.lx + row;
-        memset(E, 0, sizeof(LamDF));
-        E->lost = 1u;
-        a.lp[row] = P;
-        return make_uint2(0u, 0u);
-    }
-    lambda_setup_df(D, u, z32, J.Rz, P, a.yguard_rel, a.lx + row, a.adaptive != 0);
+    zero_lam_params(P);
+    LamDF *E = a.lx + row;
+    memset(E, 0, sizeof(LamDF));
+    E->lost = 1u;
+    a.lp[row] = P;
+    return make_uint2(0u, 0u);
+}
+
+// A row's LamParams after lambda_setup_df: its guard-band rays queued as the mode asks, the
+// record written. Returns the row's fast-path range [core_lo, core_hi) (empty: hi <= lo).
+__device__ __forceinline__ uint2 setup_finish(const LaunchArgs &a, uint32_t d, uint32_t k, uint64_t row, LamParams &P)
+{
     if (a.adaptive) {
         // the adaptive rounds trace every ray of the band themselves
     } else if (a.mode == CPD_TRACE_FP64 || (P.all_exact && a.mode == CPD_TRACE_HYBRID)) {
@@ -138,6 +134,22 @@ __device__ __forceinline__ uint2 setup_row(const LaunchArgs &a, uint64_t row, ui
     }
     a.lp[row] = P;
     return make_uint2(P.core_lo, P.core_hi);
+}
+
+// The setup of one wavelength row (below): LamParams and LamDF, and the row's guard-band
+// rays queued. Returns the row's fast-path range [core_lo, core_hi) (empty: hi <= lo).
+__device__ __forceinline__ uint2 setup_row(const LaunchArgs &a, uint64_t row, uint32_t d, double u,
+                                           const DevDesign &sD, uint32_t d0, bool stage_z, const float *sz)
+{
+    const DesignJob &J = a.jobs[d];
+    const uint32_t k = (uint32_t)(row - J.row_off);
+    const bool staged = d == d0;
+    const DevDesign &D = staged ? sD : a.designs[d];
+    const float *z32 = staged && stage_z ? sz : a.z32 + 2 * J.ray_off;
+    if (D.status) return setup_failed_row(a, row);
+    LamParams P;
+    lambda_setup_df(D, u, z32, J.Rz, P, a.yguard_rel, a.lx + row, a.adaptive != 0);
+    return setup_finish(a, d, k, row, P);
 }
 
 // One warp per block of 32 rows. The block first copies its design record and, for
@@ -209,6 +221,121 @@ __global__ void __launch_bounds__(32) setup_kernel(const LaunchArgs a)
 // The rays [j0, j1) of the 32-row block blk of design d (lane = row), each lane clamped
 // to its row's fast-path range: FP32 fast path, hits as run-length fixed-point sums
 // flushed with one 64-bit atomic per run, guard-band rays queued for the re-trace.
+// The setup of a single-design pass (a.spans set) by two warps per block of 32 rows. Each
+// row's flat-face chain splits into two halves that depend on each other only through the
+// direction entering each face: warp 0 runs the direction part of every face (the glass
+// index, the refraction, the Fresnel factors), warp 1 the position part (the distance to
+// the face, the bounds it puts on y, the point on it), face by face in step: at face k warp
+// 1 reads the direction d_k that warp 0 published at face k - 1, one block barrier per face.
+// Each warp stops where lambda_setup_df's loop would stop (a face parallel to the ray, which
+// both see from the same cosine; total internal reflection, which warp 0 reports; a bound
+// independent of y, which warp 1 reports), and warp 0 then finishes the row alone (y
+// interval, ray ranges, reference ray). The functions are lambda_setup_df's own, so every
+// output is bit-identical to the one-warp setup; the chain that is one warp per SM in the
+// plain call is about half as long.
+__global__ void __launch_bounds__(64) setup_pair_kernel(const LaunchArgs a)
+{
+    cudaTriggerProgrammaticLaunchCompletion();
+    if (a.clear_acc) {
+        const uint64_t gt = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+        const uint64_t nt = (uint64_t)gridDim.x * blockDim.x;
+        for (uint64_t i = gt; i < a.acc_cells; i += nt) a.S1[i] = a.S2[i] = 0ull;
+        unsigned long long *acc = reinterpret_cast<unsigned long long *>(a.acc);
+        const uint64_t words = (uint64_t)a.njobs * (sizeof(DesignAcc) / sizeof(unsigned long long));
+        for (uint64_t i = gt; i < words; i += nt) acc[i] = 0ull;
+    }
+    __shared__ __align__(16) DevDesign sD;
+    extern __shared__ __align__(16) float sz[];  // 2 even(stage_cap) floats
+    __shared__ ff::F2 s_dir[CPD_MAX_GLASS + 1][2][32];  // direction entering face k (x, y)
+    __shared__ uint32_t s_tir[32], s_bound[32];          // stops reported at the last face
+    __shared__ SetupPos s_pos[32];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint64_t row = blockIdx.x * 32ull + lane;
+    const DesignJob &J = a.jobs[0];
+    const bool have = row < a.total_rows;
+    const bool stage_z = J.Rz <= a.stage_cap;
+    const double u = have && warp == 0 ? a.lam_u[J.lam_off + row] : 0.0;
+    {
+        const char *src = reinterpret_cast<const char *>(a.designs);
+        char *dst = reinterpret_cast<char *>(&sD);
+        for (uint32_t i = threadIdx.x; i < sizeof(DevDesign) / 16; i += blockDim.x) cp_async16(dst + 16 * i, src + 16 * i);
+        if (stage_z) {
+            const char *zs = reinterpret_cast<const char *>(a.z32 + 2 * J.ray_off);
+            char *zd = reinterpret_cast<char *>(sz);
+            const uint32_t n16 = (J.Rz + 1u) / 2u;  // 16-byte chunks (two rays each)
+            for (uint32_t i = threadIdx.x; i < n16; i += blockDim.x) cp_async16(zd + 16 * i, zs + 16 * i);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    }
+    __syncthreads();
+    const DevDesign &D = sD;
+    const int G = D.G;
+    const float yg = (float)a.yguard_rel;
+    SetupDir Sd = setup_dir_init();
+    SetupPos Sp = setup_pos_init();
+    const ff::F2 lambda = warp == 0 ? setup_lambda(D, u) : ff::F2{0.f, 0.f};
+    bool stop = !have || D.status != 0;
+    bool lost = false;  // warp 0: a face parallel to the ray, or total internal reflection
+#pragma unroll 1
+    for (int k = 0; k < G; k++) {
+        bool tir = false;
+        if (!stop) {
+            if (warp == 0) {
+                const ff::F2 ci = face_cos(D, k, Sd.dx, Sd.dy);
+                if (ci.hi == 0.f) {
+                    lost = stop = true;
+                } else if (!face_direction(D, k, lambda, ci, Sd, false)) {
+                    lost = stop = tir = true;
+                } else {
+                    s_dir[k + 1][0][lane] = Sd.dx;
+                    s_dir[k + 1][1][lane] = Sd.dy;
+                }
+            } else {
+                const ff::F2 dx = k == 0 ? df::c(1.f) : s_dir[k][0][lane];
+                const ff::F2 dy = k == 0 ? df::c(0.f) : s_dir[k][1][lane];
+                const ff::F2 ci = face_cos(D, k, dx, dy);
+                if (ci.hi == 0.f) stop = true;  // warp 0 sees the same cosine
+                else face_position(D, k, ci, dx, dy, Sp, yg);
+                if (Sp.lost) stop = true;
+            }
+        }
+        if (warp == 0) s_tir[lane] = tir ? 1u : 0u;
+        else s_bound[lane] = Sp.lost ? 1u : 0u;
+        __syncthreads();
+        // lambda_setup_df breaks after a face's direction part that found total internal
+        // reflection, and before the face after one whose position part found a bound
+        // independent of y
+        if (warp == 0 && s_bound[lane]) stop = true;
+        if (warp == 1 && s_tir[lane]) stop = true;
+        __syncthreads();  // the flags are written again at the next face
+    }
+    if (warp == 1) s_pos[lane] = Sp;
+    __syncthreads();
+    if (warp == 1) return;
+    uint2 core = make_uint2(0u, 0u);
+    if (have) {
+        if (D.status) {
+            core = setup_failed_row(a, row);
+        } else {
+            Sp = s_pos[lane];
+            const float *z32 = stage_z ? sz : a.z32 + 2 * J.ray_off;
+            LamParams P;
+            zero_lam_params(P);
+            setup_tail(D, z32, J.Rz, P, a.lx + row, Sd, Sp, lost || Sp.lost);
+            core = setup_finish(a, 0u, (uint32_t)row, row, P);
+        }
+    }
+    // this block's 32 rows are the trace's block blockIdx.x
+    const bool any = core.y > core.x;
+    const uint32_t lo = __reduce_min_sync(0xffffffffu, any ? core.x : 0xffffffffu);
+    const uint32_t hi = __reduce_max_sync(0xffffffffu, any ? core.y : 0u);
+    if (lane == 0) {
+        const uint2 sp = hi > lo ? make_uint2(lo, hi) : make_uint2(0u, 0u);
+        a.spans[blockIdx.x] = sp;
+        if (sp.y > sp.x) atomicAdd(&a.ctl->item_counter, (unsigned long long)(sp.y - sp.x));
+    }
+}
+
 // Flagged rays a warp of the single-design trace keeps for its own re-trace.
 constexpr uint32_t kWarpFlags = 32;
 
@@ -1963,7 +2090,9 @@ int launch_pass(const LaunchArgs &a, int num_sms, uint32_t warps_per_cta, cudaSt
         // so spreading the rows over every SM matters
         const uint32_t blocks = (uint32_t)((a.total_rows + 31) / 32);
         const uint32_t cap = a.stage_cap < kStageRays ? a.stage_cap : kStageRays;
-        launch_k(setup_kernel, blocks, 32, 2 * ((cap + 1u) & ~1u) * sizeof(float), stream, false, a);
+        // a single-design pass (spans) splits each row's chain over two warps
+        launch_k(a.spans ? setup_pair_kernel : setup_kernel, blocks, a.spans ? 64 : 32,
+                 2 * ((cap + 1u) & ~1u) * sizeof(float), stream, false, a);
         launches++;
     }
     if (a.adaptive) {
