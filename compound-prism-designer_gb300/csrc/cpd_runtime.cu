@@ -94,9 +94,6 @@ constexpr uint32_t kSamplingBits = CPD_SAMPLING_ADAPTIVE | CPD_SAMPLING_EXACT;
 // Most rows of a pass whose trace takes equal shares of span slots: every warp scans the
 // blocks' spans (32 per step) to find its share.
 constexpr uint64_t kBalancedMaxRows = 16384;
-#ifndef CPD_TRACE_SPANS
-#define CPD_TRACE_SPANS 1  // 0: single-design passes take work items from the counter too
-#endif
 
 // The kernel node of `fn` in a captured graph (nullptr if none).
 cudaGraphNode_t find_kernel_node(cudaGraph_t g, const void *fn)
@@ -497,7 +494,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
     // shares per warp (no work-item counter, no tail of unequal items) and reads the
     // design's constants as kernel parameters. The bound on rows x rays keeps each warp's
     // share arithmetic in range.
-    if (CPD_TRACE_SPANS && n == 1 && !on_device && !adaptive && mode != CPD_TRACE_FP64 &&
+    if (n == 1 && !on_device && !adaptive && mode != CPD_TRACE_FP64 &&
         rows <= kBalancedMaxRows && rows * (uint64_t)jobs[0].Rz <= (1ull << 31)) {
         a.spans = reinterpret_cast<uint2 *>(S.lp.as<LamParams>() + rows);
         a.fc = ds[0].dev->fc;
