@@ -8,12 +8,20 @@
 //            chunk); lane = wavelength; FP32 exit face + detector per ray; hits
 //            accumulate per lane as run-length fixed-point sums (rays are sorted by
 //            start height, so consecutive rays mostly share a bin) flushed with one
-//            64-bit atomic per run; guard-band rays go to the queue
+//            64-bit atomic per run; guard-band rays go to the warp's list, which the warp
+//            re-traces itself (the global queue once the list is full)
 //   retrace  every queued ray: float-float re-trace (exact f64 in the FP64 study mode,
 //            bit-identical to the reference's f64 CPU trace)
-//   entropy  one warp per (design, row tile): p = sum/R, p log2 p, per-bin sums of p
-//            and p^2 in float-float with fixed-point accumulation (order independent)
-//   finalize one warp per design: H(D), MI, SEM convergence.
+//   entropy  one warp (many tiles) or one block (few) per (design, row tile): p = sum/R,
+//            p log2 p, per-bin sums of p and p^2 in float-float with fixed-point
+//            accumulation (order independent)
+//   finalize one warp per design: H(D), MI, SEM convergence (in a single-design pass the
+//            entropy block that completes the last tile runs it).
+// A single-design pass with a fixed ray count (the plain call) runs setup_pair_kernel (two
+// warps per 32 rows) and trace_spans_kernel (equal shares of the ray slots per warp, the
+// design's constants as kernel parameters) in place of the first two. Adaptive sampling
+// replaces trace and retrace with adaptive1_kernel / adaptive_kernel and
+// adaptive_exact_kernel.
 #include <cuda_runtime.h>
 
 #include "cpd_build.h"
