@@ -172,6 +172,26 @@ int orc_propagation_path(const orc_spec *s, double wavelength, double initial_y,
     return n;
 }
 
+int orc_stop_face(const orc_spec *s, double wavelength, double initial_y, int *status)
+{
+    spectrometer sp;
+    int e = build_spectrometer(s, &sp);
+    if (e) return -(100 + e);
+    const prism *cp = &sp.cp;
+    ray r = ray_start(initial_y);
+    double n1 = orc_calc_n(cp->glass[0], wavelength);
+    *status = plane_propagate(&r, &cp->planes[0], cp->height, 1.0, n1, cp->ar_coated);
+    if (*status != ORC_OK) return 0;
+    for (int k = 1; k < cp->nglass; k++) {
+        double n2 = orc_calc_n(cp->glass[k], wavelength);
+        *status = plane_propagate(&r, &cp->planes[k], cp->height, n1, n2, cp->ar_coated);
+        if (*status != ORC_OK) return k;
+        n1 = n2;
+    }
+    *status = curved_propagate(&r, cp, n1, 1.0, cp->ar_coated);
+    return *status != ORC_OK ? cp->nglass : -1;
+}
+
 /* vector_quasi_monte_carlo_integration + p_dets_l_wavelength (fitness.rs:5-34, 48-69).
  * Returns the rays consumed (the integration's final `count`). */
 static size_t p_dets_adaptive(const spectrometer *sp, double w, size_t max_m, welford *stats)

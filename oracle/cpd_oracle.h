@@ -91,6 +91,12 @@ int orc_design_dump(const orc_spec *s, double *out);
  * (G+3) rows of (origin x, origin y, dir x, dir y); returns the row count. */
 int orc_propagation_path(const orc_spec *s, double wavelength, double initial_y, double *rows);
 
+/* The face at which the prism trace of propagate_trace (ray.rs:501-541) stops for this
+ * wavelength and start height: 0..G-1 for the flat faces (0 = entrance), G for the curved
+ * exit face, -1 when the ray leaves through the exit face; *status = the stopping error
+ * (ORC_OK when it leaves). Negative build errors are returned as -(100 + e). */
+int orc_stop_face(const orc_spec *s, double wavelength, double initial_y, int *status);
+
 /* fitness() (src/fitness.rs:130-147) with the reference's adaptive SEM stops.
  * out = {size, info, deviation}. */
 int orc_fitness_adaptive(const orc_spec *s, size_t max_n, size_t max_m, double out[3]);

@@ -84,6 +84,7 @@ def lib():
         L.orc_propagate.argtypes = [sp, C.c_double, C.c_double, up, dp]
         L.orc_design_dump.argtypes = [sp, dp]
         L.orc_propagation_path.argtypes = [sp, C.c_double, C.c_double, dp]
+        L.orc_stop_face.argtypes = [sp, C.c_double, C.c_double, C.POINTER(C.c_int)]
         L.orc_fitness_adaptive.argtypes = [sp, C.c_size_t, C.c_size_t, dp]
         L.orc_fitness_adaptive_work.argtypes = [sp, C.c_size_t, C.c_size_t, dp, C.POINTER(C.c_uint64),
                                                 C.POINTER(C.c_uint64)]
@@ -198,6 +199,16 @@ def propagation_path(d: dict, wavelength: float, initial_y: float) -> np.ndarray
     rows = np.zeros((G + 3, 4))
     n = lib().orc_propagation_path(C.byref(s), float(wavelength), float(initial_y), _dp(rows))
     return rows[: max(n, 0)]
+
+
+def stop_face(d: dict, wavelength: float, initial_y: float):
+    """(face, status): where the prism trace of this wavelength and start height stops
+    (0..G-1 the flat faces, G the curved exit face, -1 none) and the error it stops with."""
+    s = make_spec(d)
+    st = C.c_int(0)
+    k = lib().orc_stop_face(C.byref(s), float(wavelength), float(initial_y), C.byref(st))
+    assert k >= -1, k
+    return k, st.value
 
 
 def fitness_adaptive(d: dict, max_n: int = 16384, max_m: int = 16384):

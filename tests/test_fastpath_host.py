@@ -61,3 +61,22 @@ def test_random_designs(fastpath_bin, tmp_path):
         # adaptive sampling's decision guard (kTqDelta = 2 quanta of 2^-20) assumes the
         # fast path's transmittance error stays below 2^-19 ~ 1.9e-6; keep a margin
         assert r["fast_t_relerr_e9"] < 1000, (G, B, r)
+
+
+@pytest.mark.parametrize("name", ["flat_face_tir_mid", "flat_face_tir_last"])
+def test_rows_lost_at_a_flat_face(fastpath_bin, tmp_path, name):
+    """Part of the band is lost to total internal reflection at a flat face: the per-row
+    setup must drop exactly those rows, and decide the rest like the exact trace."""
+    import oracle as O
+
+    case = json.load(open(os.path.join(GOLDEN, "regression_designs.json")))[name]
+    spec = synth.spectrometer_from_dict(case["design"])
+    pts = case["points"]
+    lam_all = O.gpu_points(pts["seed"], pts["wavelengths"])
+    lost = np.zeros(lam_all.size, dtype=bool)
+    lost[case["tir_rows"]] = True
+    sel = np.arange(0, lam_all.size, 4)
+    ray_u = O.gpu_points(pts["seed"], 256, first=pts["ray_first"])
+    r = _run(fastpath_bin, tmp_path, spec, lam_all[sel], ray_u)
+    assert lost[sel].any() and not lost[sel].all()
+    assert r["mismatches"] == 0 and r["outside_band_hits"] == 0 and r["df_mismatches"] == 0, r

@@ -236,3 +236,37 @@ def test_detector_size_extremes(B):
     po, st, counts = O.fitness_adaptive_points(d, lam_u, ray_u, nthreads=NTHREADS)
     assert fa.rays == int(counts.sum()) and fa.hits == st["hits"]
     assert np.abs(p - po).max() <= 1e-6
+
+
+@pytest.mark.parametrize("name", ["flat_face_tir_mid", "flat_face_tir_last"])
+def test_rows_lost_at_a_flat_face(name):
+    """Designs that lose part of the band to total internal reflection at a flat face
+    (face 2 of 4 prisms; face 5, the last flat face, of 6). The single-design pass sets up
+    each row on two warps, the direction warp stopping the position warp at the lost face;
+    the multi-design pass sets up each row on one warp. Both must give the same bits, the
+    oracle's lost rows must be empty on the GPU too, and the rest must meet the parity
+    bounds (hybrid) and the fixed-point quantum (FP64 trace)."""
+    import json
+
+    from conftest import GOLDEN
+
+    case = json.load(open(os.path.join(GOLDEN, "regression_designs.json")))[name]
+    d = case["design"]
+    spec = synth.spectrometer_from_dict(d)
+    pts = case["points"]
+    W, R, seed = pts["wavelengths"], pts["rays"], pts["seed"]
+    rows = case["tir_rows"]
+    assert 0 < len(rows) < W
+    single = spec.gpu_fitness_full([seed], max_n=W, max_eval=R)
+    for o in cpd.fitness_batch([spec, spec], seeds=seed, max_n=W, max_eval=R):
+        assert o.info == single.info and o.hits == single.hits and o.retraced == single.retraced
+    lam_u, ray_u = O.gpu_points(seed, W), O.gpu_points(seed, R, first=pts["ray_first"])
+    f, p = spec.gpu_fitness_points(lam_u, ray_u, want_p=True)
+    assert f.info == single.info and f.hits == single.hits
+    po, st = O.fitness_points(d, lam_u, ray_u, nthreads=NTHREADS)
+    assert st["hits"] > 0 and not po[rows].any() and not p[rows].any()
+    assert np.abs(p - po).max() <= 1e-6
+    assert abs(f.info - st["info"]) <= 1e-4 * abs(st["info"]) + 1e-9
+    assert f.hits == st["hits"]
+    f64, p64 = spec.gpu_fitness_points(lam_u, ray_u, mode=cpd.TRACE_FP64, want_p=True)
+    assert np.abs(p64 - po).max() <= 2.0 ** -32 and f64.hits == st["hits"]
