@@ -120,6 +120,10 @@ struct LaunchArgs {
     // the ray loop.
     FastConst fc;
     FastLimits fl;
+    // The design's job record when `spans` is set (jobs[0]), a kernel parameter: the
+    // setup's first loads (the wavelength point, the design record, the z table) then
+    // do not wait for a load of the job.
+    DesignJob one;
     // The setup stages a design's sorted z table in shared memory when it has at most
     // stage_cap rays (at most kStageRays; 0: none); the setup's blocks get
     // 8 * even(stage_cap) bytes, so a pass whose tables are small or not staged at all does

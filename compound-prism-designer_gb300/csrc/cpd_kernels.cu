@@ -259,21 +259,26 @@ __global__ void __launch_bounds__(64) setup_pair_kernel(const LaunchArgs a)
     __shared__ SetupPos s_pos[32];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint64_t row = blockIdx.x * 32ull + lane;
-    const DesignJob &J = a.jobs[0];
+    const DesignJob &J = a.one;
     const bool have = row < a.total_rows;
     const bool stage_z = J.Rz <= a.stage_cap;
     const double u = have && warp == 0 ? a.lam_u[J.lam_off + row] : 0.0;
     {
+        // two groups of copies: the design record, which the face loop needs, and the z
+        // table, which only the ray ranges after the loop read (its copies land while the
+        // faces run)
         const char *src = reinterpret_cast<const char *>(a.designs);
         char *dst = reinterpret_cast<char *>(&sD);
         for (uint32_t i = threadIdx.x; i < sizeof(DevDesign) / 16; i += blockDim.x) cp_async16(dst + 16 * i, src + 16 * i);
+        asm volatile("cp.async.commit_group;" ::: "memory");
         if (stage_z) {
             const char *zs = reinterpret_cast<const char *>(a.z32 + 2 * J.ray_off);
             char *zd = reinterpret_cast<char *>(sz);
             const uint32_t n16 = (J.Rz + 1u) / 2u;  // 16-byte chunks (two rays each)
             for (uint32_t i = threadIdx.x; i < n16; i += blockDim.x) cp_async16(zd + 16 * i, zs + 16 * i);
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
     }
     __syncthreads();
     const DevDesign &D = sD;
@@ -318,6 +323,7 @@ __global__ void __launch_bounds__(64) setup_pair_kernel(const LaunchArgs a)
         __syncthreads();  // the flags are written again at the next face
     }
     if (warp == 1) s_pos[lane] = Sp;
+    asm volatile("cp.async.wait_all;" ::: "memory");  // this thread's share of the z table
     __syncthreads();
     if (warp == 1) return;
     uint2 core = make_uint2(0u, 0u);

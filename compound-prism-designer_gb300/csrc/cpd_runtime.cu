@@ -499,6 +499,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         a.spans = reinterpret_cast<uint2 *>(S.lp.as<LamParams>() + rows);
         a.fc = ds[0].dev->fc;
         a.fl = fast_limits(a.fc, a.guards);
+        a.one = jobs[0];
     }
     a.p_out = p_out_host ? S.pout.as<double>() : nullptr;
     a.logtab = ctx->logtab.as<float>();
