@@ -7,6 +7,10 @@
 #include "cpd_ff.h"
 #include "cpd_model.h"
 
+#ifndef CPD_TILE_CELLS_BATCH
+#define CPD_TILE_CELLS_BATCH 2048
+#endif
+
 namespace cpd {
 
 // One design in a launch sequence. Offsets index the launch's shared buffers.
@@ -82,8 +86,12 @@ struct DesignOut {
     int32_t status;          // the design record's status (a device build's error)
 };
 
-// Cells per entropy tile (one warp): a design's tile is max(1, kTileCells / B) rows.
+// Cells per entropy tile: a design's tile is max(1, cells / B) rows, kTileCells for a
+// single-design pass (one CTA per tile: more tiles, more SMs busy on its short tail) and
+// kTileCellsBatch for passes of several designs (one warp per tile, many tiles: fewer,
+// larger tiles spend less on each tile's job lookup and per-bin atomics).
 constexpr uint32_t kTileCells = 512;
+constexpr uint32_t kTileCellsBatch = CPD_TILE_CELLS_BATCH;
 
 struct LaunchArgs {
     const DevDesign *designs;

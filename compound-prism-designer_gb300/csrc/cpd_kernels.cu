@@ -1307,7 +1307,7 @@ __device__ __forceinline__ void entropy_tile(const LaunchArgs &a, const DesignJo
 // WITH_P: the pass also writes p(d|lambda) (a.p_out); a kernel of its own, so that the
 // f64 conversion of every cell is not issued when nobody reads it.
 template <bool WITH_P>
-__global__ void __launch_bounds__(kEntropyThreads, 2) entropy_warp_kernel(const LaunchArgs a)
+__global__ void __launch_bounds__(kEntropyThreads, 4) entropy_warp_kernel(const LaunchArgs a)
 {
     __shared__ float tab[4 * ff::kLogTable];
     cudaTriggerProgrammaticLaunchCompletion();

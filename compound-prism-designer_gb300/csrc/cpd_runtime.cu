@@ -287,7 +287,10 @@ struct PassResult {
     bool overflow = false;
 };
 
-uint32_t tile_rows_for(uint32_t B) { return std::max<uint32_t>(1u, kTileCells / B); }
+uint32_t tile_rows_for(uint32_t B, uint32_t n)
+{
+    return std::max<uint32_t>(1u, (n > 1 ? kTileCellsBatch : kTileCells) / B);
+}
 
 // Device bytes one design occupies in a pass (histogram, per-row tables, ray tables):
 // the admission unit of the server.
@@ -350,7 +353,7 @@ int pass_issue(cpd_context *ctx, PassSlot &S, const std::vector<PassDesign> &ds,
         J.item_off = items;
         J.tile_off = tiles;
         J.nchunk = std::max<uint32_t>(1u, (J.Rz + ctx->ray_tile - 1) / ctx->ray_tile);
-        J.tile_rows = tile_rows_for(J.B);
+        J.tile_rows = tile_rows_for(J.B, n);
         J.ntiles = (J.W + J.tile_rows - 1) / J.tile_rows;
         ff::split(kTScaleInv / (double)J.R, J.unit_hi, J.unit_lo);
         ff::split(-31.0 - std::log2((double)J.R), J.lu_hi, J.lu_lo);
