@@ -63,7 +63,7 @@ SFU_PER_FAST_RAY = 5
 # launch of this workload, from the ncu capture summarised in
 # profiles/fitness_pass_plain_g6_b64_w4096_r1024.md (the figure is copied here when the
 # kernel is re-profiled; bench.py reads no profile file).
-TRACE_TRAFFIC_BYTES = 3046400
+TRACE_TRAFFIC_BYTES = 3045888
 
 
 def dist_info():
