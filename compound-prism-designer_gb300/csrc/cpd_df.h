@@ -338,7 +338,8 @@ CPD_HDN inline bool setup_tail(const DevDesign &D, const float *z32, uint32_t R,
     const F2 L0 = Sp.L0, L1 = Sp.L1, U0 = Sp.U0, U1 = Sp.U1;
     const F2 ylo = L1.hi > 0.f ? neg(div(L0, L1)) : c(-kBig), yhi = U1.hi > 0.f ? div(U0, U1) : c(kBig);
     const float glo = L1.hi > 0.f ? Sp.Lg / L1.hi : 0.f, ghi = U1.hi > 0.f ? Sp.Ug / U1.hi : 0.f;
-    if (E) {
+    auto write_e = [&]() {
+        if (!E) return;
         E->ylo = ylo;
         E->yhi = yhi;
         E->ax = Sp.ax;
@@ -354,8 +355,11 @@ CPD_HDN inline bool setup_tail(const DevDesign &D, const float *z32, uint32_t R,
         E->ts_lo = Sd.ts.lo;
         E->tp_lo = Sd.tp.lo;
         E->pad = 0u;
+    };
+    if (lost) {
+        write_e();
+        return false;
     }
-    if (lost) return false;
     // Sorted-ray index ranges: y_j = bym - bw z_j is monotone in z, so the index of a
     // height threshold T is the number of z_j below (bym - T)/bw, counted on the (hi,
     // lo) table. The four counts are branch-free lower bounds stepping together: the
@@ -390,7 +394,10 @@ CPD_HDN inline bool setup_tail(const DevDesign &D, const float *z32, uint32_t R,
     if (C.bw.hi == 0.f) {
         // every ray starts at the same height
         const F2 y = C.bym;
-        if (lt(y, addf(ylo, -glo)) || lt(addf(yhi, ghi), y)) return false;
+        if (lt(y, addf(ylo, -glo)) || lt(addf(yhi, ghi), y)) {
+            write_e();
+            return false;
+        }
         if (lt(y, addf(ylo, glo)) || lt(addf(yhi, -ghi), y)) {
             P.band_lo = 0;
             P.core_lo = P.core_hi = 0;
@@ -422,6 +429,9 @@ CPD_HDN inline bool setup_tail(const DevDesign &D, const float *z32, uint32_t R,
     if (P.core_hi > P.core_lo &&
         !reference_ray_df(D, z32, P, Sp.ax, Sp.ay, Sp.bx, Sp.by, Sd.dx, Sd.dy, Sd.n1))
         P.all_exact = 1;
+    // the re-trace's record last: its scattered stores (one line per row and field) would
+    // otherwise queue ahead of the ray-range searches' loads
+    write_e();
     return P.band_hi > P.band_lo;
 }
 
